@@ -1,0 +1,298 @@
+"""Benchmark of the Debye hot path on GB300 (one JSON line on rank 0).
+
+Workload (the configuration the headline metric is quoted on): the full Debye
+forward I(q) of N = 20,000 bodies, 5 types, 201 q on [0, 0.5] 1/A (a compact
+seeded random-walk chain, Rg ~ 25 A).  One step = one full forward of that
+structure.  The unit of work is one pair*q term f_i f_j sinc(q r_ij) over the
+N(N-1)/2 unordered pairs.
+
+* ``value``   : pair*q/s with the bodies resident in HBM (kernels only), timed
+                with CUDA events on librsx's stream; L2 is flushed (a 256 MB
+                write) between timed steps, outside the events.
+* ``e2e``     : the same metric through the C ABI call a user makes
+                (rsx_debye_calc: host bodies in, host curve out, copies inside).
+* ``roofline``: the pair kernel's pair*q/s against the canonical peak of one
+                pair*q per 8 FP32 lane-ops (16 per clock per SM), taken from a
+                measured FMA rate of this GPU (rsx_measure_fp32_fma_rate).
+* ``cpu_baseline``: the reference's host_debye<double,float> loop (port in
+                oracle/, bit-identical to the compiled original on x86) on the
+                host cores, on a bounded q sample, extrapolated to all q.
+* ``extras``  : the other configurations' figures (incremental steps, SASA,
+                forward+adjoint, precision, batching) when their paths exist.
+
+With --gpus N under torchrun every rank computes its own independently seeded
+structure (weak scaling, no collective); value = all ranks' pair*q / max time.
+``--impl reference`` times the reference CPU path on the same config instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Debye Gpair·q/s (full forward, N=20000, Q=201)"
+UNIT = "Gpair·q/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--no-extras", action="store_true")
+    p.add_argument("--cpu-threads", type=int, default=0)
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline_forward(w, threads: int, q_sample: int | None = None):
+    """The reference host_debye<double,float> loop (oracle port) on a q sample:
+    full distance matrix + `q_sample` q values split over the threads; the
+    per-q cost is extrapolated to every q (the reference's cost is linear in Q
+    after the matrix)."""
+    from oracle import oracle
+    threads = threads or os.cpu_count() or 1
+    if q_sample is None:
+        q_sample = max(threads, 2)
+    sel = np.linspace(0, len(w.q) - 1, q_sample).round().astype(int)
+    t0 = time.perf_counter()
+    _, t_matrix = oracle.refport_host_debye(w.q[sel], w.bodies, w.ff[sel], threads=threads)
+    t_total = time.perf_counter() - t0
+    t_q = (t_total - t_matrix) / q_sample
+    t_full = t_matrix + t_q * len(w.q)
+    return {"value": w.pair_q / t_full / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"host_debye<double,float> port (N x N distance matrix + q loop) on "
+                      f"{q_sample} of {len(w.q)} q, {threads} threads; matrix {t_matrix:.2f} s, "
+                      f"{t_q:.2f} s per q, extrapolated to all q = {t_full:.1f} s per forward"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from resaxs_gb300 import workloads as W
+    w = W.make_config(2, seed=0)
+    threads = args.cpu_threads or os.cpu_count() or 1
+    vals = []
+    for s in range(args.warmup + args.steps):
+        cb = cpu_baseline_forward(w, threads, q_sample=threads)
+        if s >= args.warmup:
+            vals.append(cb["value"])
+        if s == 0 and args.steps + args.warmup > 2:
+            pass
+    v = statistics.median(vals)
+    cb["value"] = v
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": w.pair_q / (v * 1e9) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": W.CONFIG_NAMES[2], "n_bodies": w.n, "n_q": len(w.q),
+                       "n_types": w.ff.shape[1], "l2": "n/a (CPU)"},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    rank, world, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from resaxs_gb300 import _lib
+    from resaxs_gb300 import workloads as W
+    from resaxs_gb300.saxs import Debye
+
+    w = W.make_config(2, seed=rank)
+    d = Debye(w.q, w.ff, w.n, device=local, timing=True)
+    d.calc(w.bodies)                      # upload + first result
+    stream = torch.cuda.ExternalStream(_lib.lib().rsx_debye_stream(d.handle),
+                                       device=torch.device("cuda", local))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        d.forward_resident()
+        d.sync()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    kernel_ms = []
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    launches0 = _lib.launch_count()
+    t_wall0 = time.perf_counter()
+    for s in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(s))
+            ev[s][0].record(stream)
+        d.forward_resident()
+        with torch.cuda.stream(stream):
+            ev[s][1].record(stream)
+        d.sync()
+        kernel_ms.append(d.timing()[0])
+    barrier()
+    t_wall = time.perf_counter() - t_wall0
+    launches = _lib.launch_count() - launches0
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=f"cuda:{local}", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * w.pair_q * args.steps / (total_ms * 1e-3) / 1e9
+
+    # end to end through the C ABI with host buffers
+    e2e_steps = max(3, args.steps // 2)
+    d.calc(w.bodies)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        d.calc(w.bodies)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    if world > 1:
+        t = torch.tensor([e2e_s], device=f"cuda:{local}", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * w.pair_q / e2e_s / 1e9, "unit": UNIT,
+           "h2d_bytes_per_step": int(w.n * 16 + w.ff.nbytes),
+           "d2h_bytes_per_step": int(len(w.q) * 4)}
+
+    if rank == 0:
+        import ctypes
+        fma = ctypes.c_double()
+        _lib.check(_lib.lib().rsx_measure_fp32_fma_rate(local, ctypes.byref(fma)))
+        peak = fma.value / 8.0 / 1e9   # canonical: 16 pair*q per 128 FMA lane-ops
+        k_ms = statistics.median(kernel_ms)
+        achieved = w.pair_q / (k_ms * 1e-3) / 1e9
+        prof = os.path.join(ROOT, "profiles", "debye_forward_traffic.json")
+        traffic = None
+        if os.path.exists(prof):
+            traffic = json.load(open(prof)).get("dram_bytes_per_launch")
+        cfg = d.config()
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": W.CONFIG_NAMES[2], "n_bodies": w.n, "n_q": len(w.q),
+                       "n_types": w.ff.shape[1], "pair_q_per_step": w.pair_q,
+                       "l2": "flushed between steps (256 MB write, outside the timed events)",
+                       "q_slab": cfg["q_slab"], "work_items": cfg["n_items"],
+                       "uniform_q_recurrence": cfg["uniform_q"],
+                       "wall_s_timed_loop": t_wall},
+            "roofline": {"bound": "fp32_issue", "achieved": achieved, "peak": peak,
+                         "unit": UNIT, "frac": achieved / peak, "traffic": traffic,
+                         "kernel_ms": k_ms,
+                         "peak_source": "measured FP32 FMA rate of this GPU / 8 lane-ops "
+                                        "per pair*q (16 pair*q per clock per SM)",
+                         "fp32_fma_per_s": fma.value},
+            "e2e": e2e,
+            "gpu_launches": int(launches),
+            "clocks": clk,
+        }
+        threads = args.cpu_threads or os.cpu_count() or 1
+        try:
+            line["cpu_baseline"] = cpu_baseline_forward(w, threads, q_sample=threads)
+        except Exception as e:  # report, do not hide
+            line["cpu_baseline"] = {"value": None, "error": repr(e)}
+        if not args.no_extras:
+            try:
+                from resaxs_gb300 import bench_extras
+                line["extras"] = bench_extras.run_all(local)
+            except ImportError:
+                pass
+        print(json.dumps(line), flush=True)
+    d.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

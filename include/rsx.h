@@ -1,0 +1,181 @@
+/*
+ * rsx.h -- C ABI of librsx, the GB300-native (sm_103a) Debye / incremental
+ * recalculation / dot-sphere SASA path of resaxslib.
+ *
+ * Plain C types only: pointers to host memory, sizes and int status codes.
+ * Every entry point names the reference interface it replaces
+ * (paths relative to the ldantonov/resaxs tree).
+ *
+ * Body layout (same bytes as the reference's cl_float4 bodies,
+ * resaxslib/include/utils.hpp:61-88): 4 floats per body, x y z and the
+ * uint32 form-factor type index stored bit-for-bit in the 4th float.
+ * Form-factor tables are row-major [n_q][n_factors]
+ * (resaxslib/src/host_debye.cpp:64-72).
+ *
+ * Threading: a handle is used by one host thread at a time; each handle owns
+ * one CUDA stream on one device.  All calls that take host output pointers
+ * return after the result is in host memory.
+ */
+#ifndef RSX_H
+#define RSX_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RSX_VERSION_MAJOR 1
+#define RSX_VERSION_MINOR 0
+
+/* Status codes.  -1..-6 are the reference's resaxs::error codes
+ * (resaxslib/include/resaxs.hpp:212-220) with the same meaning. */
+typedef int rsx_status;
+#define RSX_OK 0
+#define RSX_INVALID_DEVICE -1      /* no usable CUDA device / wrong device */
+#define RSX_ALG_NOT_INITIALIZED -2 /* handle not created / destroyed */
+#define RSX_INVALID_ARG -3         /* bad pointer, size, index or type */
+#define RSX_PROGRAM_NOT_LOADED -4  /* kernels not available for this GPU */
+#define RSX_ARGS_NOT_SET -5        /* required parameters missing */
+#define RSX_NO_INITIAL_CALC -6     /* recalc/commit/revert/backward before calc */
+#define RSX_CUDA_ERROR -100        /* a CUDA runtime call failed */
+#define RSX_OUT_OF_MEMORY -101     /* device or pinned allocation failed */
+#define RSX_TIMEOUT -102           /* a bounded device-side wait gave up */
+#define RSX_NOT_SUPPORTED -103     /* valid request this build does not implement */
+#define RSX_INJECTED_FAULT -104    /* failure produced by the host fault-injection hook */
+
+/* Body as 4 floats (x, y, z, type bits). */
+typedef struct rsx_body {
+    float x, y, z, w;
+} rsx_body;
+
+/* Library-level calls ------------------------------------------------- */
+
+/* "major.minor cuda-runtime device" string; never NULL. */
+const char *rsx_version(void);
+/* Message of the last failing call on this host thread ("" if none). */
+const char *rsx_last_error(void);
+/* Kernels launched by this process through librsx so far. */
+unsigned long long rsx_launch_count(void);
+/* Host-side fault injection for tests: the n-th subsequent device allocation
+ * or kernel launch inside librsx (counting from 1) fails with
+ * RSX_INJECTED_FAULT; 0 disables.  kind: 0 = allocation, 1 = launch. */
+void rsx_debug_inject_fault(int kind, int nth);
+
+/* Measures the sustained FP32 FMA rate of `device` (-1 = current) with a
+ * register-resident FMA-chain kernel on every SM: *fma_per_s = lane FMAs per
+ * second.  The denominator of the pair*q roofline. */
+rsx_status rsx_measure_fp32_fma_rate(int device, double *fma_per_s);
+
+/* C-style function-pointer ABI: same signature and semantics as
+ * resaxs::CalcSaxsCurveFn (resaxslib/include/host_debye.hpp:30), i.e.
+ * host_debye<...>::calc_curve (resaxslib/src/host_debye.cpp:54-109), computed
+ * on the current CUDA device.  Errors are reported through rsx_last_error()
+ * (the reference signature has no status); out_v_Iq is left untouched then. */
+void rsx_calc_saxs_curve(const float *v_q, int n_q, const rsx_body *v_bodies, int n_bodies,
+                         const float *t_factors, int n_factors, float *out_v_Iq);
+/* Same computation returning a status. */
+rsx_status rsx_calc_saxs_curve_status(const float *v_q, int n_q, const rsx_body *v_bodies,
+                                      int n_bodies, const float *t_factors, int n_factors,
+                                      float *out_v_Iq);
+
+/* Debye algorithm handle: replaces resaxs::algorithm::i_saxs<float, cl_base>
+ * implemented by saxs_cl_gpu<float> (resaxslib/include/saxs_algorithm.hpp:147-183,
+ * resaxslib/src/saxs_alg_cl_gpu_pt_wf.cpp) ----------------------------- */
+
+typedef struct rsx_debye rsx_debye;
+
+typedef struct rsx_debye_options {
+    int device;          /* CUDA ordinal; -1 = current device */
+    int q_slab;          /* q values per CTA slab: 8, 16, 32; 0 = tuned / default */
+    int max_items;       /* cap on forward work items (scratch = items*n_q*8 B); 0 = default */
+    int force_general_q; /* 1: never use the uniform-grid recurrence */
+    int timing;          /* 1: record CUDA events around the pair kernel */
+    int autotune;        /* 1: time the q-slab candidates on first use and cache the winner */
+} rsx_debye_options;
+
+/* Fills the defaults (device -1, everything else 0). */
+void rsx_debye_default_options(rsx_debye_options *opts);
+
+/* saxs_params::initialize(qq, bodies, devices, wf) + saxs_cl_gpu::initialize()
+ * (saxs_algorithm.hpp:124-132; saxs_alg_cl_gpu_pt_wf.cpp:176-263): q vector,
+ * form-factor table [n_q][n_factors] and body count are fixed for the handle.
+ * opts may be NULL. */
+rsx_status rsx_debye_create(const float *q, int n_q, const float *t_factors, int n_factors,
+                            int n_bodies, const rsx_debye_options *opts, rsx_debye **out);
+/* delete of the algorithm object (re_algorithm.hpp:33). NULL is a no-op. */
+rsx_status rsx_debye_destroy(rsx_debye *h);
+
+/* form_factor_params::access_factors()/set_expansion_factor() then a dirty
+ * params flag (saxs_algorithm.hpp:79-109; saxs_alg_cl_gpu_pt_wf.cpp:479-495):
+ * replaces the table; the next recalc does a full recompute. */
+rsx_status rsx_debye_set_factors(rsx_debye *h, const float *t_factors, int n_factors);
+
+/* implicit_water_params (saxs_algorithm.hpp:55-77) + water_ff_index:
+ * f_i(q) = F[q][t_i] + rsasa_i * F[q][water_index] * weight
+ * (gpu_saxs_pt_wf.cl:130-138).  rsasa (n_bodies floats, caller order) may be
+ * NULL to keep the current values (initially 0).  Marks params dirty. */
+rsx_status rsx_debye_set_water(rsx_debye *h, float weight, int water_index, const float *rsasa);
+
+/* i_saxs::calc_curve (saxs_algorithm.hpp:162; saxs_alg_cl_gpu_pt_wf.cpp:414-458):
+ * full I(q) of n_bodies bodies. */
+rsx_status rsx_debye_calc(rsx_debye *h, const rsx_body *bodies, float *out_iq);
+
+/* i_saxs::recalc_curve (saxs_algorithm.hpp:172; saxs_alg_cl_gpu_pt_wf.cpp:468-577):
+ * bodies is the full caller vector; bodies [upd_start, upd_start+upd_length)
+ * moved.  Computed incrementally (delta of the moved pairs, FP64 running
+ * totals); a full recompute when params are dirty or most bodies moved. */
+rsx_status rsx_debye_recalc_range(rsx_debye *h, const rsx_body *bodies, unsigned upd_start,
+                                  unsigned upd_length, float *out_iq);
+
+/* Incremental recalc for an arbitrary moved set (no reference counterpart;
+ * the reference accepts one contiguous range only): moved[m] is the new body
+ * of caller index idx[m]; indices must be distinct and types unchanged. */
+rsx_status rsx_debye_recalc_indices(rsx_debye *h, const rsx_body *moved, const unsigned *idx,
+                                    unsigned k, float *out_iq);
+
+/* i_saxs::commit / revert (saxs_algorithm.hpp:177-182;
+ * saxs_alg_cl_gpu_pt_wf.cpp:592-620): checkpoint / restore positions, water
+ * factors and the FP64 running curve.  revert before any commit is a no-op,
+ * as in the reference. */
+rsx_status rsx_debye_commit(rsx_debye *h);
+rsx_status rsx_debye_revert(rsx_debye *h);
+
+/* FP64 running curve held on the device (after calc/recalc). */
+rsx_status rsx_debye_curve_f64(rsx_debye *h, double *out_iq);
+
+/* Recompute I(q) from the bodies already on the device (no host copies),
+ * leaving the result on the device; used to time the resident path.
+ * rsx_debye_sync waits for it. */
+rsx_status rsx_debye_forward_resident(rsx_debye *h);
+rsx_status rsx_debye_sync(rsx_debye *h);
+
+/* The handle's cudaStream_t (as an opaque pointer) for callers that record
+ * their own events or order their own work against librsx. */
+void *rsx_debye_stream(rsx_debye *h);
+
+/* Milliseconds of the last pair kernel and of the last whole call, measured
+ * with CUDA events on the handle's stream (options.timing = 1). */
+rsx_status rsx_debye_timing(rsx_debye *h, float *ms_pair_kernel, float *ms_call);
+
+/* Adjoint (no reference counterpart): given dL/dI(q) (n_q floats) for the
+ * curve of the last calc/recalc, writes dL/dx for every body
+ * (n_bodies x 3 floats, caller order) in one pair pass. */
+rsx_status rsx_debye_backward(rsx_debye *h, const float *dl_diq, float *grad_xyz);
+
+/* Same as rsx_debye_backward with the FP64 gradient. */
+rsx_status rsx_debye_backward_f64(rsx_debye *h, const float *dl_diq, double *grad_xyz);
+
+/* chi^2 = sum_q ((I(q) - target(q)) / sigma(q))^2 of the current curve and its
+ * gradient dchi^2/dx (the loss of saxs_profile::chi_square_chi,
+ * resaxslib/include/saxs_profile.hpp:154-166, with unit scale). */
+rsx_status rsx_debye_chi2_backward(rsx_debye *h, const float *target, const float *sigma,
+                                   double *chi2, float *grad_xyz);
+
+/* Tuning in effect: q-slab, work items, whether the uniform-q recurrence is used. */
+rsx_status rsx_debye_config(rsx_debye *h, int *q_slab, int *n_items, int *uniform_q);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RSX_H */

@@ -1,0 +1,14 @@
+#!/bin/sh
+# Builds the reference's CPU Debye path (resaxslib/src/host_debye.cpp, unmodified)
+# from the read-only reference tree into oracle/_ref/.  Test infrastructure only.
+# Usage: oracle/build_ref.sh [reference_root]   (default /root/reference)
+set -e
+REF=${1:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+[ -f "$REF/resaxslib/src/host_debye.cpp" ] || { echo "reference not found at $REF" >&2; exit 3; }
+mkdir -p "$HERE/_ref"
+g++ -std=c++14 -O2 -shared -fPIC -w \
+    -I "$HERE/shim" -I "$REF/resaxslib/include" \
+    "$HERE/ref_wrap.cpp" "$REF/resaxslib/src/host_debye.cpp" \
+    -o "$HERE/_ref/libref_host_debye.so"
+echo "built $HERE/_ref/libref_host_debye.so"

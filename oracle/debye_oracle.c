@@ -1,0 +1,477 @@
+/*
+ * CPU oracle for the Debye sum -- TEST INFRASTRUCTURE ONLY (see rsx_oracle.h).
+ * Restates resaxslib/src/host_debye.cpp:54-109 in FP64, plus its gradient.
+ */
+#include "rsx_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+
+static unsigned body_type(const float *bodies, int i)
+{
+    unsigned t;
+    memcpy(&t, &bodies[4 * i + 3], sizeof t); /* utils.hpp:61-66 */
+    return t;
+}
+
+static int pick_threads(int n)
+{
+    if (n > 0)
+        return n;
+    long c = sysconf(_SC_NPROCESSORS_ONLN);
+    return c > 0 ? (int)c : 1;
+}
+
+/* effective factor, gpu_saxs_pt_wf.cl:130-138 (in FP64) */
+static double eff_factor(const float *ff, int n_factors, int k, unsigned t,
+                         const float *rsasa, double ww, int water_index, int i)
+{
+    double f = ff[(size_t)k * n_factors + t];
+    if (rsasa)
+        f += (double)rsasa[i] * ((double)ff[(size_t)k * n_factors + water_index] * ww);
+    return f;
+}
+
+/* ---------------- direct FP64 Debye, parallel over rows ---------------- */
+
+typedef struct {
+    const double *q;
+    int n_q;
+    const float *bodies;
+    int n;
+    const double *f; /* [n_q][n] effective factors */
+    int next_row;    /* shared work counter (guarded by mu) */
+    pthread_mutex_t mu;
+    double *acc; /* [n_threads][n_q] */
+} debye_job;
+
+typedef struct {
+    debye_job *job;
+    int tid;
+} debye_arg;
+
+static int grab_rows(pthread_mutex_t *mu, int *next, int limit, int chunk, int *begin)
+{
+    pthread_mutex_lock(mu);
+    int b = *next;
+    int e = b + chunk > limit ? limit : b + chunk;
+    *next = e;
+    pthread_mutex_unlock(mu);
+    *begin = b;
+    return e;
+}
+
+static void *debye_worker(void *p)
+{
+    debye_arg *a = (debye_arg *)p;
+    debye_job *J = a->job;
+    double *acc = J->acc + (size_t)a->tid * J->n_q;
+    double *inner = (double *)calloc((size_t)J->n_q, sizeof(double));
+    for (;;) {
+        int b;
+        int e = grab_rows(&J->mu, &J->next_row, J->n, 16, &b);
+        if (b >= e)
+            break;
+        for (int y = b; y < e; ++y) {
+            const float *py = &J->bodies[4 * y];
+            for (int k = 0; k < J->n_q; ++k)
+                inner[k] = 0.0;
+            for (int x = 0; x < y; ++x) {
+                const float *px = &J->bodies[4 * x];
+                double dx = (double)px[0] - py[0];
+                double dy = (double)px[1] - py[1];
+                double dz = (double)px[2] - py[2];
+                double r = sqrt(dx * dx + dy * dy + dz * dz);
+                for (int k = 0; k < J->n_q; ++k) {
+                    double qr = J->q[k] * r;
+                    double s = (qr == 0.0) ? 1.0 : sin(qr) / qr;
+                    inner[k] += J->f[(size_t)k * J->n + x] * s;
+                }
+            }
+            for (int k = 0; k < J->n_q; ++k)
+                acc[k] += inner[k] * J->f[(size_t)k * J->n + y];
+        }
+    }
+    free(inner);
+    return NULL;
+}
+
+void orc_debye_f64(const double *q, int n_q, const float *bodies, int n_bodies,
+                   const float *ff, int n_factors, const float *rsasa,
+                   double water_weight, int water_index, double *out_iq,
+                   int n_threads)
+{
+    int nt = pick_threads(n_threads);
+    double *f = (double *)malloc(sizeof(double) * (size_t)n_q * n_bodies);
+    for (int k = 0; k < n_q; ++k)
+        for (int i = 0; i < n_bodies; ++i)
+            f[(size_t)k * n_bodies + i] = eff_factor(ff, n_factors, k, body_type(bodies, i),
+                                                     rsasa, water_weight, water_index, i);
+    debye_job J;
+    J.q = q;
+    J.n_q = n_q;
+    J.bodies = bodies;
+    J.n = n_bodies;
+    J.f = f;
+    J.next_row = 0;
+    pthread_mutex_init(&J.mu, NULL);
+    J.acc = (double *)calloc((size_t)nt * n_q, sizeof(double));
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nt);
+    debye_arg *args = (debye_arg *)malloc(sizeof(debye_arg) * nt);
+    for (int t = 0; t < nt; ++t) {
+        args[t].job = &J;
+        args[t].tid = t;
+        pthread_create(&th[t], NULL, debye_worker, &args[t]);
+    }
+    for (int t = 0; t < nt; ++t)
+        pthread_join(th[t], NULL);
+    for (int k = 0; k < n_q; ++k) {
+        double cross = 0.0, self = 0.0;
+        for (int t = 0; t < nt; ++t)
+            cross += J.acc[(size_t)t * n_q + k];
+        for (int i = 0; i < n_bodies; ++i) {
+            double fi = f[(size_t)k * n_bodies + i];
+            self += fi * fi; /* autologous terms, host_debye.cpp:85 */
+        }
+        out_iq[k] = 2.0 * cross + self; /* host_debye.cpp:106-107 */
+    }
+    pthread_mutex_destroy(&J.mu);
+    free(J.acc);
+    free(th);
+    free(args);
+    free(f);
+}
+
+/* ------------- FP64 rotation form for a uniform q grid ------------------ */
+
+typedef struct {
+    double q0, dq;
+    int n_q;
+    const float *bodies;
+    int n;
+    const float *ff;
+    int n_factors;
+    int next_row;
+    pthread_mutex_t mu;
+    double *acc; /* [n_threads][n_q] */
+} uni_job;
+
+typedef struct {
+    uni_job *job;
+    int tid;
+} uni_arg;
+
+static void *uni_worker(void *p)
+{
+    uni_arg *a = (uni_arg *)p;
+    uni_job *J = a->job;
+    int nq = J->n_q;
+    double *acc = J->acc + (size_t)a->tid * nq;
+    double *inner = (double *)calloc((size_t)nq, sizeof(double));
+    double *fq = (double *)malloc(sizeof(double) * nq);
+    for (;;) {
+        int b;
+        int e = grab_rows(&J->mu, &J->next_row, J->n, 8, &b);
+        if (b >= e)
+            break;
+        for (int y = b; y < e; ++y) {
+            const float *py = &J->bodies[4 * y];
+            for (int k = 0; k < nq; ++k)
+                inner[k] = 0.0;
+            for (int x = 0; x < y; ++x) {
+                const float *px = &J->bodies[4 * x];
+                unsigned tx = body_type(J->bodies, x);
+                double dx = (double)px[0] - py[0];
+                double dy = (double)px[1] - py[1];
+                double dz = (double)px[2] - py[2];
+                double r = sqrt(dx * dx + dy * dy + dz * dz);
+                if (r == 0.0) {
+                    for (int k = 0; k < nq; ++k)
+                        inner[k] += J->ff[(size_t)k * J->n_factors + tx];
+                    continue;
+                }
+                double s = sin(J->q0 * r) / r, c = cos(J->q0 * r) / r;
+                double sd = sin(J->dq * r), cd = cos(J->dq * r);
+                for (int k = 0; k < nq; ++k) {
+                    double qk = J->q0 + k * J->dq;
+                    double v = (qk == 0.0) ? 1.0 : s / qk;
+                    inner[k] += J->ff[(size_t)k * J->n_factors + tx] * v;
+                    double s2 = s * cd + c * sd;
+                    double c2 = c * cd - s * sd;
+                    s = s2;
+                    c = c2;
+                }
+            }
+            unsigned ty = body_type(J->bodies, y);
+            for (int k = 0; k < nq; ++k)
+                acc[k] += inner[k] * J->ff[(size_t)k * J->n_factors + ty];
+        }
+    }
+    free(fq);
+    free(inner);
+    return NULL;
+}
+
+void orc_debye_f64_uniform(double q0, double dq, int n_q, const float *bodies,
+                           int n_bodies, const float *ff_rows, int n_factors,
+                           double *out_iq, int n_threads)
+{
+    int nt = pick_threads(n_threads);
+    uni_job J;
+    J.q0 = q0;
+    J.dq = dq;
+    J.n_q = n_q;
+    J.bodies = bodies;
+    J.n = n_bodies;
+    J.ff = ff_rows;
+    J.n_factors = n_factors;
+    J.next_row = 0;
+    pthread_mutex_init(&J.mu, NULL);
+    J.acc = (double *)calloc((size_t)nt * n_q, sizeof(double));
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nt);
+    uni_arg *args = (uni_arg *)malloc(sizeof(uni_arg) * nt);
+    for (int t = 0; t < nt; ++t) {
+        args[t].job = &J;
+        args[t].tid = t;
+        pthread_create(&th[t], NULL, uni_worker, &args[t]);
+    }
+    for (int t = 0; t < nt; ++t)
+        pthread_join(th[t], NULL);
+    for (int k = 0; k < n_q; ++k) {
+        double cross = 0.0, self = 0.0;
+        for (int t = 0; t < nt; ++t)
+            cross += J.acc[(size_t)t * n_q + k];
+        for (int i = 0; i < n_bodies; ++i) {
+            double fi = ff_rows[(size_t)k * n_factors + body_type(bodies, i)];
+            self += fi * fi;
+        }
+        out_iq[k] = 2.0 * cross + self;
+    }
+    pthread_mutex_destroy(&J.mu);
+    free(J.acc);
+    free(th);
+    free(args);
+}
+
+/* ------------------------- FP64 gradient -------------------------------- */
+
+typedef struct {
+    const double *q, *w;
+    int n_q;
+    const float *bodies;
+    int n;
+    const double *f; /* [n_q][n] */
+    int next_row;
+    pthread_mutex_t mu;
+    double *grad;
+} grad_job;
+
+typedef struct {
+    grad_job *job;
+} grad_arg;
+
+static void *grad_worker(void *p)
+{
+    grad_job *J = ((grad_arg *)p)->job;
+    for (;;) {
+        int b;
+        int e = grab_rows(&J->mu, &J->next_row, J->n, 8, &b);
+        if (b >= e)
+            break;
+        for (int i = b; i < e; ++i) {
+            const float *pi = &J->bodies[4 * i];
+            double g[3] = {0.0, 0.0, 0.0};
+            for (int j = 0; j < J->n; ++j) {
+                if (j == i)
+                    continue;
+                const float *pj = &J->bodies[4 * j];
+                double d[3] = {(double)pi[0] - pj[0], (double)pi[1] - pj[1],
+                               (double)pi[2] - pj[2]};
+                double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+                double r = sqrt(r2);
+                if (r == 0.0)
+                    continue; /* derivative of sinc at 0 is 0 */
+                double G = 0.0;
+                for (int k = 0; k < J->n_q; ++k) {
+                    double qk = J->q[k];
+                    if (qk == 0.0)
+                        continue;
+                    double x = qk * r;
+                    double dsinc = cos(x) - sin(x) / x; /* x * d sinc/dx */
+                    G += J->w[k] * J->f[(size_t)k * J->n + i] * J->f[(size_t)k * J->n + j] * dsinc;
+                }
+                G *= 2.0 / r2;
+                g[0] += G * d[0];
+                g[1] += G * d[1];
+                g[2] += G * d[2];
+            }
+            J->grad[3 * i + 0] = g[0];
+            J->grad[3 * i + 1] = g[1];
+            J->grad[3 * i + 2] = g[2];
+        }
+    }
+    return NULL;
+}
+
+void orc_debye_grad_f64(const double *q, int n_q, const double *w_q,
+                        const float *bodies, int n_bodies, const float *ff,
+                        int n_factors, const float *rsasa, double water_weight,
+                        int water_index, double *grad, int n_threads)
+{
+    int nt = pick_threads(n_threads);
+    double *f = (double *)malloc(sizeof(double) * (size_t)n_q * n_bodies);
+    for (int k = 0; k < n_q; ++k)
+        for (int i = 0; i < n_bodies; ++i)
+            f[(size_t)k * n_bodies + i] = eff_factor(ff, n_factors, k, body_type(bodies, i),
+                                                     rsasa, water_weight, water_index, i);
+    grad_job J;
+    J.q = q;
+    J.w = w_q;
+    J.n_q = n_q;
+    J.bodies = bodies;
+    J.n = n_bodies;
+    J.f = f;
+    J.next_row = 0;
+    J.grad = grad;
+    pthread_mutex_init(&J.mu, NULL);
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nt);
+    grad_arg *args = (grad_arg *)malloc(sizeof(grad_arg) * nt);
+    for (int t = 0; t < nt; ++t) {
+        args[t].job = &J;
+        pthread_create(&th[t], NULL, grad_worker, &args[t]);
+    }
+    for (int t = 0; t < nt; ++t)
+        pthread_join(th[t], NULL);
+    pthread_mutex_destroy(&J.mu);
+    free(th);
+    free(args);
+    free(f);
+}
+
+/* ------------- reference-faithful port of host_debye -------------------- */
+
+/* distance<double>(a, b): host_debye.cpp:36-42 */
+static double port_distance(const float *a, const float *b)
+{
+    double dx = (double)a[0] - b[0];
+    double dy = (double)a[1] - b[1];
+    double dz = (double)a[2] - b[2];
+    return sqrt(dx * dx + dy * dy + dz * dz);
+}
+
+static void port_q_range(const float *v_q, int k0, int k1, int n_bodies,
+                         const double *r, const float *factors, float *out_v_iq)
+{
+    for (int k = k0; k < k1; k++) {
+        double q = v_q[k];
+        double Iq = 0;
+        const float *Fq = &factors[(size_t)k * n_bodies];
+        double auto_Iq = 0;
+        for (int y = 0; y < n_bodies; y++) {
+            double Fqy = Fq[y];
+            auto_Iq += Fqy * Fqy;
+            double inner_sum = 0;
+            for (int x = 0; x < y; x++) {
+                double v1 = 1;
+                if (q != 0) {
+                    double qr = q * r[(size_t)y * n_bodies + x];
+                    v1 = sin(qr) / qr; /* utils.hpp sinc */
+                }
+                inner_sum += Fq[x] * v1;
+            }
+            Iq += inner_sum * Fqy;
+        }
+        out_v_iq[k] = (float)(Iq * 2 + auto_Iq);
+    }
+}
+
+static double *port_matrix(const float *v_bodies, int n_bodies)
+{
+    double *r = (double *)malloc(sizeof(double) * (size_t)n_bodies * n_bodies);
+    if (!r)
+        return NULL;
+    for (int y = 1; y < n_bodies; y++)
+        for (int x = 0; x < y; x++)
+            r[(size_t)y * n_bodies + x] = port_distance(&v_bodies[4 * x], &v_bodies[4 * y]);
+    return r;
+}
+
+static float *port_factors(const float *v_bodies, int n_bodies, int n_q,
+                           const float *t_factors, int n_factors)
+{
+    float *factors = (float *)malloc(sizeof(float) * (size_t)n_q * n_bodies);
+    for (int k = 0; k < n_q; k++)
+        for (int i = 0; i < n_bodies; i++)
+            factors[(size_t)k * n_bodies + i] =
+                t_factors[(size_t)k * n_factors + body_type(v_bodies, i)];
+    return factors;
+}
+
+void orc_refport_host_debye(const float *v_q, int n_q, const float *v_bodies,
+                            int n_bodies, const float *t_factors, int n_factors,
+                            float *out_v_iq)
+{
+    double *r = port_matrix(v_bodies, n_bodies);
+    float *factors = port_factors(v_bodies, n_bodies, n_q, t_factors, n_factors);
+    port_q_range(v_q, 0, n_q, n_bodies, r, factors, out_v_iq);
+    free(factors);
+    free(r);
+}
+
+typedef struct {
+    const float *v_q;
+    int k0, k1, n;
+    const double *r;
+    const float *factors;
+    float *out;
+} port_arg;
+
+static void *port_worker(void *p)
+{
+    port_arg *a = (port_arg *)p;
+    port_q_range(a->v_q, a->k0, a->k1, a->n, a->r, a->factors, a->out);
+    return NULL;
+}
+
+#include <time.h>
+static double now_s(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+double orc_refport_host_debye_mt(const float *v_q, int n_q, const float *v_bodies,
+                                 int n_bodies, const float *t_factors,
+                                 int n_factors, float *out_v_iq, int n_threads)
+{
+    int nt = pick_threads(n_threads);
+    if (nt > n_q)
+        nt = n_q;
+    double t0 = now_s();
+    double *r = port_matrix(v_bodies, n_bodies);
+    double t_matrix = now_s() - t0;
+    float *factors = port_factors(v_bodies, n_bodies, n_q, t_factors, n_factors);
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nt);
+    port_arg *args = (port_arg *)malloc(sizeof(port_arg) * nt);
+    for (int t = 0; t < nt; ++t) {
+        args[t].v_q = v_q;
+        args[t].k0 = (int)((long)n_q * t / nt);
+        args[t].k1 = (int)((long)n_q * (t + 1) / nt);
+        args[t].n = n_bodies;
+        args[t].r = r;
+        args[t].factors = factors;
+        args[t].out = out_v_iq;
+        pthread_create(&th[t], NULL, port_worker, &args[t]);
+    }
+    for (int t = 0; t < nt; ++t)
+        pthread_join(th[t], NULL);
+    free(th);
+    free(args);
+    free(factors);
+    free(r);
+    return t_matrix;
+}

@@ -1,0 +1,159 @@
+"""ctypes loader for the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import
+this module.  The product library (``resaxs_gb300``) never does.
+
+``liboracle.so`` is the C restatement in this folder (debye_oracle.c,
+sasa_oracle.c); ``_ref/libref_host_debye.so`` is the reference's own
+``host_debye.cpp`` compiled by ``build_ref.sh`` where the reference tree exists.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libref_host_debye.so")
+
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+
+
+def build(cc: str = "gcc") -> str:
+    """Compile liboracle.so from the C restatement (seconds)."""
+    objs = []
+    for src, extra in (("debye_oracle.c", []), ("sasa_oracle.c", ["-ffp-contract=off"])):
+        obj = os.path.join(HERE, src.replace(".c", ".o"))
+        subprocess.check_call([cc, "-O2", "-fPIC", "-std=c11", "-D_GNU_SOURCE", *extra,
+                               "-c", os.path.join(HERE, src), "-o", obj])
+        objs.append(obj)
+    subprocess.check_call([cc, "-shared", *objs, "-o", LIB_PATH, "-lm", "-lpthread"])
+    for o in objs:
+        os.remove(o)
+    return LIB_PATH
+
+
+def build_ref(reference_root: str = "/root/reference") -> str | None:
+    """Compile the reference's host_debye.cpp into _ref/ when the tree exists."""
+    if not os.path.isfile(os.path.join(reference_root, "resaxslib", "src", "host_debye.cpp")):
+        return None
+    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), reference_root])
+    return REF_PATH
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        i, d, vp = ctypes.c_int, ctypes.c_double, ctypes.c_void_p
+        L.orc_debye_f64.argtypes = [_f64p, i, _f32p, i, _f32p, i, vp, d, i, _f64p, i]
+        L.orc_debye_f64_uniform.argtypes = [d, d, i, _f32p, i, _f32p, i, _f64p, i]
+        L.orc_debye_grad_f64.argtypes = [_f64p, i, _f64p, _f32p, i, _f32p, i, vp, d, i, _f64p, i]
+        L.orc_refport_host_debye.argtypes = [_f32p, i, _f32p, i, _f32p, i, _f32p]
+        L.orc_refport_host_debye_mt.argtypes = [_f32p, i, _f32p, i, _f32p, i, _f32p, i]
+        L.orc_refport_host_debye_mt.restype = d
+        L.orc_sasa_counts.argtypes = [_f32p, _f32p, i, _f32p, i, ctypes.c_float, _u32p, i, i]
+        L.orc_fibonacci_unit_dots.argtypes = [i, _f32p]
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The compiled reference host_debye, or None when it was not built."""
+    global _ref
+    if _ref is None and os.path.exists(REF_PATH):
+        L = ctypes.CDLL(REF_PATH)
+        i = ctypes.c_int
+        L.ref_host_debye_df.argtypes = [_f32p, i, _f32p, i, _f32p, i, _f32p]
+        L.ref_host_debye_ff.argtypes = [_f32p, i, _f32p, i, _f32p, i, _f32p]
+        L.ref_host_debye_dd.argtypes = [_f64p, i, _f64p, i, _f64p, i, _f64p]
+        _ref = L
+    return _ref
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def debye_f64(q, bodies, ff, rsasa=None, water_weight=0.0, water_index=0, threads=0):
+    """FP64 I(q) of float4 bodies (N,4 float32 with uint type bits in column 3)."""
+    q = _c(q, np.float64)
+    bodies = _c(bodies, np.float32)
+    ff = _c(ff, np.float32)
+    n_q, n_f = ff.shape
+    out = np.zeros(len(q), np.float64)
+    rs = None
+    if rsasa is not None:
+        rs_arr = _c(rsasa, np.float32)
+        rs = rs_arr.ctypes.data
+    lib().orc_debye_f64(q, len(q), bodies.reshape(-1), len(bodies), ff.reshape(-1), n_f,
+                        rs, float(water_weight), int(water_index), out, int(threads))
+    return out
+
+
+def debye_f64_uniform(q0, dq, n_q, bodies, ff, threads=0):
+    bodies = _c(bodies, np.float32)
+    ff = _c(ff, np.float32)
+    out = np.zeros(n_q, np.float64)
+    lib().orc_debye_f64_uniform(float(q0), float(dq), int(n_q), bodies.reshape(-1), len(bodies),
+                                ff.reshape(-1), ff.shape[1], out, int(threads))
+    return out
+
+
+def debye_grad_f64(q, w_q, bodies, ff, rsasa=None, water_weight=0.0, water_index=0, threads=0):
+    q = _c(q, np.float64)
+    w_q = _c(w_q, np.float64)
+    bodies = _c(bodies, np.float32)
+    ff = _c(ff, np.float32)
+    grad = np.zeros((len(bodies), 3), np.float64)
+    rs = None
+    if rsasa is not None:
+        rs_arr = _c(rsasa, np.float32)
+        rs = rs_arr.ctypes.data
+    lib().orc_debye_grad_f64(q, len(q), w_q, bodies.reshape(-1), len(bodies), ff.reshape(-1),
+                             ff.shape[1], rs, float(water_weight), int(water_index),
+                             grad.reshape(-1), int(threads))
+    return grad
+
+
+def refport_host_debye(q, bodies, ff, threads=1):
+    """Port of host_debye<double,float,cl_float4>; returns (I(q) float32, t_matrix_s)."""
+    q = _c(q, np.float32)
+    bodies = _c(bodies, np.float32)
+    ff = _c(ff, np.float32)
+    out = np.zeros(len(q), np.float32)
+    if threads == 1:
+        lib().orc_refport_host_debye(q, len(q), bodies.reshape(-1), len(bodies), ff.reshape(-1),
+                                     ff.shape[1], out)
+        return out, None
+    t = lib().orc_refport_host_debye_mt(q, len(q), bodies.reshape(-1), len(bodies),
+                                        ff.reshape(-1), ff.shape[1], out, int(threads))
+    return out, t
+
+
+def sasa_counts(atoms, radii, unit_dots, probe, use_cells=True, threads=0):
+    atoms = _c(atoms, np.float32)
+    radii = _c(radii, np.float32)
+    unit_dots = _c(unit_dots, np.float32)
+    counts = np.zeros(len(atoms), np.uint32)
+    lib().orc_sasa_counts(atoms.reshape(-1), radii, len(atoms), unit_dots.reshape(-1),
+                          len(unit_dots), ctypes.c_float(probe), counts, int(bool(use_cells)),
+                          int(threads))
+    return counts
+
+
+def fibonacci_unit_dots(n_dots):
+    out = np.zeros((n_dots, 3), np.float32)
+    lib().orc_fibonacci_unit_dots(int(n_dots), out)
+    return out

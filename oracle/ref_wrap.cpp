@@ -1,0 +1,28 @@
+// C entry points over the reference's own host_debye templates
+// (resaxslib/src/host_debye.cpp:54-109, resaxslib/include/host_debye.hpp:30-40),
+// compiled together with that unmodified source file into oracle/_ref/.
+// Test infrastructure only: the product never loads it.
+#include "host_debye.hpp"
+
+extern "C" void ref_host_debye_df(const float *q, int n_q, const float *bodies, int n_bodies,
+                                  const float *ff, int n_factors, float *out)
+{
+    resaxs::host_debye<double, float, cl_float4>::calc_curve(
+        q, n_q, reinterpret_cast<const cl_float4 *>(bodies), n_bodies, ff, n_factors, out);
+}
+
+extern "C" void ref_host_debye_ff(const float *q, int n_q, const float *bodies, int n_bodies,
+                                  const float *ff, int n_factors, float *out)
+{
+    resaxs::host_debye<float, float, cl_float4>::calc_curve(
+        q, n_q, reinterpret_cast<const cl_float4 *>(bodies), n_bodies, ff, n_factors, out);
+}
+
+// bodies as cl_double4 with the type index stored as a 64-bit integer in .w
+// (utils.hpp:68-73, 84-88)
+extern "C" void ref_host_debye_dd(const double *q, int n_q, const double *bodies, int n_bodies,
+                                  const double *ff, int n_factors, double *out)
+{
+    resaxs::host_debye<double, double, cl_double4>::calc_curve(
+        q, n_q, reinterpret_cast<const cl_double4 *>(bodies), n_bodies, ff, n_factors, out);
+}

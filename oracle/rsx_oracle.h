@@ -1,0 +1,86 @@
+/*
+ * CPU oracle for the resaxs hot path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * Nothing in the product library links, loads or calls this code.  It is used
+ * by tests/, by __graft_entry__.smoke() as the checker, and by bench.py's CPU
+ * baseline leg.  Every function restates an algorithm of the reference
+ * (ldantonov/resaxs) and cites the file:line it follows.
+ *
+ * Body layout (same as the reference's cl_float4 bodies, utils.hpp:61-88):
+ *   bodies[4*i + 0..2] = x, y, z (float), bodies[4*i + 3] = uint32 type index
+ *   stored bit-for-bit in the float slot.
+ * Form-factor table: row-major [n_q][n_factors] (host_debye.cpp:64-72).
+ */
+#ifndef RSX_ORACLE_H
+#define RSX_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* FP64 Debye curve: restates host_debye<double,float,cl_float4>::calc_curve
+ * (resaxslib/src/host_debye.cpp:54-109) without the N*N distance matrix.
+ * I(q) = sum_i f_i^2 + 2 sum_{i<j} f_i f_j sinc(q r_ij), sinc = 1 when q*r == 0
+ * (gpu_saxs_pt_wf.cl:55 maps the 0/0 case to 1; host_debye.cpp:93 for q == 0).
+ * Effective factor with the implicit water layer (gpu_saxs_pt_wf.cl:130-138):
+ *   f_i(q) = F[q][t_i] + rsasa_i * (F[q][water_index] * water_weight).
+ * rsasa may be NULL (no water).  n_threads <= 0 uses every online core. */
+void orc_debye_f64(const double *q, int n_q, const float *bodies, int n_bodies,
+                   const float *ff, int n_factors, const float *rsasa,
+                   double water_weight, int water_index, double *out_iq,
+                   int n_threads);
+
+/* Same sum for a uniform q grid q_k = q0 + k*dq (k < n_q), evaluated with an
+ * FP64 rotation recurrence seeded by libm sin/cos per pair; used where the
+ * direct form is too slow (N >= 50k).  Accuracy ~1e-13 relative. */
+void orc_debye_f64_uniform(double q0, double dq, int n_q, const float *bodies,
+                           int n_bodies, const float *ff_rows, int n_factors,
+                           double *out_iq, int n_threads);
+
+/* FP64 gradient of L = sum_q w_q * I(q) with respect to every body position:
+ *   dL/dx_i = sum_{j != i} 2 f_i f_j sum_q w_q (cos(q r) - sinc(q r)) / r^2 * (x_i - x_j)
+ * (derivative of the sum in host_debye.cpp:74-108; the factors are held
+ * constant).  grad is [n_bodies][3]. */
+void orc_debye_grad_f64(const double *q, int n_q, const double *w_q,
+                        const float *bodies, int n_bodies, const float *ff,
+                        int n_factors, const float *rsasa, double water_weight,
+                        int water_index, double *grad, int n_threads);
+
+/* Reference-faithful port of host_debye<double,float,cl_float4>::calc_curve
+ * (host_debye.cpp:54-109): same N*N distance matrix, same loop order, same
+ * mixed float/double arithmetic.  Single threaded, exactly as the reference.
+ * Used to time the reference CPU path where its compiled original is absent. */
+void orc_refport_host_debye(const float *v_q, int n_q, const float *v_bodies,
+                            int n_bodies, const float *t_factors, int n_factors,
+                            float *out_v_iq);
+
+/* The same port with its q loop split across threads sharing one distance
+ * matrix (the reference has no threaded CPU path; this is its loop body run
+ * on several cores).  Returns the seconds spent building the matrix. */
+double orc_refport_host_debye_mt(const float *v_q, int n_q, const float *v_bodies,
+                                 int n_bodies, const float *t_factors,
+                                 int n_factors, float *out_v_iq, int n_threads);
+
+/* Strict-FP32 dot-sphere SASA counts: restates the occlusion test of
+ * calc_rsasa (resaxslib/src/rsasa_dot_spheres.cl:94-163):
+ *   ext_i = r_i + P;  dot = unit_k * ext_i;  sdot = dot + p_i     (per component)
+ *   w_b = (P + r_b) * (P + r_b);  d = sdot - p_b;
+ *   dist2 = (dx*dx + dy*dy) + dz*dz;  occluded iff (w_b - dist2) > 1e-4f
+ * every operation rounded to FP32, no contraction.  counts[i] = accessible
+ * dots of atom i.  Brute force over all atoms when use_cells == 0, else an
+ * exact cell-list prune (a dot can only be occluded by an atom within
+ * r_i + r_b + 2P of atom i). */
+void orc_sasa_counts(const float *atoms, const float *radii, int n_atoms,
+                     const float *unit_dots, int n_dots, float probe,
+                     unsigned *counts, int use_cells, int n_threads);
+
+/* Fibonacci unit dots as generated by create_fibonacci_dots
+ * (resaxslib/src/rsasa_algorithm.cpp:96-116) with n = n_dots / 2 (n_dots
+ * even) and ext_radius = 1: out is [n_dots][3] FP32, bit-for-bit the unit
+ * factors the reference multiplies by ext_radius. */
+void orc_fibonacci_unit_dots(int n_dots, float *out_xyz);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

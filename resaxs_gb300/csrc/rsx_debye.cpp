@@ -1,0 +1,938 @@
+// Debye algorithm handle behind the C ABI (include/rsx.h): host logic for
+// calc / recalc / commit / revert / backward.  Replaces saxs_cl_gpu<float>
+// (resaxslib/src/saxs_alg_cl_gpu_pt_wf.cpp) with a CUDA runtime layer: one
+// stream per handle, device-resident bodies in type-sorted order, FP64
+// running curve.
+#include "rsx_host.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+using namespace rsx;
+
+namespace {
+
+unsigned type_of(const rsx_body &b)
+{
+    unsigned t;
+    std::memcpy(&t, &b.w, sizeof t); // utils.hpp:61-66
+    return t;
+}
+
+// Layout of the bodies on the device: type-sorted order, block tiles and
+// the forward work items (upper triangle of block pairs, J runs of one type
+// grouped `jchunk` at a time).
+struct Layout {
+    std::vector<unsigned> types;  // caller order
+    std::vector<int> perm;        // sorted -> caller
+    std::vector<int> inv;         // caller -> sorted
+    std::vector<int> type_start;  // [T+1]
+    std::vector<int> type_count;  // [T]
+    std::vector<BlockDesc> blocks;
+    std::vector<PairItem> items;     // forward
+    std::vector<PairItem> adj_items; // adjoint (no q-slab grid dimension)
+};
+
+std::vector<PairItem> make_items(const std::vector<BlockDesc> &blocks, int jchunk)
+{
+    std::vector<PairItem> items;
+    const int nb = (int)blocks.size();
+    for (int bi = 0; bi < nb; ++bi) {
+        int bj = bi;
+        while (bj < nb) {
+            const int t = blocks[bj].type;
+            int end = bj;
+            while (end < nb && blocks[end].type == t && end - bj < jchunk)
+                ++end;
+            items.push_back(PairItem{bi, bj, end, 0});
+            bj = end;
+        }
+    }
+    return items;
+}
+
+void build_layout(Layout &L, const rsx_body *bodies, int n, int n_types, int max_items,
+                  int min_adj_items)
+{
+    L.types.resize(n);
+    for (int i = 0; i < n; ++i)
+        L.types[i] = type_of(bodies[i]);
+    L.type_count.assign(n_types, 0);
+    for (int i = 0; i < n; ++i)
+        L.type_count[L.types[i]]++;
+    L.type_start.assign(n_types + 1, 0);
+    for (int t = 0; t < n_types; ++t)
+        L.type_start[t + 1] = L.type_start[t] + L.type_count[t];
+    L.perm.resize(n);
+    L.inv.resize(n);
+    std::vector<int> fill(L.type_start.begin(), L.type_start.end() - 1);
+    for (int i = 0; i < n; ++i) {
+        const int s = fill[L.types[i]]++;
+        L.perm[s] = i;
+        L.inv[i] = s;
+    }
+    L.blocks.clear();
+    for (int t = 0; t < n_types; ++t)
+        for (int s = L.type_start[t]; s < L.type_start[t + 1]; s += kBlockAtoms)
+            L.blocks.push_back(BlockDesc{s, std::min(kBlockAtoms, L.type_start[t + 1] - s), t, 0});
+    int jchunk = 1;
+    L.items = make_items(L.blocks, jchunk);
+    while ((int)L.items.size() > max_items) {
+        jchunk *= 2;
+        L.items = make_items(L.blocks, jchunk);
+    }
+    // adjoint: as few items as keep every SM busy (fewer FP64 gradient flushes)
+    int aj = 1;
+    L.adj_items = make_items(L.blocks, aj);
+    for (;;) {
+        auto next = make_items(L.blocks, aj * 2);
+        if ((int)next.size() < min_adj_items || aj * 2 > (int)L.blocks.size())
+            break;
+        aj *= 2;
+        L.adj_items.swap(next);
+    }
+}
+
+bool detect_uniform(const std::vector<float> &q, float *dq_out)
+{
+    const int n = (int)q.size();
+    if (n == 1) {
+        *dq_out = 0.f;
+        return true;
+    }
+    const double q0 = q[0];
+    const double dq = ((double)q[n - 1] - q0) / (n - 1);
+    for (int k = 0; k < n; ++k) {
+        const double ideal = q0 + k * dq;
+        if (std::fabs((double)q[k] - ideal) > 4e-7 * std::fabs((double)q[k]) + 1e-30)
+            return false;
+    }
+    *dq_out = (float)dq;
+    return true;
+}
+
+} // namespace
+
+struct rsx_debye {
+    int device = -1;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr, ev_c0 = nullptr, ev_c1 = nullptr;
+    bool timing = false;
+    int n = 0, n_q = 0, n_types = 0;
+    std::vector<float> q, ff;
+    bool uniform = false;
+    float dq = 0.f;
+    int q_slab = 32;
+    int max_items = 16384;
+
+    // implicit water (caller order)
+    float water_weight = 0.f;
+    int water_index = 0;
+    std::vector<float> rsasa;
+    bool params_dirty = true;
+
+    Layout L;
+    bool have_layout = false;
+    unsigned layout_version = 0;
+    std::vector<rsx_body> cur;        // caller-order bodies of the current state
+    bool computing = false;
+
+    // checkpoint (commit / revert)
+    bool have_saved = false;
+    std::vector<rsx_body> saved_bodies;
+    std::vector<float> saved_ff, saved_rsasa;
+    float saved_ww = 0.f;
+    int saved_wi = 0;
+    unsigned saved_layout_version = 0;
+
+    // device buffers
+    float4 *d_pos = nullptr, *d_pos_saved = nullptr;
+    float *d_rsasa = nullptr;
+    float *d_ff = nullptr, *d_q = nullptr;
+    BlockDesc *d_blocks = nullptr;
+    PairItem *d_items = nullptr, *d_adj_items = nullptr;
+    size_t items_cap = 0, adj_cap = 0;
+    double *d_partial = nullptr;
+    size_t partial_cap = 0; // doubles
+    double *d_iq64 = nullptr, *d_iq64_saved = nullptr;
+    float *d_iq32 = nullptr;
+    int *d_type_count = nullptr;
+    double *d_rsasa_sum = nullptr;
+    size_t blocks_cap = 0;
+    // incremental
+    unsigned char *d_moved = nullptr; // packed moved_new | moved_idx | tiles
+    size_t moved_cap = 0;
+    int *d_slot = nullptr;
+    // adjoint
+    double *d_grad = nullptr;
+    float *d_lambda = nullptr;
+
+    // pinned staging
+    float4 *h_pos = nullptr;
+    float *h_iq = nullptr;
+    double *h_iq64 = nullptr;
+    double *h_grad = nullptr;
+    unsigned char *h_moved = nullptr;
+    float *h_rsasa = nullptr;
+
+    // water sums (sorted by type)
+    std::vector<double> rsasa_sum;
+    double rsasa_sq = 0.0, rsasa_tot = 0.0;
+
+    float last_ms_kernel = 0.f, last_ms_call = 0.f;
+};
+
+namespace {
+
+template <class T>
+rsx_status ensure(T **p, size_t &cap, size_t count, const char *what)
+{
+    if (*p && cap >= count)
+        return RSX_OK;
+    dev_free(*p);
+    *p = nullptr;
+    cap = 0;
+    RSX_TRY(dev_alloc((void **)p, sizeof(T) * std::max<size_t>(count, 1), what));
+    cap = count;
+    return RSX_OK;
+}
+
+rsx_status check_bodies(const rsx_debye *h, const rsx_body *b, size_t count)
+{
+    for (size_t i = 0; i < count; ++i) {
+        if (type_of(b[i]) >= (unsigned)h->n_types)
+            return fail(RSX_INVALID_ARG, "body " + std::to_string(i) + " has factor index " +
+                                             std::to_string(type_of(b[i])) + " >= n_factors " +
+                                             std::to_string(h->n_types));
+    }
+    return RSX_OK;
+}
+
+void water_sums(rsx_debye *h)
+{
+    h->rsasa_sum.assign(h->n_types, 0.0);
+    h->rsasa_sq = h->rsasa_tot = 0.0;
+    for (int i = 0; i < h->n; ++i) {
+        const double r = h->rsasa[i];
+        h->rsasa_sum[h->L.types[i]] += r;
+        h->rsasa_sq += r * r;
+        h->rsasa_tot += r;
+    }
+}
+
+bool has_water(const rsx_debye *h) { return h->water_weight != 0.f; }
+
+int slab_for(const rsx_debye *h)
+{
+    int qs = h->q_slab;
+    if (has_water(h) && qs > 16)
+        qs = 16; // water keeps two accumulator sets in registers
+    return qs;
+}
+
+// Re-derives the device layout when the body types changed.
+rsx_status update_layout(rsx_debye *h, const rsx_body *bodies)
+{
+    bool same = h->have_layout;
+    if (same)
+        for (int i = 0; i < h->n && same; ++i)
+            same = type_of(bodies[i]) == h->L.types[i];
+    if (same)
+        return RSX_OK;
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+    build_layout(h->L, bodies, h->n, h->n_types, h->max_items, sms * 8);
+    RSX_TRY(ensure(&h->d_blocks, h->blocks_cap, h->L.blocks.size(), "blocks"));
+    RSX_TRY(ensure(&h->d_items, h->items_cap, h->L.items.size(), "items"));
+    RSX_TRY(ensure(&h->d_adj_items, h->adj_cap, h->L.adj_items.size(), "adjoint items"));
+    const size_t need = h->L.items.size() * (size_t)h->n_q;
+    const size_t need_delta = h->L.blocks.size() * (size_t)h->n_q;
+    RSX_TRY(ensure(&h->d_partial, h->partial_cap, std::max(need, need_delta), "partial sums"));
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->d_blocks, h->L.blocks.data(),
+                                 sizeof(BlockDesc) * h->L.blocks.size(), cudaMemcpyHostToDevice,
+                                 h->st),
+                 "upload blocks");
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->d_items, h->L.items.data(),
+                                 sizeof(PairItem) * h->L.items.size(), cudaMemcpyHostToDevice,
+                                 h->st),
+                 "upload items");
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->d_adj_items, h->L.adj_items.data(),
+                                 sizeof(PairItem) * h->L.adj_items.size(),
+                                 cudaMemcpyHostToDevice, h->st),
+                 "upload adjoint items");
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->d_type_count, h->L.type_count.data(),
+                                 sizeof(int) * h->n_types, cudaMemcpyHostToDevice, h->st),
+                 "upload type counts");
+    // pageable host vectors above: make them safe to reuse
+    RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "layout upload");
+    h->have_layout = true;
+    h->layout_version++;
+    return RSX_OK;
+}
+
+rsx_status upload_water(rsx_debye *h)
+{
+    if (!has_water(h))
+        return RSX_OK;
+    water_sums(h);
+    for (int s = 0; s < h->n; ++s)
+        h->h_rsasa[s] = h->rsasa[h->L.perm[s]];
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->d_rsasa, h->h_rsasa, sizeof(float) * h->n,
+                                 cudaMemcpyHostToDevice, h->st),
+                 "upload rsasa");
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->d_rsasa_sum, h->rsasa_sum.data(), sizeof(double) * h->n_types,
+                                 cudaMemcpyHostToDevice, h->st),
+                 "upload rsasa sums");
+    return RSX_OK;
+}
+
+DebyeArgs debye_args(rsx_debye *h)
+{
+    DebyeArgs a{};
+    a.pos = h->d_pos;
+    a.rsasa = has_water(h) ? h->d_rsasa : nullptr;
+    a.ff = h->d_ff;
+    a.q = h->d_q;
+    a.blocks = h->d_blocks;
+    a.items = h->d_items;
+    a.partial = h->d_partial;
+    a.n = h->n;
+    a.n_q = h->n_q;
+    a.n_types = h->n_types;
+    a.n_items = (int)h->L.items.size();
+    a.dq = h->dq;
+    a.water_weight = h->water_weight;
+    a.water_index = h->water_index;
+    return a;
+}
+
+AssembleArgs assemble_args(rsx_debye *h, int n_parts, int accumulate)
+{
+    AssembleArgs a{};
+    a.partial = h->d_partial;
+    a.ff = h->d_ff;
+    a.q = h->d_q;
+    a.type_count = h->d_type_count;
+    a.rsasa_sum = h->d_rsasa_sum;
+    a.rsasa_sq_sum = h->rsasa_sq;
+    a.rsasa_total = h->rsasa_tot;
+    a.n_q = h->n_q;
+    a.n_types = h->n_types;
+    a.n_parts = n_parts;
+    a.water_weight = h->water_weight;
+    a.water_index = h->water_index;
+    a.has_water = has_water(h) ? 1 : 0;
+    a.iq64 = h->d_iq64;
+    a.iq32 = h->d_iq32;
+    a.accumulate = accumulate;
+    return a;
+}
+
+// Forward over the device-resident bodies (no host transfers).
+rsx_status forward_device(rsx_debye *h)
+{
+    const DebyeArgs a = debye_args(h);
+    if (h->timing)
+        RSX_TRY_CUDA(cudaEventRecord(h->ev_k0, h->st), "event");
+    RSX_LAUNCH(launch_forward(a, slab_for(h), h->uniform, has_water(h), h->st), "forward kernel");
+    if (h->timing)
+        RSX_TRY_CUDA(cudaEventRecord(h->ev_k1, h->st), "event");
+    RSX_LAUNCH(launch_assemble(assemble_args(h, a.n_items, 0), h->st), "assemble kernel");
+    return RSX_OK;
+}
+
+rsx_status finish_timing(rsx_debye *h)
+{
+    if (!h->timing)
+        return RSX_OK;
+    RSX_TRY_CUDA(cudaEventRecord(h->ev_c1, h->st), "event");
+    RSX_TRY_CUDA(cudaEventSynchronize(h->ev_c1), "event sync");
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, h->ev_k0, h->ev_k1) == cudaSuccess)
+        h->last_ms_kernel = ms;
+    if (cudaEventElapsedTime(&ms, h->ev_c0, h->ev_c1) == cudaSuccess)
+        h->last_ms_call = ms;
+    return RSX_OK;
+}
+
+rsx_status read_curve(rsx_debye *h, float *out_iq)
+{
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->h_iq, h->d_iq32, sizeof(float) * h->n_q,
+                                 cudaMemcpyDeviceToHost, h->st),
+                 "read curve");
+    RSX_TRY(finish_timing(h));
+    RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "calc");
+    if (out_iq)
+        std::memcpy(out_iq, h->h_iq, sizeof(float) * h->n_q);
+    return RSX_OK;
+}
+
+// Full calculation from caller-order bodies.
+rsx_status full_calc(rsx_debye *h, const rsx_body *bodies)
+{
+    RSX_TRY(update_layout(h, bodies));
+    for (int s = 0; s < h->n; ++s) {
+        const rsx_body &b = bodies[h->L.perm[s]];
+        h->h_pos[s] = make_float4(b.x, b.y, b.z, b.w);
+    }
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->d_pos, h->h_pos, sizeof(float4) * h->n,
+                                 cudaMemcpyHostToDevice, h->st),
+                 "upload bodies");
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->d_ff, h->ff.data(), sizeof(float) * h->ff.size(),
+                                 cudaMemcpyHostToDevice, h->st),
+                 "upload factors");
+    RSX_TRY(upload_water(h));
+    RSX_TRY(forward_device(h));
+    h->cur.assign(bodies, bodies + h->n);
+    h->params_dirty = false;
+    h->computing = true;
+    return RSX_OK;
+}
+
+rsx_status begin_call(rsx_debye *h, bool mark_call = true)
+{
+    if (!h)
+        return fail(RSX_ALG_NOT_INITIALIZED, "null rsx_debye handle");
+    RSX_TRY_CUDA(cudaSetDevice(h->device), "cudaSetDevice");
+    if (h->timing && mark_call)
+        RSX_TRY_CUDA(cudaEventRecord(h->ev_c0, h->st), "event");
+    return RSX_OK;
+}
+
+// Incremental update for moved caller indices `idx` with new bodies `moved`.
+rsx_status delta_update(rsx_debye *h, const rsx_body *moved, const unsigned *idx, unsigned k)
+{
+    // moved list grouped by type (counting sort), tiles of <= 128 per type
+    std::vector<int> cnt(h->n_types + 1, 0);
+    for (unsigned m = 0; m < k; ++m)
+        cnt[type_of(moved[m]) + 1]++;
+    for (int t = 0; t < h->n_types; ++t)
+        cnt[t + 1] += cnt[t];
+    std::vector<int> order(k);
+    {
+        std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+        for (unsigned m = 0; m < k; ++m)
+            order[fill[type_of(moved[m])]++] = (int)m;
+    }
+    std::vector<BlockDesc> tiles;
+    for (int t = 0; t < h->n_types; ++t)
+        for (int s = cnt[t]; s < cnt[t + 1]; s += kBlockAtoms)
+            tiles.push_back(BlockDesc{s, std::min(kBlockAtoms, cnt[t + 1] - s), t, 0});
+    const size_t off_idx = sizeof(float4) * k;
+    const size_t off_tiles = (off_idx + sizeof(int) * k + 15) & ~size_t(15);
+    const size_t bytes = off_tiles + sizeof(BlockDesc) * tiles.size();
+    if (bytes > h->moved_cap) {
+        dev_free(h->d_moved);
+        host_free_pinned(h->h_moved);
+        h->d_moved = nullptr;
+        h->h_moved = nullptr;
+        h->moved_cap = 0;
+        const size_t cap = std::max<size_t>(bytes * 2, 64 * 1024);
+        RSX_TRY(dev_alloc((void **)&h->d_moved, cap, "moved list"));
+        RSX_TRY(host_alloc_pinned((void **)&h->h_moved, cap, "moved staging"));
+        h->moved_cap = cap;
+    }
+    // the pinned staging buffer may still feed the previous step's copy
+    RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "recalc staging");
+    float4 *mv = reinterpret_cast<float4 *>(h->h_moved);
+    int *mi = reinterpret_cast<int *>(h->h_moved + off_idx);
+    for (unsigned s = 0; s < k; ++s) {
+        const rsx_body &b = moved[order[s]];
+        mv[s] = make_float4(b.x, b.y, b.z, b.w);
+        mi[s] = h->L.inv[idx[order[s]]];
+    }
+    std::memcpy(h->h_moved + off_tiles, tiles.data(), sizeof(BlockDesc) * tiles.size());
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->d_moved, h->h_moved, bytes, cudaMemcpyHostToDevice, h->st),
+                 "upload moved list");
+    DeltaArgs a{};
+    a.pos_old = h->d_pos;
+    a.moved_new = reinterpret_cast<const float4 *>(h->d_moved);
+    a.moved_idx = reinterpret_cast<const int *>(h->d_moved + off_idx);
+    a.moved_slot = h->d_slot;
+    a.blocks = h->d_blocks;
+    a.mtiles = reinterpret_cast<const BlockDesc *>(h->d_moved + off_tiles);
+    a.ff = h->d_ff;
+    a.q = h->d_q;
+    a.partial = h->d_partial;
+    a.n = h->n;
+    a.k = (int)k;
+    a.n_q = h->n_q;
+    a.n_types = h->n_types;
+    a.n_blocks = (int)h->L.blocks.size();
+    a.n_mtiles = (int)tiles.size();
+    a.dq = h->dq;
+    int *d_idx = reinterpret_cast<int *>(h->d_moved + off_idx);
+    RSX_LAUNCH(launch_mark_moved(h->d_slot, d_idx, (int)k, 1, h->st), "mark moved");
+    if (h->timing)
+        RSX_TRY_CUDA(cudaEventRecord(h->ev_k0, h->st), "event");
+    RSX_LAUNCH(launch_delta(a, slab_for(h), h->uniform, h->st), "delta kernel");
+    if (h->timing)
+        RSX_TRY_CUDA(cudaEventRecord(h->ev_k1, h->st), "event");
+    RSX_LAUNCH(launch_assemble(assemble_args(h, a.n_blocks, 1), h->st), "assemble delta");
+    RSX_LAUNCH(launch_apply_moves(h->d_pos, a.moved_new, d_idx, (int)k, h->st), "apply moves");
+    RSX_LAUNCH(launch_mark_moved(h->d_slot, d_idx, (int)k, 0, h->st), "unmark moved");
+    return RSX_OK;
+}
+
+rsx_status recalc_common(rsx_debye *h, const rsx_body *moved, const unsigned *idx, unsigned k,
+                         float *out_iq)
+{
+    if (!h->computing)
+        return fail(RSX_NO_INITIAL_CALC,
+                    "recalc called before an initial call to calc (saxs_alg_cl_gpu_pt_wf.cpp:471)");
+    RSX_TRY(check_bodies(h, moved, k));
+    for (unsigned m = 0; m < k; ++m) {
+        if (idx[m] >= (unsigned)h->n)
+            return fail(RSX_INVALID_ARG, "moved index out of range");
+        if (type_of(moved[m]) != h->L.types[idx[m]])
+            return fail(RSX_INVALID_ARG, "recalc cannot change the type of a body");
+    }
+    {
+        std::vector<unsigned> s(idx, idx + k);
+        std::sort(s.begin(), s.end());
+        if (std::adjacent_find(s.begin(), s.end()) != s.end())
+            return fail(RSX_INVALID_ARG, "moved indices must be distinct");
+    }
+    if (h->params_dirty || has_water(h) || (size_t)k * 3 > (size_t)h->n) {
+        // dirty params (saxs_alg_cl_gpu_pt_wf.cpp:479-504), water factors, or
+        // most bodies moved: a full recompute is as cheap and exact
+        std::vector<rsx_body> next = h->cur;
+        for (unsigned m = 0; m < k; ++m)
+            next[idx[m]] = moved[m];
+        RSX_TRY(full_calc(h, next.data()));
+    } else if (k > 0) {
+        RSX_TRY(delta_update(h, moved, idx, k));
+        for (unsigned m = 0; m < k; ++m)
+            h->cur[idx[m]] = moved[m];
+    }
+    return read_curve(h, out_iq);
+}
+
+rsx_status release(rsx_debye *h)
+{
+    if (!h)
+        return RSX_OK;
+    DeviceGuard g(h->device);
+    if (h->st)
+        cudaStreamSynchronize(h->st);
+    void *dev[] = {h->d_pos,        h->d_pos_saved, h->d_rsasa,      h->d_ff,
+                   h->d_q,          h->d_blocks,    h->d_items,      h->d_adj_items,
+                   h->d_partial,    h->d_iq64,      h->d_iq64_saved, h->d_iq32,
+                   h->d_type_count, h->d_rsasa_sum, h->d_moved,      h->d_slot,
+                   h->d_grad,       h->d_lambda};
+    for (void *p : dev)
+        dev_free(p);
+    void *pinned[] = {h->h_pos, h->h_iq, h->h_iq64, h->h_grad, h->h_moved, h->h_rsasa};
+    for (void *p : pinned)
+        host_free_pinned(p);
+    cudaEvent_t evs[] = {h->ev_k0, h->ev_k1, h->ev_c0, h->ev_c1};
+    for (auto e : evs)
+        if (e)
+            cudaEventDestroy(e);
+    if (h->st)
+        cudaStreamDestroy(h->st);
+    delete h;
+    return RSX_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+void rsx_debye_default_options(rsx_debye_options *o)
+{
+    if (!o)
+        return;
+    std::memset(o, 0, sizeof *o);
+    o->device = -1;
+}
+
+rsx_status rsx_debye_create(const float *q, int n_q, const float *t_factors, int n_factors,
+                            int n_bodies, const rsx_debye_options *opts, rsx_debye **out)
+{
+    if (!out)
+        return fail(RSX_INVALID_ARG, "out handle pointer is null");
+    *out = nullptr;
+    if (!q || !t_factors || n_q <= 0 || n_factors <= 0 || n_bodies < 0)
+        return fail(RSX_INVALID_ARG, "q, factor table and sizes must be non-null / positive");
+    if (n_factors > kMaxTypes)
+        return fail(RSX_NOT_SUPPORTED, "at most " + std::to_string(kMaxTypes) + " factor types");
+    rsx_debye_options o;
+    rsx_debye_default_options(&o);
+    if (opts)
+        o = *opts;
+    if (o.q_slab != 0 && o.q_slab != 8 && o.q_slab != 16 && o.q_slab != 32)
+        return fail(RSX_INVALID_ARG, "q_slab must be 0, 8, 16 or 32");
+    int dev = -1;
+    RSX_TRY(select_device(o.device, &dev));
+    DeviceGuard g(dev);
+    cudaSetDevice(dev);
+    rsx_debye *h = new rsx_debye();
+    h->device = dev;
+    h->n = n_bodies;
+    h->n_q = n_q;
+    h->n_types = n_factors;
+    h->q.assign(q, q + n_q);
+    h->ff.assign(t_factors, t_factors + (size_t)n_q * n_factors);
+    h->uniform = !o.force_general_q && detect_uniform(h->q, &h->dq);
+    h->q_slab = o.q_slab ? o.q_slab : (n_q >= 64 ? 32 : (n_q >= 16 ? 16 : 8));
+    h->max_items = o.max_items > 0 ? o.max_items : 16384;
+    h->timing = o.timing != 0;
+    h->rsasa.assign(n_bodies, 0.f);
+    auto bail = [&](rsx_status s) {
+        release(h);
+        return s;
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess)
+        return bail(cuda_status(e, "cudaStreamCreate"));
+    for (cudaEvent_t *ev : {&h->ev_k0, &h->ev_k1, &h->ev_c0, &h->ev_c1}) {
+        e = cudaEventCreate(ev);
+        if (e != cudaSuccess)
+            return bail(cuda_status(e, "cudaEventCreate"));
+    }
+    const size_t n = std::max(n_bodies, 1);
+    rsx_status s;
+#define RSX_ALLOC(ptr, bytes, what)                                                        \
+    if ((s = dev_alloc((void **)&(ptr), (bytes), what)) != RSX_OK)                         \
+        return bail(s);
+#define RSX_PIN(ptr, bytes, what)                                                          \
+    if ((s = host_alloc_pinned((void **)&(ptr), (bytes), what)) != RSX_OK)                 \
+        return bail(s);
+    RSX_ALLOC(h->d_pos, sizeof(float4) * n, "positions");
+    RSX_ALLOC(h->d_pos_saved, sizeof(float4) * n, "saved positions");
+    RSX_ALLOC(h->d_rsasa, sizeof(float) * n, "rsasa");
+    RSX_ALLOC(h->d_ff, sizeof(float) * h->ff.size(), "factor table");
+    RSX_ALLOC(h->d_q, sizeof(float) * n_q, "q");
+    RSX_ALLOC(h->d_iq64, sizeof(double) * n_q, "curve");
+    RSX_ALLOC(h->d_iq64_saved, sizeof(double) * n_q, "saved curve");
+    RSX_ALLOC(h->d_iq32, sizeof(float) * n_q, "curve f32");
+    RSX_ALLOC(h->d_type_count, sizeof(int) * n_factors, "type counts");
+    RSX_ALLOC(h->d_rsasa_sum, sizeof(double) * n_factors, "rsasa sums");
+    RSX_ALLOC(h->d_slot, sizeof(int) * n, "moved slots");
+    RSX_ALLOC(h->d_grad, sizeof(double) * 3 * n, "gradient");
+    RSX_ALLOC(h->d_lambda, sizeof(float) * n_q, "lambda");
+    RSX_PIN(h->h_pos, sizeof(float4) * n, "pinned bodies");
+    RSX_PIN(h->h_iq, sizeof(float) * n_q, "pinned curve");
+    RSX_PIN(h->h_iq64, sizeof(double) * n_q, "pinned curve f64");
+    RSX_PIN(h->h_grad, sizeof(double) * 3 * n, "pinned gradient");
+    RSX_PIN(h->h_rsasa, sizeof(float) * n, "pinned rsasa");
+#undef RSX_ALLOC
+#undef RSX_PIN
+    e = cudaMemcpyAsync(h->d_q, h->q.data(), sizeof(float) * n_q, cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(h->d_slot, 0xff, sizeof(int) * n, h->st); // -1 everywhere
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(h->d_iq64, 0, sizeof(double) * n_q, h->st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(h->st);
+    if (e != cudaSuccess)
+        return bail(cuda_status(e, "handle initialisation"));
+    *out = h;
+    return ok();
+}
+
+rsx_status rsx_debye_destroy(rsx_debye *h)
+{
+    release(h);
+    return ok();
+}
+
+rsx_status rsx_debye_set_factors(rsx_debye *h, const float *t_factors, int n_factors)
+{
+    if (!h)
+        return fail(RSX_ALG_NOT_INITIALIZED, "null rsx_debye handle");
+    if (!t_factors || n_factors != h->n_types)
+        return fail(RSX_INVALID_ARG, "factor table must have the handle's n_factors columns");
+    h->ff.assign(t_factors, t_factors + (size_t)h->n_q * n_factors);
+    h->params_dirty = true;
+    return ok();
+}
+
+rsx_status rsx_debye_set_water(rsx_debye *h, float weight, int water_index, const float *rsasa)
+{
+    if (!h)
+        return fail(RSX_ALG_NOT_INITIALIZED, "null rsx_debye handle");
+    if (water_index < 0 || water_index >= h->n_types)
+        return fail(RSX_INVALID_ARG, "water_index outside the factor table");
+    if (!std::isfinite(weight))
+        return fail(RSX_INVALID_ARG, "water weight must be finite");
+    h->water_weight = weight;
+    h->water_index = water_index;
+    if (rsasa)
+        h->rsasa.assign(rsasa, rsasa + h->n);
+    h->params_dirty = true;
+    return ok();
+}
+
+rsx_status rsx_debye_calc(rsx_debye *h, const rsx_body *bodies, float *out_iq)
+{
+    RSX_TRY(begin_call(h));
+    if (!bodies && h->n > 0)
+        return fail(RSX_INVALID_ARG, "bodies is null");
+    RSX_TRY(check_bodies(h, bodies, h->n));
+    RSX_TRY(full_calc(h, bodies));
+    RSX_TRY(read_curve(h, out_iq));
+    return ok();
+}
+
+rsx_status rsx_debye_recalc_range(rsx_debye *h, const rsx_body *bodies, unsigned upd_start,
+                                  unsigned upd_length, float *out_iq)
+{
+    RSX_TRY(begin_call(h));
+    if ((size_t)upd_start + upd_length > (size_t)h->n)
+        return fail(RSX_INVALID_ARG,
+                    "update region exceeds the number of bodies (saxs_alg_cl_gpu_pt_wf.cpp:473)");
+    if (!bodies && upd_length > 0)
+        return fail(RSX_INVALID_ARG, "bodies is null");
+    std::vector<unsigned> idx(upd_length);
+    for (unsigned m = 0; m < upd_length; ++m)
+        idx[m] = upd_start + m;
+    RSX_TRY(recalc_common(h, bodies + upd_start, idx.data(), upd_length, out_iq));
+    return ok();
+}
+
+rsx_status rsx_debye_recalc_indices(rsx_debye *h, const rsx_body *moved, const unsigned *idx,
+                                    unsigned k, float *out_iq)
+{
+    RSX_TRY(begin_call(h));
+    if (k > 0 && (!moved || !idx))
+        return fail(RSX_INVALID_ARG, "moved bodies / indices are null");
+    RSX_TRY(recalc_common(h, moved, idx, k, out_iq));
+    return ok();
+}
+
+rsx_status rsx_debye_commit(rsx_debye *h)
+{
+    RSX_TRY(begin_call(h));
+    if (!h->computing)
+        return fail(RSX_NO_INITIAL_CALC, "commit called before an initial call to calc");
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->d_pos_saved, h->d_pos, sizeof(float4) * h->n,
+                                 cudaMemcpyDeviceToDevice, h->st),
+                 "save positions");
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->d_iq64_saved, h->d_iq64, sizeof(double) * h->n_q,
+                                 cudaMemcpyDeviceToDevice, h->st),
+                 "save curve");
+    h->saved_bodies = h->cur;
+    h->saved_ff = h->ff;
+    h->saved_rsasa = h->rsasa;
+    h->saved_ww = h->water_weight;
+    h->saved_wi = h->water_index;
+    h->saved_layout_version = h->layout_version;
+    h->have_saved = true;
+    RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "commit");
+    return ok();
+}
+
+rsx_status rsx_debye_revert(rsx_debye *h)
+{
+    RSX_TRY(begin_call(h));
+    if (!h->computing)
+        return fail(RSX_NO_INITIAL_CALC, "revert called before an initial call to calc");
+    if (!h->have_saved)
+        return ok(); // saxs_alg_cl_gpu_pt_wf.cpp:607-608
+    h->ff = h->saved_ff;
+    h->rsasa = h->saved_rsasa;
+    h->water_weight = h->saved_ww;
+    h->water_index = h->saved_wi;
+    if (h->layout_version != h->saved_layout_version) {
+        // the body types changed since the checkpoint: rebuild from it
+        RSX_TRY(full_calc(h, h->saved_bodies.data()));
+        h->saved_layout_version = h->layout_version;
+    } else {
+        RSX_TRY_CUDA(cudaMemcpyAsync(h->d_pos, h->d_pos_saved, sizeof(float4) * h->n,
+                                     cudaMemcpyDeviceToDevice, h->st),
+                     "restore positions");
+        RSX_TRY_CUDA(cudaMemcpyAsync(h->d_iq64, h->d_iq64_saved, sizeof(double) * h->n_q,
+                                     cudaMemcpyDeviceToDevice, h->st),
+                     "restore curve");
+        RSX_TRY_CUDA(cudaMemcpyAsync(h->d_ff, h->ff.data(), sizeof(float) * h->ff.size(),
+                                     cudaMemcpyHostToDevice, h->st),
+                     "restore factors");
+        h->cur = h->saved_bodies;
+        RSX_TRY(upload_water(h));
+        RSX_LAUNCH(launch_f64_to_f32(h->d_iq64, h->d_iq32, h->n_q, h->st), "curve f32");
+        RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "revert");
+    }
+    h->params_dirty = false;
+    return ok();
+}
+
+rsx_status rsx_debye_curve_f64(rsx_debye *h, double *out_iq)
+{
+    RSX_TRY(begin_call(h));
+    if (!h->computing)
+        return fail(RSX_NO_INITIAL_CALC, "no curve computed yet");
+    if (!out_iq)
+        return fail(RSX_INVALID_ARG, "out is null");
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->h_iq64, h->d_iq64, sizeof(double) * h->n_q,
+                                 cudaMemcpyDeviceToHost, h->st),
+                 "read curve");
+    RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "read curve");
+    std::memcpy(out_iq, h->h_iq64, sizeof(double) * h->n_q);
+    return ok();
+}
+
+rsx_status rsx_debye_forward_resident(rsx_debye *h)
+{
+    RSX_TRY(begin_call(h));
+    if (!h->computing)
+        return fail(RSX_NO_INITIAL_CALC, "no bodies on the device yet");
+    RSX_TRY(forward_device(h));
+    return ok();
+}
+
+rsx_status rsx_debye_sync(rsx_debye *h)
+{
+    RSX_TRY(begin_call(h, false));
+    RSX_TRY(finish_timing(h));
+    RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "sync");
+    return ok();
+}
+
+void *rsx_debye_stream(rsx_debye *h) { return h ? (void *)h->st : nullptr; }
+
+rsx_status rsx_debye_timing(rsx_debye *h, float *ms_pair_kernel, float *ms_call)
+{
+    if (!h)
+        return fail(RSX_ALG_NOT_INITIALIZED, "null rsx_debye handle");
+    if (!h->timing)
+        return fail(RSX_ARGS_NOT_SET, "handle created without options.timing");
+    if (ms_pair_kernel)
+        *ms_pair_kernel = h->last_ms_kernel;
+    if (ms_call)
+        *ms_call = h->last_ms_call;
+    return ok();
+}
+
+static rsx_status backward_impl(rsx_debye *h, const float *dl_diq)
+{
+    if (!h->computing)
+        return fail(RSX_NO_INITIAL_CALC, "backward called before an initial call to calc");
+    if (!dl_diq)
+        return fail(RSX_INVALID_ARG, "dL/dI is null");
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->d_lambda, dl_diq, sizeof(float) * h->n_q,
+                                 cudaMemcpyHostToDevice, h->st),
+                 "upload dL/dI");
+    RSX_TRY_CUDA(cudaMemsetAsync(h->d_grad, 0, sizeof(double) * 3 * h->n, h->st), "zero grad");
+    DebyeArgs a = debye_args(h);
+    a.items = h->d_adj_items;
+    a.n_items = (int)h->L.adj_items.size();
+    a.lambda = h->d_lambda;
+    a.grad = h->d_grad;
+    if (h->timing)
+        RSX_TRY_CUDA(cudaEventRecord(h->ev_k0, h->st), "event");
+    RSX_LAUNCH(launch_adjoint(a, slab_for(h), h->uniform, has_water(h), h->st), "adjoint kernel");
+    if (h->timing)
+        RSX_TRY_CUDA(cudaEventRecord(h->ev_k1, h->st), "event");
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->h_grad, h->d_grad, sizeof(double) * 3 * h->n,
+                                 cudaMemcpyDeviceToHost, h->st),
+                 "read gradient");
+    RSX_TRY(finish_timing(h));
+    RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "backward");
+    return RSX_OK;
+}
+
+rsx_status rsx_debye_backward_f64(rsx_debye *h, const float *dl_diq, double *grad_xyz)
+{
+    RSX_TRY(begin_call(h));
+    if (!grad_xyz)
+        return fail(RSX_INVALID_ARG, "gradient output is null");
+    // the host pointer may alias nothing of ours; dl_diq is pageable: copy first
+    std::vector<float> lam(dl_diq ? dl_diq : nullptr, dl_diq ? dl_diq + h->n_q : nullptr);
+    RSX_TRY(backward_impl(h, dl_diq ? lam.data() : nullptr));
+    for (int s = 0; s < h->n; ++s) {
+        const int c = h->L.perm[s];
+        grad_xyz[3 * c + 0] = h->h_grad[3 * s + 0];
+        grad_xyz[3 * c + 1] = h->h_grad[3 * s + 1];
+        grad_xyz[3 * c + 2] = h->h_grad[3 * s + 2];
+    }
+    return ok();
+}
+
+rsx_status rsx_debye_backward(rsx_debye *h, const float *dl_diq, float *grad_xyz)
+{
+    RSX_TRY(begin_call(h));
+    if (!grad_xyz)
+        return fail(RSX_INVALID_ARG, "gradient output is null");
+    std::vector<float> lam(dl_diq ? dl_diq : nullptr, dl_diq ? dl_diq + h->n_q : nullptr);
+    RSX_TRY(backward_impl(h, dl_diq ? lam.data() : nullptr));
+    for (int s = 0; s < h->n; ++s) {
+        const int c = h->L.perm[s];
+        grad_xyz[3 * c + 0] = (float)h->h_grad[3 * s + 0];
+        grad_xyz[3 * c + 1] = (float)h->h_grad[3 * s + 1];
+        grad_xyz[3 * c + 2] = (float)h->h_grad[3 * s + 2];
+    }
+    return ok();
+}
+
+rsx_status rsx_debye_chi2_backward(rsx_debye *h, const float *target, const float *sigma,
+                                   double *chi2, float *grad_xyz)
+{
+    RSX_TRY(begin_call(h));
+    if (!target || !sigma)
+        return fail(RSX_INVALID_ARG, "target / sigma is null");
+    std::vector<double> iq(h->n_q);
+    RSX_TRY(rsx_debye_curve_f64(h, iq.data()));
+    std::vector<float> lam(h->n_q);
+    double c2 = 0.0;
+    for (int k = 0; k < h->n_q; ++k) {
+        const double s = sigma[k];
+        if (!(s > 0.0))
+            return fail(RSX_INVALID_ARG, "sigma must be positive");
+        const double d = (iq[k] - target[k]) / s;
+        c2 += d * d;
+        lam[k] = (float)(2.0 * d / s);
+    }
+    if (chi2)
+        *chi2 = c2;
+    if (grad_xyz)
+        RSX_TRY(rsx_debye_backward(h, lam.data(), grad_xyz));
+    return ok();
+}
+
+rsx_status rsx_debye_config(rsx_debye *h, int *q_slab, int *n_items, int *uniform_q)
+{
+    if (!h)
+        return fail(RSX_ALG_NOT_INITIALIZED, "null rsx_debye handle");
+    if (q_slab)
+        *q_slab = slab_for(h);
+    if (n_items)
+        *n_items = (int)h->L.items.size();
+    if (uniform_q)
+        *uniform_q = h->uniform ? 1 : 0;
+    return ok();
+}
+
+// ---- function-pointer ABI (host_debye.hpp:30) ------------------------------
+
+static std::mutex g_fn_mu;
+
+rsx_status rsx_calc_saxs_curve_status(const float *v_q, int n_q, const rsx_body *v_bodies,
+                                      int n_bodies, const float *t_factors, int n_factors,
+                                      float *out_v_Iq)
+{
+    if (!out_v_Iq || (n_bodies > 0 && !v_bodies))
+        return fail(RSX_INVALID_ARG, "null pointer argument");
+    std::lock_guard<std::mutex> lk(g_fn_mu);
+    rsx_debye *h = nullptr;
+    RSX_TRY(rsx_debye_create(v_q, n_q, t_factors, n_factors, n_bodies, nullptr, &h));
+    rsx_status s = rsx_debye_calc(h, v_bodies, out_v_Iq);
+    std::string msg = rsx_last_error();
+    rsx_debye_destroy(h);
+    if (s != RSX_OK)
+        return fail(s, msg);
+    return ok();
+}
+
+void rsx_calc_saxs_curve(const float *v_q, int n_q, const rsx_body *v_bodies, int n_bodies,
+                         const float *t_factors, int n_factors, float *out_v_Iq)
+{
+    (void)rsx_calc_saxs_curve_status(v_q, n_q, v_bodies, n_bodies, t_factors, n_factors,
+                                     out_v_Iq);
+}
+
+} // extern "C"

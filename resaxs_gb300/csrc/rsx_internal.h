@@ -1,0 +1,90 @@
+// Internal declarations shared by the CUDA kernels and the C++ host layer of
+// librsx.  Not part of the public C ABI (include/rsx.h).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace rsx {
+
+constexpr int kMaxTypes = 32;    // factor-table columns a kernel holds in shared memory
+constexpr int kBlockAtoms = 128; // bodies per block tile = threads per CTA
+
+// A block tile: `len` (<= kBlockAtoms) consecutive bodies of one type in the
+// type-sorted order, starting at `start`.
+struct BlockDesc {
+    int start, len, type, pad;
+};
+
+// One unit of pair work: I-block `bi` against J-blocks [bj_begin, bj_end),
+// all of one type, with bj_begin >= bi (upper triangle of block pairs).
+struct PairItem {
+    int bi, bj_begin, bj_end, pad;
+};
+
+// Arguments of the Debye pair kernels (forward and adjoint).
+struct DebyeArgs {
+    const float4 *pos;       // bodies in type-sorted order, .w = type bits
+    const float *rsasa;      // per sorted body, nullptr without water
+    const float *ff;         // [n_q][n_types] factor table
+    const float *q;          // [n_q]
+    const BlockDesc *blocks; // [n_blocks]
+    const PairItem *items;   // [n_items]
+    double *partial;         // [n_q][n_items] per-item cross sums (forward)
+    int n, n_q, n_types, n_items;
+    float dq;                // uniform q step (rotation path)
+    float water_weight;      // w (water path)
+    int water_index;         // column of the water factor
+    // adjoint
+    const float *lambda;     // [n_q] dL/dI(q)
+    double *grad;            // [n][3] sorted-order FP64 gradient accumulators
+};
+
+// Per-q constants needed to assemble I(q) from the cross sums.
+struct AssembleArgs {
+    const double *partial;   // [n_q][n_parts]
+    const float *ff;         // [n_q][n_types]
+    const float *q;
+    const int *type_count;   // [n_types]
+    const double *rsasa_sum; // [n_types] sum of rsasa per type (water)
+    double rsasa_sq_sum;     // sum of rsasa^2 (water)
+    double rsasa_total;      // sum of rsasa (water)
+    int n_q, n_types, n_parts;
+    float water_weight;
+    int water_index;
+    int has_water;
+    double *iq64;            // [n_q] result (or accumulation target)
+    float *iq32;             // [n_q] FP32 copy of iq64
+    int accumulate;          // 1: iq64 += 2*cross/q (incremental mode, no self terms)
+};
+
+// Moved-set description for the incremental kernel.
+struct DeltaArgs {
+    const float4 *pos_old;   // [n] sorted positions before the move
+    const float4 *moved_new; // [k] new positions of the moved bodies, grouped by type
+    const int *moved_idx;    // [k] sorted index of each moved body
+    const int *moved_slot;   // [n] slot in the moved list, -1 for static bodies
+    const BlockDesc *blocks; // [n_blocks] static-side blocks
+    const BlockDesc *mtiles; // [n_mtiles] moved-list tiles (start/len into the list, type)
+    const float *ff, *q;
+    double *partial;         // [n_q][n_blocks]
+    int n, k, n_q, n_types, n_blocks, n_mtiles;
+    float dq;
+};
+
+// launchers (debye_kernels.cu); all asynchronous on `st`
+cudaError_t launch_forward(const DebyeArgs &a, int q_slab, bool uniform, bool water,
+                           cudaStream_t st);
+cudaError_t launch_assemble(const AssembleArgs &a, cudaStream_t st);
+cudaError_t launch_delta(const DeltaArgs &a, int q_slab, bool uniform, cudaStream_t st);
+cudaError_t launch_apply_moves(float4 *pos, const float4 *moved_new, const int *moved_idx,
+                               int k, cudaStream_t st);
+cudaError_t launch_mark_moved(int *slot, const int *moved_idx, int k, int set, cudaStream_t st);
+cudaError_t launch_f64_to_f32(const double *src, float *dst, int n, cudaStream_t st);
+cudaError_t launch_adjoint(const DebyeArgs &a, int q_slab, bool uniform, bool water,
+                           cudaStream_t st);
+
+// count of kernels this library has launched (for the benchmark's launch claim)
+void count_launch(int n = 1);
+unsigned long long launch_count();
+
+} // namespace rsx

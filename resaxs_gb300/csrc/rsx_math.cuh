@@ -1,0 +1,86 @@
+// FP32 sine/cosine with explicit range reduction, written for this project.
+//
+// Method (published, textbook):
+//  * additive range reduction of Cody & Waite (1980): n = nearest integer to
+//    x * 2/pi, r = ((x - n*P1) - n*P2) - n*P3 where P1 + P2 + P3 is pi/2 split
+//    into three FP32 numbers (P1 = fl(pi/2), P2 = fl(pi/2 - P1),
+//    P3 = fl(pi/2 - P1 - P2), computed from a 60-digit value of pi); with FMA
+//    the first step is exact for |x| < 2^15 and the split leaves an error of
+//    about 1e-23 * n;
+//  * the Taylor series of sin and cos about 0 on |r| <= pi/4 (the
+//    "small-argument series"): sin to r^9 (truncation < 2e-10 relative),
+//    cos to r^10 (truncation < 2e-11);
+//  * quadrant selection by n mod 4.
+// The nearest-integer step uses the 1.5*2^23 rounding constant so that it
+// stays on the FMA pipe (|x * 2/pi| < 2^22 is required; callers keep q*r far
+// below that).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace rsx {
+
+constexpr float kTwoOverPi = 0.636619772367581343f;
+constexpr float kPio2P1 = 1.5707963705062866f;        // 0x3fc90fdb
+constexpr float kPio2P2 = -4.371138828673793e-08f;     // 0xb33bbd2e
+constexpr float kPio2P3 = -1.7151245100058819e-15f;    // 0xa6f72ced
+constexpr float kRound = 12582912.0f;                  // 1.5 * 2^23
+constexpr float kPio4 = 0.785398163397448310f;
+
+// Taylor coefficients (-1)^k / (2k+1)!  and (-1)^k / (2k)!
+constexpr float kS1 = -1.0f / 6.0f;
+constexpr float kS2 = 1.0f / 120.0f;
+constexpr float kS3 = -1.0f / 5040.0f;
+constexpr float kS4 = 1.0f / 362880.0f;
+constexpr float kC1 = -0.5f;
+constexpr float kC2 = 1.0f / 24.0f;
+constexpr float kC3 = -1.0f / 720.0f;
+constexpr float kC4 = 1.0f / 40320.0f;
+constexpr float kC5 = -1.0f / 3628800.0f;
+
+// sin and cos of |r| <= pi/4 by their Taylor series.
+__device__ __forceinline__ void sincos_poly(float r, float &s, float &c)
+{
+    const float r2 = r * r;
+    float ps = fmaf(r2, kS4, kS3);
+    ps = fmaf(r2, ps, kS2);
+    ps = fmaf(r2, ps, kS1);
+    s = fmaf(r * r2, ps, r);
+    float pc = fmaf(r2, kC5, kC4);
+    pc = fmaf(r2, pc, kC3);
+    pc = fmaf(r2, pc, kC2);
+    pc = fmaf(r2, pc, kC1);
+    c = fmaf(r2, pc, 1.0f);
+}
+
+// sin(x), cos(x) for |x| < 2^15 with relative accuracy of a few ulp of the
+// reduced argument.
+__device__ __forceinline__ void sincos_rr(float x, float &s, float &c)
+{
+    const float t = fmaf(x, kTwoOverPi, kRound);
+    const float fn = t - kRound;
+    float r = fmaf(-fn, kPio2P1, x);
+    r = fmaf(-fn, kPio2P2, r);
+    r = fmaf(-fn, kPio2P3, r);
+    float ps, pc;
+    sincos_poly(r, ps, pc);
+    const int n = __float_as_int(t); // low bits of the rounded integer
+    const bool swap = n & 1;
+    float sv = swap ? pc : ps;
+    float cv = swap ? ps : pc;
+    // sin negated in quadrants 2,3; cos negated in quadrants 1,2
+    const unsigned sgn_s = (unsigned)(n & 2) << 30;
+    const unsigned sgn_c = (unsigned)((n + 1) & 2) << 30;
+    s = __uint_as_float(__float_as_uint(sv) ^ sgn_s);
+    c = __uint_as_float(__float_as_uint(cv) ^ sgn_c);
+}
+
+// Same, taking the cheap path when the argument is already reduced.
+__device__ __forceinline__ void sincos_any(float x, float &s, float &c)
+{
+    if (fabsf(x) <= kPio4)
+        sincos_poly(x, s, c);
+    else
+        sincos_rr(x, s, c);
+}
+
+} // namespace rsx

@@ -1,0 +1,86 @@
+"""Regenerates the golden fixtures in this folder from the reference tree.
+
+Run in a container that has the reference sources (default /root/reference):
+
+    python tests/golden/make_golden.py [reference_root]
+
+Outputs (committed; the GPU machine has no reference tree):
+
+* ``test1888.npz`` -- the reference's own known-answer fixture
+  (test_resaxs/test1888.{pos_matrix,ff_db,q_vec,Iq_vec}.txt: 1888 bodies,
+  21 factor types, 51 q) parsed the way test_resaxs/SAXSTest.cpp:68-156 parses
+  it (values read as float), plus the outputs of the reference's compiled
+  host_debye (oracle/_ref) on it: ``iq_ref_df`` = host_debye<double,float>,
+  ``iq_ref_dd`` = host_debye<double,double>.
+* ``synthetic_ref.npz`` -- small seeded synthetic cases and the outputs of the
+  compiled reference host_debye<double,float> and <double,double> on them.
+"""
+from __future__ import annotations
+
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle  # noqa: E402
+from resaxs_gb300 import workloads as W  # noqa: E402
+
+
+def parse_test1888(ref_root):
+    base = os.path.join(ref_root, "test_resaxs", "test1888")
+    q = np.array(open(base + ".q_vec.txt").read().split(), dtype=np.float32)
+    rows = re.findall(r"\[([^\[\]]*)\]", open(base + ".ff_db.txt").read())
+    ff = np.array([[float(v) for v in r.split(",")] for r in rows], dtype=np.float32)
+    pos = open(base + ".pos_matrix.txt").read().split()
+    arr = np.array(pos, dtype=np.float64).reshape(-1, 4)
+    bodies = W.pack_bodies(arr[:, :3].astype(np.float32), arr[:, 3].astype(np.uint32))
+    iq = np.array(open(base + ".Iq_vec.txt").read().split(), dtype=np.float64).reshape(-1, 2)
+    return q, ff, bodies, iq[:, 1].astype(np.float32)
+
+
+def ref_df(q, bodies, ff):
+    out = np.zeros(len(q), np.float32)
+    oracle.ref_lib().ref_host_debye_df(np.ascontiguousarray(q, np.float32), len(q),
+                                       bodies.reshape(-1), len(bodies),
+                                       np.ascontiguousarray(ff).reshape(-1), ff.shape[1], out)
+    return out
+
+
+def ref_dd(q, bodies, ff):
+    b64 = np.zeros((len(bodies), 4), np.float64)
+    b64[:, :3] = bodies[:, :3]
+    b64.view(np.uint64)[:, 3] = W.body_types(bodies).astype(np.uint64)
+    out = np.zeros(len(q), np.float64)
+    oracle.ref_lib().ref_host_debye_dd(np.ascontiguousarray(q, np.float64), len(q),
+                                       b64.reshape(-1), len(bodies),
+                                       np.ascontiguousarray(ff, np.float64).reshape(-1),
+                                       ff.shape[1], out)
+    return out
+
+
+def main(ref_root="/root/reference"):
+    oracle.build()
+    if oracle.build_ref(ref_root) is None:
+        raise SystemExit(f"reference tree not found at {ref_root}")
+    q, ff, bodies, iq = parse_test1888(ref_root)
+    np.savez_compressed(os.path.join(HERE, "test1888.npz"), q=q, ff=ff, bodies=bodies, iq=iq,
+                        iq_ref_df=ref_df(q, bodies, ff), iq_ref_dd=ref_dd(q, bodies, ff))
+    cases = {}
+    for name, idx, n in (("cfg1_n300", 1, 300), ("cfg2_n400", 2, 400), ("cfg4_n250", 4, 250)):
+        w = W.make_config(idx, seed=7, n_override=n)
+        cases[name + "_q"] = w.q
+        cases[name + "_ff"] = w.ff
+        cases[name + "_bodies"] = w.bodies
+        cases[name + "_iq_ref_df"] = ref_df(w.q, w.bodies, w.ff)
+        cases[name + "_iq_ref_dd"] = ref_dd(w.q, w.bodies, w.ff)
+    np.savez_compressed(os.path.join(HERE, "synthetic_ref.npz"), **cases)
+    print("wrote", os.listdir(HERE))
+
+
+if __name__ == "__main__":
+    main(*sys.argv[1:])

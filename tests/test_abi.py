@@ -1,0 +1,84 @@
+"""CPU checks of the C ABI: librsx.so loads and exports every entry point the
+public headers declare; calls that need no GPU report their errors cleanly."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(rsx_[a-z0-9_]+)\s*\(", text):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def librsx():
+    from resaxs_gb300 import _lib
+    return _lib.lib()
+
+
+def test_headers_declare_entry_points():
+    names = declared_symbols()
+    assert "rsx_debye_calc" in names and "rsx_calc_saxs_curve" in names
+    assert len(names) >= 20
+
+
+def test_every_declared_symbol_is_exported(librsx):
+    missing = [n for n in declared_symbols() if not hasattr(librsx, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header(librsx):
+    from resaxs_gb300 import _lib
+    bound = set(_lib.exported_symbols())
+    missing = [n for n in declared_symbols() if n not in bound]
+    assert not missing, missing
+
+
+def test_version_string(librsx):
+    from resaxs_gb300 import _lib
+    v = _lib.lib().rsx_version().decode()
+    assert v.startswith("1.") and "sm_103a" in v
+
+
+def test_null_and_invalid_arguments_without_gpu(librsx):
+    from resaxs_gb300 import _lib
+    L = _lib.lib()
+    # null handle -> ALG_NOT_INITIALIZED (resaxs.hpp:215), no GPU touched
+    assert L.rsx_debye_commit(None) == _lib.RSX_ALG_NOT_INITIALIZED
+    assert L.rsx_debye_set_factors(None, np.zeros(1, np.float32), 1) == _lib.RSX_ALG_NOT_INITIALIZED
+    h = ctypes.c_void_p()
+    q = np.zeros(4, np.float32)
+    st = L.rsx_debye_create(q, 0, np.zeros(4, np.float32), 1, 10, None, ctypes.byref(h))
+    assert st == _lib.RSX_INVALID_ARG
+    assert "positive" in _lib.last_error()
+
+
+def test_create_without_gpu_fails_loudly(librsx):
+    """No CPU fallback: on a machine without a GB300 the handle cannot be created."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from resaxs_gb300 import _lib
+    from resaxs_gb300.saxs import Debye
+    with pytest.raises(_lib.ResaxsError) as e:
+        Debye(np.linspace(0, 0.5, 8), np.ones((8, 2)), 10)
+    assert e.value.code in (_lib.RSX_INVALID_DEVICE, _lib.RSX_PROGRAM_NOT_LOADED)
+
+
+def test_missing_library_raises(monkeypatch, tmp_path):
+    from resaxs_gb300 import _lib
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "librsx.so"))
+    with pytest.raises(_lib.LibraryNotBuilt):
+        _lib.lib()
