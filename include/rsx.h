@@ -62,6 +62,14 @@ unsigned long long rsx_launch_count(void);
  * RSX_INJECTED_FAULT; 0 disables.  kind: 0 = allocation, 1 = launch. */
 void rsx_debug_inject_fault(int kind, int nth);
 
+/* Host-only check of the device layout librsx derives from the body types
+ * (type-sorted block tiles of <= 128 bodies, upper-triangle work items with
+ * at most max_items items): counts, and *pairs_covered_ok = 1 when every block
+ * pair (bi <= bj) is covered exactly once.  Touches no GPU; for tests. */
+rsx_status rsx_debug_layout(const rsx_body *bodies, int n_bodies, int n_factors, int max_items,
+                            int min_adj_items, int *n_blocks, int *n_items, int *n_adj_items,
+                            int *pairs_covered_ok);
+
 /* Measures the sustained FP32 FMA rate of `device` (-1 = current) with a
  * register-resident FMA-chain kernel on every SM: *fma_per_s = lane FMAs per
  * second.  The denominator of the pair*q roofline. */

@@ -64,6 +64,8 @@ SIGNATURES = [
     ("rsx_last_error", ctypes.c_char_p, []),
     ("rsx_launch_count", ctypes.c_ulonglong, []),
     ("rsx_debug_inject_fault", None, [_i, _i]),
+    ("rsx_debug_layout", _st, [_f32p, _i, _i, _i, _i, ctypes.POINTER(_i), ctypes.POINTER(_i),
+                               ctypes.POINTER(_i), ctypes.POINTER(_i)]),
     ("rsx_calc_saxs_curve", None, [_f32p, _i, _f32p, _i, _f32p, _i, _f32p]),
     ("rsx_calc_saxs_curve_status", _st, [_f32p, _i, _f32p, _i, _f32p, _i, _f32p]),
     ("rsx_debye_default_options", None, [ctypes.POINTER(DebyeOptions)]),

@@ -39,6 +39,7 @@ struct Layout {
 std::vector<PairItem> make_items(const std::vector<BlockDesc> &blocks, int jchunk)
 {
     std::vector<PairItem> items;
+    jchunk = std::max(jchunk, 1);
     const int nb = (int)blocks.size();
     for (int bi = 0; bi < nb; ++bi) {
         int bj = bi;
@@ -78,18 +79,23 @@ void build_layout(Layout &L, const rsx_body *bodies, int n, int n_types, int max
     for (int t = 0; t < n_types; ++t)
         for (int s = L.type_start[t]; s < L.type_start[t + 1]; s += kBlockAtoms)
             L.blocks.push_back(BlockDesc{s, std::min(kBlockAtoms, L.type_start[t + 1] - s), t, 0});
+    // grow the J run per item until the item count fits; it cannot drop below
+    // one item per (I-block, type run), reached once jchunk >= n_blocks
+    const int nb = (int)L.blocks.size();
     int jchunk = 1;
     L.items = make_items(L.blocks, jchunk);
-    while ((int)L.items.size() > max_items) {
-        jchunk *= 2;
+    while ((int)L.items.size() > max_items && jchunk < nb) {
+        jchunk = std::min(jchunk * 2, nb);
         L.items = make_items(L.blocks, jchunk);
     }
     // adjoint: as few items as keep every SM busy (fewer FP64 gradient flushes)
     int aj = 1;
     L.adj_items = make_items(L.blocks, aj);
     for (;;) {
+        if (aj * 2 > nb)
+            break;
         auto next = make_items(L.blocks, aj * 2);
-        if ((int)next.size() < min_adj_items || aj * 2 > (int)L.blocks.size())
+        if ((int)next.size() < min_adj_items)
             break;
         aj *= 2;
         L.adj_items.swap(next);
@@ -904,6 +910,51 @@ rsx_status rsx_debye_config(rsx_debye *h, int *q_slab, int *n_items, int *unifor
         *n_items = (int)h->L.items.size();
     if (uniform_q)
         *uniform_q = h->uniform ? 1 : 0;
+    return ok();
+}
+
+rsx_status rsx_debug_layout(const rsx_body *bodies, int n_bodies, int n_factors, int max_items,
+                            int min_adj_items, int *n_blocks, int *n_items, int *n_adj_items,
+                            int *pairs_covered_ok)
+{
+    if ((!bodies && n_bodies > 0) || n_bodies < 0 || n_factors <= 0 || n_factors > kMaxTypes ||
+        max_items <= 0)
+        return fail(RSX_INVALID_ARG, "bad layout arguments");
+    for (int i = 0; i < n_bodies; ++i)
+        if (type_of(bodies[i]) >= (unsigned)n_factors)
+            return fail(RSX_INVALID_ARG, "type out of range");
+    Layout L;
+    build_layout(L, bodies, n_bodies, n_factors, max_items, min_adj_items);
+    if (n_blocks)
+        *n_blocks = (int)L.blocks.size();
+    if (n_items)
+        *n_items = (int)L.items.size();
+    if (n_adj_items)
+        *n_adj_items = (int)L.adj_items.size();
+    if (pairs_covered_ok) {
+        // every unordered block pair (bi <= bj) must be covered exactly once
+        // by each item list, and every block must hold one type only
+        bool good = true;
+        for (const auto &b : L.blocks)
+            for (int s = b.start; s < b.start + b.len && good; ++s)
+                good = L.types[L.perm[s]] == (unsigned)b.type;
+        for (const auto *items : {&L.items, &L.adj_items}) {
+            const int nb = (int)L.blocks.size();
+            std::vector<int> seen((size_t)nb * nb, 0);
+            for (const auto &it : *items) {
+                if (it.bj_begin < it.bi || it.bj_end <= it.bj_begin)
+                    good = false;
+                for (int bj = it.bj_begin; bj < it.bj_end && good; ++bj) {
+                    good = L.blocks[bj].type == L.blocks[it.bj_begin].type;
+                    seen[(size_t)it.bi * nb + bj]++;
+                }
+            }
+            for (int bi = 0; bi < nb; ++bi)
+                for (int bj = 0; bj < nb; ++bj)
+                    good = good && seen[(size_t)bi * nb + bj] == (bj >= bi ? 1 : 0);
+        }
+        *pairs_covered_ok = good ? 1 : 0;
+    }
     return ok();
 }
 

@@ -82,3 +82,23 @@ def test_missing_library_raises(monkeypatch, tmp_path):
     monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "librsx.so"))
     with pytest.raises(_lib.LibraryNotBuilt):
         _lib.lib()
+
+
+@pytest.mark.parametrize("n,types,max_items", [(1500, 5, 7), (1500, 5, 16384), (0, 3, 10),
+                                               (1, 2, 1), (5000, 8, 100), (300, 21, 3)])
+def test_layout_covers_every_block_pair_once(librsx, n, types, max_items):
+    """Host logic of the work decomposition (no GPU): type-uniform block tiles,
+    each block pair (bi <= bj) in exactly one item, bounded item count."""
+    from resaxs_gb300 import _lib
+    from resaxs_gb300 import workloads as W
+    rng = np.random.default_rng(n + types)
+    bodies = W.pack_bodies(rng.normal(size=(n, 3)), rng.integers(0, types, n))
+    nb, ni, na, good = (ctypes.c_int() for _ in range(4))
+    _lib.check(_lib.lib().rsx_debug_layout(bodies.reshape(-1), n, types, max_items, 1216,
+                                           ctypes.byref(nb), ctypes.byref(ni), ctypes.byref(na),
+                                           ctypes.byref(good)))
+    assert good.value == 1
+    assert nb.value >= (n + 127) // 128
+    if n:
+        # at most one item per (I-block, remaining type run) once the cap bites
+        assert ni.value <= max(max_items, nb.value * types)
