@@ -95,7 +95,7 @@ typedef struct rsx_debye rsx_debye;
 
 typedef struct rsx_debye_options {
     int device;          /* CUDA ordinal; -1 = current device */
-    int q_slab;          /* q values per CTA slab: 8, 16, 32; 0 = tuned / default */
+    int q_slab;          /* q values per CTA slab: 8, 16, 32, 64; 0 = tuned / default */
     int max_items;       /* cap on forward work items (scratch = items*n_q*8 B); 0 = default */
     int force_general_q; /* 1: never use the uniform-grid recurrence */
     int timing;          /* 1: record CUDA events around the pair kernel */
@@ -182,6 +182,40 @@ rsx_status rsx_debye_chi2_backward(rsx_debye *h, const float *target, const floa
 
 /* Tuning in effect: q-slab, work items, whether the uniform-q recurrence is used. */
 rsx_status rsx_debye_config(rsx_debye *h, int *q_slab, int *n_items, int *uniform_q);
+
+/* Dot-sphere SASA: replaces resaxs::algorithm::i_rsasa<float,float,cl_base>
+ * implemented by rsasa_cl_gpu (resaxslib/include/rsasa_algorithm.hpp:42-61,
+ * resaxslib/src/rsasa_cl_gpu_alg.cpp, kernel rsasa_dot_spheres.cl:94-163) ---- */
+
+typedef struct rsx_sasa rsx_sasa;
+
+/* Unit dots of create_fibonacci_dots (resaxslib/src/rsasa_algorithm.cpp:96-116)
+ * with n = n_dots/2 (n_dots even): out_xyz is n_dots x 3 FP32, the factors the
+ * reference multiplies by (radius + probe). */
+rsx_status rsx_sasa_fibonacci_dots(int n_dots, float *out_xyz);
+/* The 32 unit directions of create_dodeca_icosa_dots
+ * (rsasa_algorithm.cpp:156-208), the reference GPU path's dot set: 32 x 3. */
+rsx_status rsx_sasa_dodeca_icosa_dots(float *out_xyz);
+
+/* rsasa_cl_gpu::initialize(dot_spheres_cl_params) (rsasa_cl_gpu_alg.cpp:38-57):
+ * atom count, unit dot set (n_dots <= 4096) and probe radius fixed per handle. */
+rsx_status rsx_sasa_create(int n_atoms, const float *unit_dots, int n_dots, float probe,
+                           int device, rsx_sasa **out);
+rsx_status rsx_sasa_destroy(rsx_sasa *h);
+
+/* Accessible-dot counts per atom (the uint buffer of do_recalc_rsasa,
+ * rsasa_cl_gpu_alg.cpp:177-197): dot k of atom i sits at p_i + unit_k * (r_i + P)
+ * and is occluded by atom b when (P + r_b)^2 - |dot - p_b|^2 > 1e-4, each
+ * operation rounded to FP32 without contraction.  radii are per atom. */
+rsx_status rsx_sasa_counts(rsx_sasa *h, const rsx_body *atoms, const float *radii,
+                           unsigned *out_counts);
+
+/* i_rsasa::calc_rsasa / recalc_rsasa: rsasa_i = count_i / n_dots
+ * (rsasa_cl_gpu_alg.cpp:153-197). */
+rsx_status rsx_sasa_calc(rsx_sasa *h, const rsx_body *atoms, const float *radii, float *out_rsasa);
+
+/* Occlusion tests performed and kernel milliseconds of the last call. */
+rsx_status rsx_sasa_stats(rsx_sasa *h, unsigned long long *tests, float *ms_kernel);
 
 #ifdef __cplusplus
 }

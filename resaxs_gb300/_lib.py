@@ -92,6 +92,14 @@ SIGNATURES = [
                                       _vp]),
     ("rsx_debye_config", _st, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i),
                                ctypes.POINTER(_i)]),
+    ("rsx_sasa_fibonacci_dots", _st, [_i, _f32p]),
+    ("rsx_sasa_dodeca_icosa_dots", _st, [_f32p]),
+    ("rsx_sasa_create", _st, [_i, _f32p, _i, ctypes.c_float, _i, ctypes.POINTER(_vp)]),
+    ("rsx_sasa_destroy", _st, [_vp]),
+    ("rsx_sasa_counts", _st, [_vp, _f32p, _f32p, _u32p]),
+    ("rsx_sasa_calc", _st, [_vp, _f32p, _f32p, _f32p]),
+    ("rsx_sasa_stats", _st, [_vp, ctypes.POINTER(ctypes.c_ulonglong),
+                             ctypes.POINTER(ctypes.c_float)]),
 ]
 
 _lib = None

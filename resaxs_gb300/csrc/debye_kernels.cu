@@ -79,42 +79,144 @@ __device__ __forceinline__ void pair_r(const float4 &a, const float4 &b, float &
 // forward
 // ----------------------------------------------------------------------------
 
+// Seeds of the uniform-grid recurrence for one pair.  With x0 = q_0 r,
+// theta = dq r and s_k = sin(x0 + k theta) / r (already scaled by `sc`):
+//  * cos(theta) >= 0: Reinsch's modification of the second-order recurrence
+//    (Reinsch; analysed by Gentleman, Comput. J. 12 (1969) 160-165):
+//      d_{k+1} = d_k + lam s_k,  s_{k+1} = s_k + d_{k+1},
+//      lam = -4 sin^2(theta/2),  d_0 = s_0 - s_{-1} = 2 sin(theta/2) cos(x0 - theta/2) / r
+//    2 FP32 ops per step; it keeps relative accuracy for small theta where the
+//    plain s_{k+1} = 2 cos(theta) s_k - s_{k-1} loses it (cos(theta) ~ 1).
+//  * cos(theta) < 0 (coarse q grids): rotation of (s, c) by theta.
+struct PairSeed {
+    float s, d, lam; // Reinsch state (small) or s, c (rotation, in s, d)
+    float sd, cd;    // rotation step (big only)
+    bool big;
+};
+
+__device__ __forceinline__ PairSeed pair_seed(float x0, float th, float sc)
+{
+    PairSeed p;
+    float s0, c0, sh, ch;
+    sincos_rr(x0, s0, c0);
+    sincos_any(0.5f * th, sh, ch);
+    p.big = ch * ch < sh * sh;
+    p.s = s0 * sc;
+    if (!p.big) {
+        p.lam = -4.0f * sh * sh;
+        p.d = 2.0f * sh * fmaf(c0, ch, s0 * sh) * sc;
+        p.sd = p.cd = 0.f;
+    } else {
+        p.d = c0 * sc;                    // cos(x0) / r
+        p.sd = 2.0f * sh * ch;            // sin(theta)
+        p.cd = fmaf(-2.0f * sh, sh, 1.0f); // cos(theta)
+        p.lam = 0.f;
+    }
+    return p;
+}
+
+// One pair over the slab: S[k] += s_k (and SW[k] += w * s_k).
+template <int QS, bool WATER>
+__device__ __forceinline__ void pair_slab(PairSeed p, float wj, float (&S)[QS], float *SW)
+{
+    if (!p.big) {
+        float s = p.s, d = p.d;
+#pragma unroll
+        for (int k = 0; k < QS; ++k) {
+            S[k] += s;
+            if (WATER)
+                SW[k] = fmaf(wj, s, SW[k]);
+            d = fmaf(p.lam, s, d);
+            s += d;
+        }
+    } else {
+        float s = p.s, c = p.d;
+#pragma unroll
+        for (int k = 0; k < QS; ++k) {
+            S[k] += s;
+            if (WATER)
+                SW[k] = fmaf(wj, s, SW[k]);
+            const float sn = fmaf(c, p.sd, s * p.cd);
+            const float cn = fmaf(-s, p.sd, c * p.cd);
+            s = sn;
+            c = cn;
+        }
+    }
+}
+
+// Two pairs whose recurrences both use the Reinsch form, interleaved for ILP.
+template <int QS>
+__device__ __forceinline__ void pair2_slab(const PairSeed &a, const PairSeed &b, float (&S)[QS])
+{
+    float sa = a.s, da = a.d, sb = b.s, db = b.d;
+#pragma unroll
+    for (int k = 0; k < QS; ++k) {
+        S[k] += sa + sb;
+        da = fmaf(a.lam, sa, da);
+        db = fmaf(b.lam, sb, db);
+        sa += da;
+        sb += db;
+    }
+}
+
+template <int QS>
+__device__ __forceinline__ void reduce_scatter_any(float (&v)[QS], int lane)
+{
+    if constexpr (QS <= 32) {
+        warp_reduce_scatter<QS>(v, lane);
+    } else {
+        // QS = 64: two independent 32-wide scatters; lane L ends with index L
+        // in v[0] and index 32 + L in v[32]
+        float lo[32], hi[32];
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+            lo[k] = v[k];
+            hi[k] = v[32 + k];
+        }
+        warp_reduce_scatter<32>(lo, lane);
+        warp_reduce_scatter<32>(hi, lane);
+        v[0] = lo[0];
+        v[32] = hi[0];
+    }
+}
+
 template <int QS, bool UNIFORM, bool WATER>
 __global__ void __launch_bounds__(kBlockAtoms) forward_kernel(const DebyeArgs a)
 {
     __shared__ float4 s_pos[kBlockAtoms];
     __shared__ float s_rs[WATER ? kBlockAtoms : 1];
     __shared__ float s_q[QS], s_fi[QS], s_fj[QS], s_fw[QS];
+    __shared__ float s_comp[QS][kBlockAtoms];                 // Kahan terms, per thread
+    __shared__ float s_compw[WATER ? QS : 1][kBlockAtoms];
     __shared__ double s_red[kBlockAtoms / 32][QS];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const PairItem it = a.items[blockIdx.x];
     const BlockDesc bi = a.blocks[it.bi];
     const int tj = a.blocks[it.bj_begin].type;
-    const int k0 = blockIdx.y * QS;
-    if (tid < QS) {
-        const int k = k0 + tid;
-        const bool in = k < a.n_q;
-        s_q[tid] = in ? a.q[k] : 0.f;
-        s_fi[tid] = in ? a.ff[(size_t)k * a.n_types + bi.type] : 0.f;
-        s_fj[tid] = in ? a.ff[(size_t)k * a.n_types + tj] : 0.f;
-        s_fw[tid] = (WATER && in) ? a.water_weight * a.ff[(size_t)k * a.n_types + a.water_index]
-                                  : 0.f;
+    const int k0 = a.k_base + blockIdx.y * QS;
+    for (int k = tid; k < QS; k += kBlockAtoms) {
+        const int kk = k0 + k;
+        const bool in = kk < a.n_q;
+        s_q[k] = in ? a.q[kk] : 0.f;
+        s_fi[k] = in ? a.ff[(size_t)kk * a.n_types + bi.type] : 0.f;
+        s_fj[k] = in ? a.ff[(size_t)kk * a.n_types + tj] : 0.f;
+        s_fw[k] = (WATER && in) ? a.water_weight * a.ff[(size_t)kk * a.n_types + a.water_index]
+                                : 0.f;
     }
     const int i = bi.start + tid;
     const bool valid_i = tid < bi.len;
     const float4 pi = valid_i ? a.pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float rs_i = (WATER && valid_i) ? a.rsasa[i] : 0.f;
 
-    float acc[QS], comp[QS];
-    float accw[WATER ? QS : 1], compw[WATER ? QS : 1];
+    float acc[QS], accw[WATER ? QS : 1];
 #pragma unroll
     for (int k = 0; k < QS; ++k) {
         acc[k] = 0.f;
-        comp[k] = 0.f;
+        s_comp[k][tid] = 0.f;
         if (WATER) {
             accw[k] = 0.f;
-            compw[k] = 0.f;
+            s_compw[k][tid] = 0.f;
         }
     }
     __syncthreads();
@@ -138,28 +240,33 @@ __global__ void __launch_bounds__(kBlockAtoms) forward_kernel(const DebyeArgs a)
             if (WATER)
                 SW[k] = 0.f;
         }
-        for (int jj = 0; jj < bj.len; ++jj) {
-            const float4 pj = s_pos[jj];
+        int jj = 0;
+        if (UNIFORM && !WATER) {
+            for (; jj + 1 < bj.len; jj += 2) {
+                float r1, ri1, r2, ri2, dx, dy, dz;
+                pair_r(pi, s_pos[jj], r1, ri1, dx, dy, dz);
+                pair_r(pi, s_pos[jj + 1], r2, ri2, dx, dy, dz);
+                const bool u1 = valid_i && (!diag || jj > tid);
+                const bool u2 = valid_i && (!diag || jj + 1 > tid);
+                const PairSeed p1 = pair_seed(q0 * r1, dq * r1, u1 ? ri1 : 0.f);
+                const PairSeed p2 = pair_seed(q0 * r2, dq * r2, u2 ? ri2 : 0.f);
+                if (!p1.big && !p2.big) {
+                    pair2_slab<QS>(p1, p2, S);
+                } else {
+                    pair_slab<QS, false>(p1, 0.f, S, SW);
+                    pair_slab<QS, false>(p2, 0.f, S, SW);
+                }
+            }
+        }
+        for (; jj < bj.len; ++jj) {
             float r, rinv, dx, dy, dz;
-            pair_r(pi, pj, r, rinv, dx, dy, dz);
+            pair_r(pi, s_pos[jj], r, rinv, dx, dy, dz);
             const bool use = valid_i && (!diag || jj > tid);
             const float sc = use ? rinv : 0.f;
             const float rs_j = WATER ? s_rs[jj] : 0.f;
             if (UNIFORM) {
-                float s0, c0, sd, cd;
-                sincos_rr(q0 * r, s0, c0);
-                sincos_any(dq * r, sd, cd);
-                float s = s0 * sc, c = c0 * sc;
-#pragma unroll
-                for (int k = 0; k < QS; ++k) {
-                    S[k] += s;
-                    if (WATER)
-                        SW[k] = fmaf(rs_j, s, SW[k]);
-                    const float sn = fmaf(c, sd, s * cd);
-                    const float cn = fmaf(-s, sd, c * cd);
-                    s = sn;
-                    c = cn;
-                }
+                const PairSeed p = pair_seed(q0 * r, dq * r, sc);
+                pair_slab<QS, WATER>(p, rs_j, S, SW);
             } else {
 #pragma unroll
                 for (int k = 0; k < QS; ++k) {
@@ -174,35 +281,48 @@ __global__ void __launch_bounds__(kBlockAtoms) forward_kernel(const DebyeArgs a)
         }
 #pragma unroll
         for (int k = 0; k < QS; ++k) {
-            kahan_add(acc[k], comp[k], S[k]);
-            if (WATER)
-                kahan_add(accw[k], compw[k], SW[k]);
+            float c = s_comp[k][tid];
+            kahan_add(acc[k], c, S[k]);
+            s_comp[k][tid] = c;
+            if (WATER) {
+                float cw = s_compw[k][tid];
+                kahan_add(accw[k], cw, SW[k]);
+                s_compw[k][tid] = cw;
+            }
         }
     }
 
     float v[QS];
 #pragma unroll
     for (int k = 0; k < QS; ++k) {
+        const float tot = acc[k] - s_comp[k][tid];
         if (WATER) {
             const float fi = fmaf(rs_i, s_fw[k], s_fi[k]);
-            const float sum = fmaf(s_fj[k], acc[k] - comp[k], s_fw[k] * (accw[k] - compw[k]));
-            v[k] = valid_i ? fi * sum : 0.f;
+            const float totw = accw[k] - s_compw[k][tid];
+            v[k] = valid_i ? fi * fmaf(s_fj[k], tot, s_fw[k] * totw) : 0.f;
         } else {
-            v[k] = valid_i ? acc[k] - comp[k] : 0.f;
+            v[k] = valid_i ? tot : 0.f;
         }
     }
-    warp_reduce_scatter<QS>(v, lane);
-    if (lane < QS)
+    reduce_scatter_any<QS>(v, lane);
+    if (QS <= 32) {
+        if (lane < QS)
+            s_red[warp][lane] = (double)v[0];
+    } else {
         s_red[warp][lane] = (double)v[0];
+        s_red[warp][32 + lane] = (double)v[QS > 32 ? 32 : 0];
+    }
     __syncthreads();
-    if (tid < QS && k0 + tid < a.n_q) {
+    for (int k = tid; k < QS; k += kBlockAtoms) {
+        if (k0 + k >= a.n_q)
+            continue;
         double s = 0.0;
 #pragma unroll
         for (int w = 0; w < kBlockAtoms / 32; ++w)
-            s += s_red[w][tid];
+            s += s_red[w][k];
         if (!WATER)
-            s *= (double)s_fi[tid] * (double)s_fj[tid];
-        a.partial[(size_t)(k0 + tid) * a.n_items + blockIdx.x] = s;
+            s *= (double)s_fi[k] * (double)s_fj[k];
+        a.partial[(size_t)(k0 + k) * a.n_items + blockIdx.x] = s;
     }
 }
 
@@ -558,37 +678,67 @@ __global__ void __launch_bounds__(kBlockAtoms) adjoint_kernel(const DebyeArgs a,
 // launchers
 // ----------------------------------------------------------------------------
 
-template <int QS>
-static cudaError_t forward_qs(const DebyeArgs &a, bool uniform, bool water, cudaStream_t st)
+template <int QS, bool U, bool W>
+static cudaError_t forward_launch(DebyeArgs a, int k_base, int n_slabs, cudaStream_t st)
 {
-    const dim3 grid(a.n_items, (a.n_q + QS - 1) / QS);
-    if (uniform && !water)
-        forward_kernel<QS, true, false><<<grid, kBlockAtoms, 0, st>>>(a);
-    else if (uniform && water)
-        forward_kernel<QS, true, true><<<grid, kBlockAtoms, 0, st>>>(a);
-    else if (!uniform && !water)
-        forward_kernel<QS, false, false><<<grid, kBlockAtoms, 0, st>>>(a);
-    else
-        forward_kernel<QS, false, true><<<grid, kBlockAtoms, 0, st>>>(a);
+    a.k_base = k_base;
+    const dim3 grid(a.n_items, n_slabs);
+    forward_kernel<QS, U, W><<<grid, kBlockAtoms, 0, st>>>(a);
     count_launch();
     return cudaGetLastError();
 }
 
+template <int QS>
+static cudaError_t forward_qs(const DebyeArgs &a, int k_base, int n_slabs, bool uniform,
+                              bool water, cudaStream_t st)
+{
+    if (uniform && !water)
+        return forward_launch<QS, true, false>(a, k_base, n_slabs, st);
+    if (uniform && water)
+        return forward_launch<QS, true, true>(a, k_base, n_slabs, st);
+    if (!uniform && !water)
+        return forward_launch<QS, false, false>(a, k_base, n_slabs, st);
+    return forward_launch<QS, false, true>(a, k_base, n_slabs, st);
+}
+
+static cudaError_t forward_dispatch(const DebyeArgs &a, int qs, int k_base, int n_slabs,
+                                    bool uniform, bool water, cudaStream_t st)
+{
+    switch (qs) {
+    case 8:
+        return forward_qs<8>(a, k_base, n_slabs, uniform, water, st);
+    case 16:
+        return forward_qs<16>(a, k_base, n_slabs, uniform, water, st);
+    case 32:
+        return forward_qs<32>(a, k_base, n_slabs, uniform, water, st);
+    case 64: // uniform grid without water only (register budget)
+        return (uniform && !water) ? forward_launch<64, true, false>(a, k_base, n_slabs, st)
+                                   : cudaErrorInvalidValue;
+    default:
+        return cudaErrorInvalidValue;
+    }
+}
+
+// Full slabs of q_slab values, then the remainder in the smallest slab of
+// 8 / 16 / 32 that covers it (a second launch on the same stream).
 cudaError_t launch_forward(const DebyeArgs &a, int q_slab, bool uniform, bool water,
                            cudaStream_t st)
 {
     if (a.n_items == 0)
         return cudaSuccess;
-    switch (q_slab) {
-    case 8:
-        return forward_qs<8>(a, uniform, water, st);
-    case 16:
-        return forward_qs<16>(a, uniform, water, st);
-    case 32:
-        return forward_qs<32>(a, uniform, water, st);
-    default:
-        return cudaErrorInvalidValue;
+    const int full = a.n_q / q_slab;
+    const int rest = a.n_q - full * q_slab;
+    if (full > 0) {
+        cudaError_t e = forward_dispatch(a, q_slab, 0, full, uniform, water, st);
+        if (e != cudaSuccess)
+            return e;
     }
+    if (rest > 0) {
+        const int tail = rest <= 8 ? 8 : (rest <= 16 ? 16 : (rest <= 32 ? 32 : q_slab));
+        const int n_tail = (rest + tail - 1) / tail;
+        return forward_dispatch(a, tail, full * q_slab, n_tail, uniform, water, st);
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_assemble(const AssembleArgs &a, cudaStream_t st)

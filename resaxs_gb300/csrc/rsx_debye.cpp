@@ -236,6 +236,8 @@ int slab_for(const rsx_debye *h)
     int qs = h->q_slab;
     if (has_water(h) && qs > 16)
         qs = 16; // water keeps two accumulator sets in registers
+    if (!h->uniform && qs > 32)
+        qs = 32; // the direct-sine path has no 64-wide variant
     return qs;
 }
 
@@ -570,8 +572,8 @@ rsx_status rsx_debye_create(const float *q, int n_q, const float *t_factors, int
     rsx_debye_default_options(&o);
     if (opts)
         o = *opts;
-    if (o.q_slab != 0 && o.q_slab != 8 && o.q_slab != 16 && o.q_slab != 32)
-        return fail(RSX_INVALID_ARG, "q_slab must be 0, 8, 16 or 32");
+    if (o.q_slab != 0 && o.q_slab != 8 && o.q_slab != 16 && o.q_slab != 32 && o.q_slab != 64)
+        return fail(RSX_INVALID_ARG, "q_slab must be 0, 8, 16, 32 or 64");
     int dev = -1;
     RSX_TRY(select_device(o.device, &dev));
     DeviceGuard g(dev);

@@ -31,6 +31,7 @@ struct DebyeArgs {
     const PairItem *items;   // [n_items]
     double *partial;         // [n_q][n_items] per-item cross sums (forward)
     int n, n_q, n_types, n_items;
+    int k_base;              // first q index of the launch (set by the launcher)
     float dq;                // uniform q step (rotation path)
     float water_weight;      // w (water path)
     int water_index;         // column of the water factor

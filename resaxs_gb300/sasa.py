@@ -1,0 +1,120 @@
+"""Dot-sphere SASA through librsx: ``DotSphereSasa`` owns an ``rsx_sasa``
+handle; ``RsasaAlgorithm`` mirrors resaxslib's ``i_rsasa`` interface
+(resaxslib/include/rsasa_algorithm.hpp:42-61)."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import ResaxsError, check, lib
+
+__all__ = ["DotSphereSasa", "RsasaAlgorithm", "fibonacci_dots", "dodeca_icosa_dots"]
+
+
+def fibonacci_dots(n_dots: int) -> np.ndarray:
+    out = np.zeros((n_dots, 3), np.float32)
+    check(lib().rsx_sasa_fibonacci_dots(int(n_dots), out.reshape(-1)))
+    return out
+
+
+def dodeca_icosa_dots() -> np.ndarray:
+    out = np.zeros((32, 3), np.float32)
+    check(lib().rsx_sasa_dodeca_icosa_dots(out.reshape(-1)))
+    return out
+
+
+class DotSphereSasa:
+    """Accessible-dot counts of every atom for a fixed unit dot set and probe."""
+
+    def __init__(self, n_atoms: int, n_dots: int = 960, probe: float = 1.4, unit_dots=None,
+                 device: int = -1):
+        if unit_dots is None:
+            unit_dots = fibonacci_dots(n_dots)
+        self.unit = np.ascontiguousarray(unit_dots, np.float32)
+        self.n = int(n_atoms)
+        self.n_dots = len(self.unit)
+        self.probe = float(probe)
+        h = ctypes.c_void_p()
+        check(lib().rsx_sasa_create(self.n, self.unit.reshape(-1), self.n_dots,
+                                    ctypes.c_float(self.probe), int(device), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().rsx_sasa_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def counts(self, atoms, radii) -> np.ndarray:
+        atoms = np.ascontiguousarray(atoms, np.float32)
+        radii = np.ascontiguousarray(radii, np.float32)
+        out = np.zeros(self.n, np.uint32)
+        check(lib().rsx_sasa_counts(self._h, atoms.reshape(-1), radii, out))
+        return out
+
+    def rsasa(self, atoms, radii) -> np.ndarray:
+        atoms = np.ascontiguousarray(atoms, np.float32)
+        radii = np.ascontiguousarray(radii, np.float32)
+        out = np.zeros(self.n, np.float32)
+        check(lib().rsx_sasa_calc(self._h, atoms.reshape(-1), radii, out))
+        return out
+
+    def stats(self):
+        t = ctypes.c_ulonglong()
+        ms = ctypes.c_float()
+        check(lib().rsx_sasa_stats(self._h, ctypes.byref(t), ctypes.byref(ms)))
+        return int(t.value), float(ms.value)
+
+
+class RsasaAlgorithm:
+    """Mirror of ``i_rsasa<float>``: ``initialize(params)`` then
+    ``calc_rsasa(atoms, rsasa)`` / ``recalc_rsasa(atoms, rsasa)``.  Radii come
+    from ``radius_of_type`` (one radius per body type index in atoms[:, 3])."""
+
+    def __init__(self):
+        self._s = None
+        self._computing = False
+
+    def initialize(self, n_atoms: int, radius_of_type, probe_radius: float = 1.4,
+                   unit_dots=None, n_dots: int = 960, device: int = -1):
+        self.radius_of_type = np.asarray(radius_of_type, np.float32)
+        if self._s is not None:
+            self._s.close()
+        self._s = DotSphereSasa(n_atoms, n_dots=n_dots, probe=probe_radius, unit_dots=unit_dots,
+                                device=device)
+
+    def _radii(self, atoms):
+        types = np.ascontiguousarray(atoms, np.float32).view(np.uint32)[:, 3]
+        if types.size and types.max() >= len(self.radius_of_type):
+            raise ResaxsError(_lib.RSX_INVALID_ARG, "atom type without a radius")
+        return self.radius_of_type[types]
+
+    def calc_rsasa(self, atoms, rsasa=None):
+        if self._s is None:
+            raise ResaxsError(_lib.RSX_ARGS_NOT_SET, "initialize() was not called")
+        if rsasa is not None and len(rsasa) < len(atoms):
+            raise ResaxsError(_lib.RSX_INVALID_ARG, "rsasa vector too small")
+        res = self._s.rsasa(atoms, self._radii(atoms))
+        self._computing = True
+        if rsasa is not None:
+            rsasa[: len(res)] = res
+            return rsasa
+        return res
+
+    def recalc_rsasa(self, atoms, rsasa=None):
+        if not self._computing:
+            raise ResaxsError(_lib.RSX_NO_INITIAL_CALC, "recalc_rsasa() before calc_rsasa()")
+        return self.calc_rsasa(atoms, rsasa)
