@@ -102,6 +102,10 @@ typedef struct rsx_debye_options {
     int autotune;        /* 1: time the q-slab candidates on first use and cache the winner */
 } rsx_debye_options;
 
+/* Forgets every autotuned tile choice of this process (the file named by
+ * RSX_AUTOTUNE_CACHE, if any, is not reloaded afterwards). */
+void rsx_autotune_clear(void);
+
 /* Fills the defaults (device -1, everything else 0). */
 void rsx_debye_default_options(rsx_debye_options *opts);
 
@@ -216,6 +220,33 @@ rsx_status rsx_sasa_calc(rsx_sasa *h, const rsx_body *atoms, const float *radii,
 
 /* Occlusion tests performed and kernel milliseconds of the last call. */
 rsx_status rsx_sasa_stats(rsx_sasa *h, unsigned long long *tests, float *ms_kernel);
+
+/* Batched ensembles (no reference counterpart: the reference evaluates an
+ * ensemble one model at a time, calc_saxs/calc_saxs.hpp:611-624).  M members
+ * with their own body counts share q and the factor table; each pass runs as
+ * one CUDA graph holding persistent pair kernels. --------------------------- */
+
+typedef struct rsx_batch rsx_batch;
+
+/* member_sizes[m] bodies per member; bodies of all members are passed
+ * concatenated in member order.  opts as for rsx_debye_create (autotune = 1
+ * picks the q-slab by timing the first pass). */
+rsx_status rsx_batch_create(const float *q, int n_q, const float *t_factors, int n_factors,
+                            const int *member_sizes, int n_members,
+                            const rsx_debye_options *opts, rsx_batch **out);
+rsx_status rsx_batch_destroy(rsx_batch *h);
+/* I(q) of every member: out_iq is n_members x n_q. */
+rsx_status rsx_batch_forward(rsx_batch *h, const rsx_body *bodies, float *out_iq);
+/* Per-member targets and sigmas (n_members x n_q each) of the chi^2 loss. */
+rsx_status rsx_batch_set_targets(rsx_batch *h, const float *targets, const float *sigma);
+/* Forward, chi^2_m = sum_q ((I_m - t_m)/sigma_m)^2 and dchi^2_m/dx for every
+ * body of every member, in one pass (out_iq, chi2, grad_xyz may be NULL). */
+rsx_status rsx_batch_forward_chi2_backward(rsx_batch *h, const rsx_body *bodies, float *out_iq,
+                                           double *chi2, float *grad_xyz);
+/* Milliseconds of the last pass (graph launch to completion, CUDA events). */
+rsx_status rsx_batch_timing(rsx_batch *h, float *ms_last_pass);
+rsx_status rsx_batch_config(rsx_batch *h, int *q_slab, int *n_items, int *persistent_ctas,
+                            int *uniform_q);
 
 #ifdef __cplusplus
 }

@@ -99,10 +99,10 @@ static void *debye_worker(void *p)
     return NULL;
 }
 
-void orc_debye_f64(const double *q, int n_q, const float *bodies, int n_bodies,
-                   const float *ff, int n_factors, const float *rsasa,
-                   double water_weight, int water_index, double *out_iq,
-                   int n_threads)
+void orc_debye_f64_libm(const double *q, int n_q, const float *bodies, int n_bodies,
+                        const float *ff, int n_factors, const float *rsasa,
+                        double water_weight, int water_index, double *out_iq,
+                        int n_threads)
 {
     int nt = pick_threads(n_threads);
     double *f = (double *)malloc(sizeof(double) * (size_t)n_q * n_bodies);
@@ -145,7 +145,197 @@ void orc_debye_f64(const double *q, int n_q, const float *bodies, int n_bodies,
     free(f);
 }
 
+
+/* ------------- direct FP64 Debye with the oracle's own sine -------------- */
+
+/* FP64 sine for the oracle, written for it: Cody & Waite reduction by pi/2
+ * (pi/2 = C1 + C2 + C3, C1 and C2 with 32 significant bits so n*C1, n*C2 are
+ * exact for |n| < 2^21), then the Taylor series of sin / cos on |r| <= pi/4
+ * (to r^17 / r^18: truncation below 1e-19).  Branch-free so that the loops
+ * below vectorise. */
+#define ORC_C1 0x1.921fb54400000p+0
+#define ORC_C2 0x1.0b4611a600000p-34
+#define ORC_C3 0x1.3198a2e037073p-69
+#define ORC_2PI_INV 0.6366197723675814
+
+static inline double orc_sin(double x)
+{
+    double n = __builtin_nearbyint(x * ORC_2PI_INV);
+    double r = ((x - n * ORC_C1) - n * ORC_C2) - n * ORC_C3;
+    double r2 = r * r;
+    double ps = 1.0 / 355687428096000.0; /* 1/17! */
+    ps = ps * r2 - 1.0 / 1307674368000.0;
+    ps = ps * r2 + 1.0 / 6227020800.0;
+    ps = ps * r2 - 1.0 / 39916800.0;
+    ps = ps * r2 + 1.0 / 362880.0;
+    ps = ps * r2 - 1.0 / 5040.0;
+    ps = ps * r2 + 1.0 / 120.0;
+    ps = ps * r2 - 1.0 / 6.0;
+    double sv = r + r * r2 * ps;
+    double pc = -1.0 / 6402373705728000.0; /* -1/18! */
+    pc = pc * r2 + 1.0 / 20922789888000.0;
+    pc = pc * r2 - 1.0 / 87178291200.0;
+    pc = pc * r2 + 1.0 / 479001600.0;
+    pc = pc * r2 - 1.0 / 3628800.0;
+    pc = pc * r2 + 1.0 / 40320.0;
+    pc = pc * r2 - 1.0 / 720.0;
+    pc = pc * r2 + 1.0 / 24.0;
+    pc = pc * r2 - 0.5;
+    double cv = 1.0 + r2 * pc;
+    long long qn = (long long)n;
+    double v = (qn & 1) ? cv : sv;
+    return (qn & 2) ? -v : v;
+}
+
+double orc_sin_probe(double x) { return orc_sin(x); }
+
+typedef struct {
+    const double *q;
+    int n_q;
+    const float *bodies;
+    int n;
+    const double *f; /* [n_q][n] */
+    int next_row;
+    pthread_mutex_t mu;
+    double *acc; /* [n_threads][n_q] */
+} fast_job;
+
+typedef struct {
+    fast_job *job;
+    int tid;
+} fast_arg;
+
+static void *fast_worker(void *p)
+{
+    fast_arg *a = (fast_arg *)p;
+    fast_job *J = a->job;
+    const int n = J->n;
+    double *acc = J->acc + (size_t)a->tid * J->n_q;
+    double *r = (double *)malloc(sizeof(double) * (size_t)(n + 1));
+    double *t = (double *)malloc(sizeof(double) * (size_t)(n + 1));
+    for (;;) {
+        int b;
+        int e = grab_rows(&J->mu, &J->next_row, J->n, 8, &b);
+        if (b >= e)
+            break;
+        for (int y = b; y < e; ++y) {
+            const float *py = &J->bodies[4 * y];
+            const double yx = py[0], yy = py[1], yz = py[2];
+            for (int x = 0; x < y; ++x) {
+                const float *px = &J->bodies[4 * x];
+                double dx = (double)px[0] - yx, dy = (double)px[1] - yy, dz = (double)px[2] - yz;
+                r[x] = sqrt(dx * dx + dy * dy + dz * dz);
+            }
+            for (int k = 0; k < J->n_q; ++k) {
+                const double qk = J->q[k];
+                const double *fk = J->f + (size_t)k * n;
+                for (int x = 0; x < y; ++x) {
+                    double qr = qk * r[x];
+                    double sn = orc_sin(qr);
+                    double s = (qr == 0.0) ? 1.0 : sn / (qr == 0.0 ? 1.0 : qr);
+                    t[x] = fk[x] * s;
+                }
+                double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+                int x = 0;
+                for (; x + 3 < y; x += 4) {
+                    s0 += t[x];
+                    s1 += t[x + 1];
+                    s2 += t[x + 2];
+                    s3 += t[x + 3];
+                }
+                for (; x < y; ++x)
+                    s0 += t[x];
+                acc[k] += ((s0 + s1) + (s2 + s3)) * fk[y];
+            }
+        }
+    }
+    free(r);
+    free(t);
+    return NULL;
+}
+
+void orc_debye_f64(const double *q, int n_q, const float *bodies, int n_bodies,
+                   const float *ff, int n_factors, const float *rsasa,
+                   double water_weight, int water_index, double *out_iq,
+                   int n_threads)
+{
+    int nt = pick_threads(n_threads);
+    double *f = (double *)malloc(sizeof(double) * (size_t)n_q * (n_bodies > 0 ? n_bodies : 1));
+    for (int k = 0; k < n_q; ++k)
+        for (int i = 0; i < n_bodies; ++i)
+            f[(size_t)k * n_bodies + i] = eff_factor(ff, n_factors, k, body_type(bodies, i),
+                                                     rsasa, water_weight, water_index, i);
+    fast_job J;
+    J.q = q;
+    J.n_q = n_q;
+    J.bodies = bodies;
+    J.n = n_bodies;
+    J.f = f;
+    J.next_row = 0;
+    pthread_mutex_init(&J.mu, NULL);
+    J.acc = (double *)calloc((size_t)nt * n_q, sizeof(double));
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nt);
+    fast_arg *args = (fast_arg *)malloc(sizeof(fast_arg) * nt);
+    for (int t = 0; t < nt; ++t) {
+        args[t].job = &J;
+        args[t].tid = t;
+        pthread_create(&th[t], NULL, fast_worker, &args[t]);
+    }
+    for (int t = 0; t < nt; ++t)
+        pthread_join(th[t], NULL);
+    for (int k = 0; k < n_q; ++k) {
+        double cross = 0.0, self = 0.0;
+        for (int t = 0; t < nt; ++t)
+            cross += J.acc[(size_t)t * n_q + k];
+        for (int i = 0; i < n_bodies; ++i) {
+            double fi = f[(size_t)k * n_bodies + i];
+            self += fi * fi;
+        }
+        out_iq[k] = 2.0 * cross + self;
+    }
+    pthread_mutex_destroy(&J.mu);
+    free(J.acc);
+    free(th);
+    free(args);
+    free(f);
+}
+
 /* ------------- FP64 rotation form for a uniform q grid ------------------ */
+
+/* sin and cos of x with the oracle's reduction and series, branch-free (the
+ * quadrant selects compile to blends) so that loops over pairs vectorise. */
+static inline void orc_sincos(double x, double *s, double *c)
+{
+    const double magic = 0x1.8p52;
+    double n = (x * ORC_2PI_INV + magic) - magic;
+    double r = ((x - n * ORC_C1) - n * ORC_C2) - n * ORC_C3;
+    double r2 = r * r;
+    double ps = 1.0 / 355687428096000.0;
+    ps = ps * r2 - 1.0 / 1307674368000.0;
+    ps = ps * r2 + 1.0 / 6227020800.0;
+    ps = ps * r2 - 1.0 / 39916800.0;
+    ps = ps * r2 + 1.0 / 362880.0;
+    ps = ps * r2 - 1.0 / 5040.0;
+    ps = ps * r2 + 1.0 / 120.0;
+    ps = ps * r2 - 1.0 / 6.0;
+    double sv = r + r * r2 * ps;
+    double pc = -1.0 / 6402373705728000.0;
+    pc = pc * r2 + 1.0 / 20922789888000.0;
+    pc = pc * r2 - 1.0 / 87178291200.0;
+    pc = pc * r2 + 1.0 / 479001600.0;
+    pc = pc * r2 - 1.0 / 3628800.0;
+    pc = pc * r2 + 1.0 / 40320.0;
+    pc = pc * r2 - 1.0 / 720.0;
+    pc = pc * r2 + 1.0 / 24.0;
+    pc = pc * r2 - 0.5;
+    double cv = 1.0 + r2 * pc;
+    long long qn = (long long)n;
+    double odd = (double)(qn & 1);
+    double sgn_s = 1.0 - (double)(qn & 2);          /* quadrants 2,3: -sin */
+    double sgn_c = 1.0 - (double)((qn + 1) & 2);    /* quadrants 1,2: -cos */
+    *s = sgn_s * (odd * cv + (1.0 - odd) * sv);
+    *c = sgn_c * (odd * sv + (1.0 - odd) * cv);
+}
 
 typedef struct {
     double q0, dq;
@@ -168,10 +358,17 @@ static void *uni_worker(void *p)
 {
     uni_arg *a = (uni_arg *)p;
     uni_job *J = a->job;
-    int nq = J->n_q;
+    const int nq = J->n_q, n = J->n;
     double *acc = J->acc + (size_t)a->tid * nq;
-    double *inner = (double *)calloc((size_t)nq, sizeof(double));
-    double *fq = (double *)malloc(sizeof(double) * nq);
+    double *s = (double *)malloc(sizeof(double) * (size_t)(n + 1));
+    double *c = (double *)malloc(sizeof(double) * (size_t)(n + 1));
+    double *sd = (double *)malloc(sizeof(double) * (size_t)(n + 1));
+    double *cd = (double *)malloc(sizeof(double) * (size_t)(n + 1));
+    double *w = (double *)malloc(sizeof(double) * (size_t)(n + 1));
+    double *fx = (double *)malloc(sizeof(double) * (size_t)(n + 1));
+    unsigned *tx = (unsigned *)malloc(sizeof(unsigned) * (size_t)(n + 1));
+    for (int x = 0; x < n; ++x)
+        tx[x] = body_type(J->bodies, x);
     for (;;) {
         int b;
         int e = grab_rows(&J->mu, &J->next_row, J->n, 8, &b);
@@ -179,39 +376,64 @@ static void *uni_worker(void *p)
             break;
         for (int y = b; y < e; ++y) {
             const float *py = &J->bodies[4 * y];
-            for (int k = 0; k < nq; ++k)
-                inner[k] = 0.0;
+            const double yx = py[0], yy = py[1], yz = py[2];
             for (int x = 0; x < y; ++x) {
                 const float *px = &J->bodies[4 * x];
-                unsigned tx = body_type(J->bodies, x);
-                double dx = (double)px[0] - py[0];
-                double dy = (double)px[1] - py[1];
-                double dz = (double)px[2] - py[2];
+                double dx = (double)px[0] - yx, dy = (double)px[1] - yy, dz = (double)px[2] - yz;
                 double r = sqrt(dx * dx + dy * dy + dz * dz);
-                if (r == 0.0) {
-                    for (int k = 0; k < nq; ++k)
-                        inner[k] += J->ff[(size_t)k * J->n_factors + tx];
-                    continue;
+                /* coincident bodies: sinc = 1 for every q (handled by the
+                 * r -> tiny limit of sin(q r)/(q r)) */
+                r = r > 1e-12 ? r : 1e-12;
+                double s0, c0, s1, c1;
+                orc_sincos(J->q0 * r, &s0, &c0);
+                orc_sincos(J->dq * r, &s1, &c1);
+                double ir = 1.0 / r;
+                s[x] = s0 * ir;
+                c[x] = c0 * ir;
+                sd[x] = s1;
+                cd[x] = c1;
+            }
+            const unsigned ty = body_type(J->bodies, y);
+            for (int k = 0; k < nq; ++k) {
+                const double qk = J->q0 + k * J->dq;
+                const float *row = J->ff + (size_t)k * J->n_factors;
+                for (int x = 0; x < y; ++x)
+                    fx[x] = row[tx[x]];
+                double s0 = 0, s1 = 0;
+                int x = 0;
+                for (; x + 1 < y; x += 2) {
+                    s0 += fx[x] * s[x];
+                    s1 += fx[x + 1] * s[x + 1];
                 }
-                double s = sin(J->q0 * r) / r, c = cos(J->q0 * r) / r;
-                double sd = sin(J->dq * r), cd = cos(J->dq * r);
-                for (int k = 0; k < nq; ++k) {
-                    double qk = J->q0 + k * J->dq;
-                    double v = (qk == 0.0) ? 1.0 : s / qk;
-                    inner[k] += J->ff[(size_t)k * J->n_factors + tx] * v;
-                    double s2 = s * cd + c * sd;
-                    double c2 = c * cd - s * sd;
-                    s = s2;
-                    c = c2;
+                for (; x < y; ++x)
+                    s0 += fx[x] * s[x];
+                double inner = s0 + s1;
+                if (qk == 0.0) { /* sinc = 1 */
+                    double t = 0;
+                    for (int z = 0; z < y; ++z)
+                        t += fx[z];
+                    inner = t;
+                } else {
+                    inner /= qk;
+                }
+                acc[k] += inner * row[ty];
+                for (int z = 0; z < y; ++z) {
+                    double s2 = s[z] * cd[z] + c[z] * sd[z];
+                    double c2 = c[z] * cd[z] - s[z] * sd[z];
+                    s[z] = s2;
+                    c[z] = c2;
                 }
             }
-            unsigned ty = body_type(J->bodies, y);
-            for (int k = 0; k < nq; ++k)
-                acc[k] += inner[k] * J->ff[(size_t)k * J->n_factors + ty];
+            (void)w;
         }
     }
-    free(fq);
-    free(inner);
+    free(s);
+    free(c);
+    free(sd);
+    free(cd);
+    free(w);
+    free(fx);
+    free(tx);
     return NULL;
 }
 

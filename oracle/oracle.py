@@ -27,7 +27,8 @@ _u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
 def build(cc: str = "gcc") -> str:
     """Compile liboracle.so from the C restatement (seconds)."""
     objs = []
-    for src, extra in (("debye_oracle.c", []), ("sasa_oracle.c", ["-ffp-contract=off"])):
+    for src, extra in (("debye_oracle.c", ["-O3", "-fno-math-errno"]),
+                       ("sasa_oracle.c", ["-ffp-contract=off"])):
         obj = os.path.join(HERE, src.replace(".c", ".o"))
         subprocess.check_call([cc, "-O2", "-fPIC", "-std=c11", "-D_GNU_SOURCE", *extra,
                                "-c", os.path.join(HERE, src), "-o", obj])
@@ -58,6 +59,9 @@ def lib():
         L = ctypes.CDLL(LIB_PATH)
         i, d, vp = ctypes.c_int, ctypes.c_double, ctypes.c_void_p
         L.orc_debye_f64.argtypes = [_f64p, i, _f32p, i, _f32p, i, vp, d, i, _f64p, i]
+        L.orc_debye_f64_libm.argtypes = [_f64p, i, _f32p, i, _f32p, i, vp, d, i, _f64p, i]
+        L.orc_sin_probe.argtypes = [d]
+        L.orc_sin_probe.restype = d
         L.orc_debye_f64_uniform.argtypes = [d, d, i, _f32p, i, _f32p, i, _f64p, i]
         L.orc_debye_grad_f64.argtypes = [_f64p, i, _f64p, _f32p, i, _f32p, i, vp, d, i, _f64p, i]
         L.orc_refport_host_debye.argtypes = [_f32p, i, _f32p, i, _f32p, i, _f32p]
@@ -99,6 +103,16 @@ def debye_f64(q, bodies, ff, rsasa=None, water_weight=0.0, water_index=0, thread
         rs = rs_arr.ctypes.data
     lib().orc_debye_f64(q, len(q), bodies.reshape(-1), len(bodies), ff.reshape(-1), n_f,
                         rs, float(water_weight), int(water_index), out, int(threads))
+    return out
+
+
+def debye_f64_libm(q, bodies, ff, threads=0):
+    q = _c(q, np.float64)
+    bodies = _c(bodies, np.float32)
+    ff = _c(ff, np.float32)
+    out = np.zeros(len(q), np.float64)
+    lib().orc_debye_f64_libm(q, len(q), bodies.reshape(-1), len(bodies), ff.reshape(-1),
+                             ff.shape[1], None, 0.0, 0, out, int(threads))
     return out
 
 

@@ -22,6 +22,8 @@ extern "C" {
  * (resaxslib/src/host_debye.cpp:54-109) without the N*N distance matrix.
  * I(q) = sum_i f_i^2 + 2 sum_{i<j} f_i f_j sinc(q r_ij), sinc = 1 when q*r == 0
  * (gpu_saxs_pt_wf.cl:55 maps the 0/0 case to 1; host_debye.cpp:93 for q == 0).
+ * Uses the oracle's own FP64 sine (range reduction + Taylor series, relative
+ * error ~1e-16) in vectorisable loops.
  * Effective factor with the implicit water layer (gpu_saxs_pt_wf.cl:130-138):
  *   f_i(q) = F[q][t_i] + rsasa_i * (F[q][water_index] * water_weight).
  * rsasa may be NULL (no water).  n_threads <= 0 uses every online core. */
@@ -29,6 +31,15 @@ void orc_debye_f64(const double *q, int n_q, const float *bodies, int n_bodies,
                    const float *ff, int n_factors, const float *rsasa,
                    double water_weight, int water_index, double *out_iq,
                    int n_threads);
+
+/* The same with libm sin per term (slower; cross-checks orc_debye_f64). */
+void orc_debye_f64_libm(const double *q, int n_q, const float *bodies, int n_bodies,
+                        const float *ff, int n_factors, const float *rsasa,
+                        double water_weight, int water_index, double *out_iq,
+                        int n_threads);
+
+/* The oracle's own FP64 sine (tests compare it with libm). */
+double orc_sin_probe(double x);
 
 /* Same sum for a uniform q grid q_k = q0 + k*dq (k < n_q), evaluated with an
  * FP64 rotation recurrence seeded by libm sin/cos per pair; used where the

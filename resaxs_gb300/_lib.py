@@ -69,6 +69,7 @@ SIGNATURES = [
     ("rsx_calc_saxs_curve", None, [_f32p, _i, _f32p, _i, _f32p, _i, _f32p]),
     ("rsx_calc_saxs_curve_status", _st, [_f32p, _i, _f32p, _i, _f32p, _i, _f32p]),
     ("rsx_debye_default_options", None, [ctypes.POINTER(DebyeOptions)]),
+    ("rsx_autotune_clear", None, []),
     ("rsx_debye_create", _st, [_f32p, _i, _f32p, _i, _i, ctypes.POINTER(DebyeOptions),
                                ctypes.POINTER(_vp)]),
     ("rsx_debye_destroy", _st, [_vp]),
@@ -100,6 +101,15 @@ SIGNATURES = [
     ("rsx_sasa_calc", _st, [_vp, _f32p, _f32p, _f32p]),
     ("rsx_sasa_stats", _st, [_vp, ctypes.POINTER(ctypes.c_ulonglong),
                              ctypes.POINTER(ctypes.c_float)]),
+    ("rsx_batch_create", _st, [_f32p, _i, _f32p, _i, np.ctypeslib.ndpointer(np.int32), _i,
+                               ctypes.POINTER(DebyeOptions), ctypes.POINTER(_vp)]),
+    ("rsx_batch_destroy", _st, [_vp]),
+    ("rsx_batch_forward", _st, [_vp, _f32p, _f32p]),
+    ("rsx_batch_set_targets", _st, [_vp, _f32p, _f32p]),
+    ("rsx_batch_forward_chi2_backward", _st, [_vp, _f32p, _vp, _vp, _vp]),
+    ("rsx_batch_timing", _st, [_vp, ctypes.POINTER(ctypes.c_float)]),
+    ("rsx_batch_config", _st, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i),
+                               ctypes.POINTER(_i)]),
 ]
 
 _lib = None

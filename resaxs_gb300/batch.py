@@ -1,0 +1,88 @@
+"""Batched ensembles through librsx: ``DebyeBatch`` owns an ``rsx_batch``
+handle (members share q and the factor table; each pass is one CUDA graph of
+persistent pair kernels)."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from ._lib import DebyeOptions, check, lib
+
+__all__ = ["DebyeBatch"]
+
+
+class DebyeBatch:
+    def __init__(self, q, factors, member_sizes, *, device: int = -1, q_slab: int = 0,
+                 autotune: bool = False, force_general_q: bool = False):
+        self.q = np.ascontiguousarray(q, np.float32)
+        factors = np.ascontiguousarray(factors, np.float32)
+        self.sizes = np.ascontiguousarray(member_sizes, np.int32)
+        self.n_members = len(self.sizes)
+        self.n_q = len(self.q)
+        self.n_total = int(self.sizes.sum())
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes)]).astype(np.int64)
+        opts = DebyeOptions()
+        lib().rsx_debye_default_options(ctypes.byref(opts))
+        opts.device = device
+        opts.q_slab = q_slab
+        opts.autotune = int(autotune)
+        opts.force_general_q = int(force_general_q)
+        h = ctypes.c_void_p()
+        check(lib().rsx_batch_create(self.q, self.n_q, factors.reshape(-1), factors.shape[1],
+                                     self.sizes, self.n_members, ctypes.byref(opts),
+                                     ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().rsx_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _pack(self, members):
+        if isinstance(members, np.ndarray):
+            return np.ascontiguousarray(members, np.float32)
+        return np.ascontiguousarray(np.concatenate(members, axis=0), np.float32)
+
+    def forward(self, members) -> np.ndarray:
+        b = self._pack(members)
+        out = np.zeros((self.n_members, self.n_q), np.float32)
+        check(lib().rsx_batch_forward(self._h, b.reshape(-1), out.reshape(-1)))
+        return out
+
+    def set_targets(self, targets, sigma):
+        t = np.ascontiguousarray(targets, np.float32).reshape(-1)
+        s = np.ascontiguousarray(sigma, np.float32).reshape(-1)
+        check(lib().rsx_batch_set_targets(self._h, t, s))
+
+    def forward_chi2_backward(self, members):
+        b = self._pack(members)
+        out = np.zeros((self.n_members, self.n_q), np.float32)
+        chi2 = np.zeros(self.n_members, np.float64)
+        grad = np.zeros((self.n_total, 3), np.float32)
+        check(lib().rsx_batch_forward_chi2_backward(self._h, b.reshape(-1), out.ctypes.data,
+                                                    chi2.ctypes.data, grad.ctypes.data))
+        return out, chi2, grad
+
+    def timing(self) -> float:
+        ms = ctypes.c_float()
+        check(lib().rsx_batch_timing(self._h, ctypes.byref(ms)))
+        return ms.value
+
+    def config(self):
+        v = [ctypes.c_int() for _ in range(4)]
+        check(lib().rsx_batch_config(self._h, *[ctypes.byref(x) for x in v]))
+        return {"q_slab": v[0].value, "n_items": v[1].value, "persistent_ctas": v[2].value,
+                "uniform_q": bool(v[3].value)}

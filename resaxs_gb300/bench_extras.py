@@ -1,0 +1,203 @@
+"""Secondary measurements of bench.py: one entry per benchmark configuration
+besides the headline forward (incremental recalc + SASA, forward+adjoint,
+precision, batching).  Every figure comes from librsx on the GPU; the FP64
+oracle (oracle/, test infrastructure) is used only to report errors."""
+from __future__ import annotations
+
+import statistics
+import time
+
+import numpy as np
+
+
+def _rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
+
+
+def recalc(device: int, steps: int = 1000, k: int = 50):
+    """Config 2: N=20,000, Q=201; `steps` moves of k random bodies (Gaussian
+    sigma 0.5 A) through rsx_debye_recalc_indices; the FP64 running curve is
+    compared with a fresh full calculation at the end (drift)."""
+    from . import workloads as W
+    from .saxs import Debye
+    w = W.make_config(2, seed=0)
+    rng = np.random.default_rng(42)
+    bodies = w.bodies.copy()
+    moves = []
+    for _ in range(steps):
+        idx = rng.choice(w.n, size=k, replace=False).astype(np.uint32)
+        moved = bodies[idx].copy()
+        moved[:, :3] += rng.normal(0, 0.5, (k, 3)).astype(np.float32)
+        bodies[idx] = moved
+        moves.append((idx, moved))
+    kernel_ms = []
+    with Debye(w.q, w.ff, w.n, device=device, timing=True) as d:
+        d.calc(w.bodies)
+        full_ms = d.timing()[0]
+        t0 = time.perf_counter()
+        for idx, moved in moves:
+            d.recalc_indices(moved, idx)
+            kernel_ms.append(d.timing()[0])
+        wall = time.perf_counter() - t0
+        running = d.curve_f64()
+    with Debye(w.q, w.ff, w.n, device=device) as d2:
+        d2.calc(bodies)
+        fresh = d2.curve_f64()
+    terms = 2 * (k * (w.n - k) + k * (k - 1) // 2) * len(w.q)
+    k_med = statistics.median(kernel_ms)
+    return {"workload": "N=20000 Q=201, k=50 moved per step, sigma 0.5 A",
+            "steps": steps, "step_ms_api": wall / steps * 1e3, "steps_per_s": steps / wall,
+            "delta_kernel_ms": k_med, "sinc_terms_per_step": terms,
+            "delta_kernel_gterms_per_s": terms / (k_med * 1e-3) / 1e9,
+            "full_forward_kernel_ms": full_ms,
+            "speedup_vs_full_recompute_per_step": full_ms / (wall / steps * 1e3),
+            "max_rel_drift_vs_fresh_full_calc": _rel(running, fresh)}
+
+
+def sasa(device: int):
+    """Config 2 SASA: 20,000 atoms, 960 Fibonacci dots, radii U[1.2,1.9], probe 1.4;
+    counts compared with the strict-FP32 oracle (bit-exact)."""
+    from oracle import oracle
+    from . import workloads as W
+    from .sasa import DotSphereSasa, fibonacci_dots
+    w = W.make_config(2, seed=0)
+    radii = np.random.default_rng(0).uniform(1.2, 1.9, w.n).astype(np.float32)
+    with DotSphereSasa(w.n, n_dots=960, probe=1.4, device=device) as s:
+        s.counts(w.bodies, radii)
+        times, kms = [], []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            c = s.counts(w.bodies, radii)
+            times.append(time.perf_counter() - t0)
+            tests, ms = s.stats()
+            kms.append(ms)
+    ref = oracle.sasa_counts(w.bodies, radii, fibonacci_dots(960), 1.4)
+    k_ms = statistics.median(kms)
+    return {"workload": "N=20000 atoms, 960 dots, probe 1.4", "call_ms_api": statistics.median(times) * 1e3,
+            "kernel_ms": k_ms, "occlusion_tests": int(tests),
+            "gtests_per_s": tests / (k_ms * 1e-3) / 1e9, "dots_per_s": w.n * 960 / (k_ms * 1e-3),
+            "exposed_dots": int(c.sum()), "count_mismatches_vs_oracle": int(np.sum(c != ref))}
+
+
+def adjoint(device: int):
+    """Config 3: N=50,000, Q=256 on [0,0.6]; chi^2 against a copy displaced by
+    sigma 1.0 A with sigma_q = 0.01 I_t: forward vs forward+adjoint time."""
+    from . import workloads as W
+    from .saxs import Debye
+    w = W.make_config(3, seed=0)
+    rng = np.random.default_rng(3)
+    tb = w.bodies.copy()
+    tb[:, :3] += rng.normal(0, 1.0, (w.n, 3)).astype(np.float32)
+    with Debye(w.q, w.ff, w.n, device=device, timing=True) as d:
+        target = d.calc(tb)
+        sigma = (0.01 * target).astype(np.float32)
+        d.calc(w.bodies)
+        fwd, adj, tot = [], [], []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            d.calc(w.bodies)
+            fwd.append(d.timing()[0])
+            _, g = d.chi2_backward(target, sigma)
+            adj.append(d.timing()[0])
+            tot.append(time.perf_counter() - t0)
+    f = statistics.median(fwd)
+    a = statistics.median(adj)
+    pq = w.pair_q
+    return {"workload": "N=50000 Q=256", "forward_kernel_ms": f, "adjoint_kernel_ms": a,
+            "fwd_plus_adjoint_over_fwd": (f + a) / f,
+            "forward_gpairq_per_s": pq / (f * 1e-3) / 1e9,
+            "adjoint_gpairq_per_s": pq / (a * 1e-3) / 1e9,
+            "api_fwd_plus_adjoint_ms": statistics.median(tot) * 1e3,
+            "grad_finite": bool(np.all(np.isfinite(g)))}
+
+
+def precision(device: int, n_q_check: int = 8):
+    """Config 4: N=200,000 in a 60 A sphere, 8 types, Q=512 on [0,1]: per-q
+    relative error against the FP64 oracle on a uniform q subset."""
+    from oracle import oracle
+    from . import workloads as W
+    from .saxs import Debye
+    w = W.make_config(4, seed=0)
+    with Debye(w.q, w.ff, w.n, device=device, timing=True) as d:
+        d.calc(w.bodies)
+        ms = []
+        for _ in range(2):
+            d.forward_resident()
+            d.sync()
+            ms.append(d.timing()[0])
+        out = d.curve_f64()
+    step = len(w.q) // n_q_check
+    sel = np.arange(0, len(w.q), step)[:n_q_check]
+    q64 = w.q.astype(np.float64)
+    dq = (q64[-1] - q64[0]) / (len(q64) - 1)
+    t0 = time.perf_counter()
+    ref = oracle.debye_f64_uniform(q64[0], step * dq, len(sel), w.bodies, w.ff[sel])
+    t_or = time.perf_counter() - t0
+    err = np.abs(out[sel] - ref) / np.abs(ref)
+    k_ms = min(ms)
+    return {"workload": "N=200000 Q=512 T=8", "forward_kernel_ms": k_ms,
+            "gpairq_per_s": w.pair_q / (k_ms * 1e-3) / 1e9,
+            "q_checked": [float(x) for x in w.q[sel]],
+            "rel_err_per_q": [float(x) for x in err], "max_rel_err": float(err.max()),
+            "oracle_seconds": t_or}
+
+
+def batching(device: int):
+    """Config 5: 256 members, N ~ U[1000, 30000], Q=201: one graph-captured
+    persistent pass (forward, and forward + per-member chi^2 adjoint) against
+    per-conformation launches of the single-structure forward."""
+    from . import workloads as W
+    from .batch import DebyeBatch
+    from .saxs import Debye
+    q, ff, members = W.batch_members(n_members=256, seed=0)
+    sizes = [len(m) for m in members]
+    pair_q = sum(n * (n - 1) // 2 for n in sizes) * len(q)
+    with DebyeBatch(q, ff, sizes, device=device) as b:
+        out = b.forward(members)
+        fwd = []
+        for _ in range(3):
+            b.forward(members)
+            fwd.append(b.timing())
+        t = out * np.float32(1.01)
+        b.set_targets(t, (0.01 * t + 1e-3).astype(np.float32))
+        b.forward_chi2_backward(members)
+        both = []
+        for _ in range(2):
+            b.forward_chi2_backward(members)
+            both.append(b.timing())
+        cfg = b.config()
+    # per-conformation launches: one handle per member, kernels only (events)
+    per = 0.0
+    api = 0.0
+    for m in members:
+        with Debye(q, ff, len(m), device=device, timing=True) as d:
+            d.calc(m)
+            t0 = time.perf_counter()
+            d.calc(m)
+            api += time.perf_counter() - t0
+            d.forward_resident()
+            d.sync()
+            per += d.timing()[1]   # CUDA events around the member's forward + assembly
+    f = min(fwd)
+    return {"workload": "256 members N~U[1000,30000] Q=201", "pair_q": pair_q,
+            "batched_forward_ms": f, "batched_gpairq_per_s": pair_q / (f * 1e-3) / 1e9,
+            "batched_fwd_plus_adjoint_ms": min(both),
+            "per_conformation_forward_ms_sum": per,
+            "per_conformation_api_ms_sum": api * 1e3,
+            "speedup_vs_per_conformation_kernels": per / f,
+            "speedup_vs_per_conformation_api": api * 1e3 / f, "config": cfg}
+
+
+def run_all(device: int):
+    out = {}
+    for name, fn in (("recalc", recalc), ("sasa", sasa), ("adjoint", adjoint),
+                     ("precision", precision), ("batching", batching)):
+        t0 = time.perf_counter()
+        try:
+            out[name] = fn(device)
+        except Exception as e:  # report the failure in the line, do not hide it
+            out[name] = {"error": repr(e)}
+        out[name]["wall_s"] = time.perf_counter() - t0
+    return out

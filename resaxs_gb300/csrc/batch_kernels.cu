@@ -1,0 +1,250 @@
+// Batched ensembles of conformations with uneven atom counts, for sm_103a.
+//
+// All members share the q grid and factor table; their bodies are
+// concatenated (each member type-sorted within its own range) and their block
+// tiles and work items are concatenated too, so a work item never mixes
+// members.  One persistent kernel per pass walks the whole ensemble: every
+// CTA repeatedly takes the next (item, q-slab) unit from an atomic counter
+// (largest items first) and runs the same per-item code as the single-
+// structure kernels (debye_device.cuh).  There is no waiting on other CTAs:
+// the counter only hands out work, so a CTA finishes as soon as the units
+// run out.
+#include "debye_device.cuh"
+#include "rsx_batch_internal.h"
+
+namespace rsx {
+
+template <int QS, bool UNIFORM>
+__global__ void __launch_bounds__(kBlockAtoms, QS >= 64 ? 3 : 1)
+    batch_forward_kernel(const DebyeArgs a, const int *work_order, int n_units, int n_slabs,
+                         int k_base, int *counter)
+{
+    __shared__ int s_w;
+    for (;;) {
+        if (threadIdx.x == 0)
+            s_w = atomicAdd(counter, 1);
+        __syncthreads();
+        const int w = s_w;
+        __syncthreads();
+        if (w >= n_units)
+            break;
+        const int item = work_order[w / n_slabs];
+        forward_item<QS, UNIFORM, false>(a, item, k_base + (w % n_slabs) * QS);
+    }
+}
+
+template <int QS, bool UNIFORM>
+__global__ void __launch_bounds__(kBlockAtoms)
+    batch_adjoint_kernel(const DebyeArgs a, const int *work_order, int n_units, int n_slabs,
+                         int *counter)
+{
+    __shared__ int s_w;
+    for (;;) {
+        if (threadIdx.x == 0)
+            s_w = atomicAdd(counter, 1);
+        __syncthreads();
+        const int w = s_w;
+        __syncthreads();
+        if (w >= n_units)
+            break;
+        adjoint_item<QS, UNIFORM, false>(a, work_order[w], n_slabs);
+    }
+}
+
+__global__ void __launch_bounds__(256) batch_assemble_kernel(const BatchAssembleArgs a)
+{
+    __shared__ double s_w[8];
+    const int k = blockIdx.x, m = blockIdx.y;
+    const int2 rg = a.item_range[m];
+    const double *row = a.partial + (size_t)k * a.n_items;
+    double s = 0.0;
+    for (int x = rg.x + threadIdx.x; x < rg.y; x += blockDim.x)
+        s += row[x];
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1)
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0)
+        s_w[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x != 0)
+        return;
+    double cross = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+        cross += s_w[w];
+    const double q = a.q[k];
+    double self = 0.0, sumf = 0.0;
+    const float *ff = a.ff + (size_t)k * a.n_types;
+    const int *cnt = a.type_count + (size_t)m * a.n_types;
+    for (int t = 0; t < a.n_types; ++t) {
+        self += cnt[t] * (double)ff[t] * ff[t];
+        sumf += cnt[t] * (double)ff[t];
+    }
+    const double iq = (q != 0.0) ? self + 2.0 * cross / q : sumf * sumf;
+    a.iq64[(size_t)m * a.n_q + k] = iq;
+    a.iq32[(size_t)m * a.n_q + k] = (float)iq;
+}
+
+__global__ void __launch_bounds__(256) batch_loss_kernel(const BatchLossArgs a)
+{
+    __shared__ double s_w[8];
+    const int m = blockIdx.x;
+    double c2 = 0.0;
+    for (int k = threadIdx.x; k < a.n_q; k += blockDim.x) {
+        const size_t o = (size_t)m * a.n_q + k;
+        const double sg = a.sigma[o];
+        const double d = (a.iq64[o] - a.target[o]) / sg;
+        c2 += d * d;
+        a.lambda[o] = (float)(2.0 * d / sg);
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1)
+        c2 += __shfl_xor_sync(0xffffffffu, c2, o);
+    if ((threadIdx.x & 31) == 0)
+        s_w[threadIdx.x >> 5] = c2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+            t += s_w[w];
+        a.chi2[m] = t;
+    }
+}
+
+template <int QS, bool U>
+static cudaError_t fwd_launch(const DebyeArgs &a, const int *order, int n_items, int n_slabs,
+                              int k_base, int *counter, int grid, cudaStream_t st)
+{
+    batch_forward_kernel<QS, U><<<grid, kBlockAtoms, 0, st>>>(a, order, n_items * n_slabs,
+                                                              n_slabs, k_base, counter);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_forward(const DebyeArgs &a, const int *work_order, int n_work_items,
+                                 int q_slab, int n_slabs, int k_base, bool uniform,
+                                 int *counter, int grid, cudaStream_t st)
+{
+    if (n_work_items == 0 || n_slabs == 0)
+        return cudaSuccess;
+#define RSX_BF(QS)                                                                         \
+    return uniform ? fwd_launch<QS, true>(a, work_order, n_work_items, n_slabs, k_base,    \
+                                          counter, grid, st)                               \
+                   : fwd_launch<QS, false>(a, work_order, n_work_items, n_slabs, k_base,   \
+                                           counter, grid, st)
+    switch (q_slab) {
+    case 8:
+        RSX_BF(8);
+    case 16:
+        RSX_BF(16);
+    case 32:
+        RSX_BF(32);
+    case 64:
+        if (!uniform)
+            return cudaErrorInvalidValue;
+        return fwd_launch<64, true>(a, work_order, n_work_items, n_slabs, k_base, counter, grid,
+                                    st);
+    default:
+        return cudaErrorInvalidValue;
+    }
+#undef RSX_BF
+}
+
+template <int QS, bool U>
+static cudaError_t adj_launch(const DebyeArgs &a, const int *order, int n_items, int *counter,
+                              int grid, cudaStream_t st)
+{
+    const int n_slabs = (a.n_q + QS - 1) / QS;
+    const size_t smem = (size_t)n_slabs * QS * 4 * sizeof(float);
+    auto kfn = batch_adjoint_kernel<QS, U>;
+    if (smem > 48 * 1024) {
+        cudaError_t e =
+            cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess)
+            return e;
+    }
+    kfn<<<grid, kBlockAtoms, smem, st>>>(a, order, n_items, n_slabs, counter);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_adjoint(const DebyeArgs &a, const int *work_order, int n_work_items,
+                                 int q_slab, bool uniform, int *counter, int grid,
+                                 cudaStream_t st)
+{
+    if (n_work_items == 0)
+        return cudaSuccess;
+    const int qs = q_slab > 32 ? 32 : q_slab; // the adjoint keeps two sums, not QS
+    switch (qs) {
+    case 8:
+        return uniform ? adj_launch<8, true>(a, work_order, n_work_items, counter, grid, st)
+                       : adj_launch<8, false>(a, work_order, n_work_items, counter, grid, st);
+    case 16:
+        return uniform ? adj_launch<16, true>(a, work_order, n_work_items, counter, grid, st)
+                       : adj_launch<16, false>(a, work_order, n_work_items, counter, grid, st);
+    default:
+        return uniform ? adj_launch<32, true>(a, work_order, n_work_items, counter, grid, st)
+                       : adj_launch<32, false>(a, work_order, n_work_items, counter, grid, st);
+    }
+}
+
+cudaError_t launch_batch_assemble(const BatchAssembleArgs &a, cudaStream_t st)
+{
+    if (a.n_members == 0)
+        return cudaSuccess;
+    batch_assemble_kernel<<<dim3(a.n_q, a.n_members), 256, 0, st>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_loss(const BatchLossArgs &a, cudaStream_t st)
+{
+    if (a.n_members == 0)
+        return cudaSuccess;
+    batch_loss_kernel<<<a.n_members, 256, 0, st>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <class K>
+static int occupancy_grid(K kfn, size_t smem, int sms)
+{
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kBlockAtoms, smem) !=
+            cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    return per_sm * sms;
+}
+
+int batch_forward_grid(int q_slab, bool uniform, int sms)
+{
+    switch (q_slab) {
+    case 8:
+        return uniform ? occupancy_grid(batch_forward_kernel<8, true>, 0, sms)
+                       : occupancy_grid(batch_forward_kernel<8, false>, 0, sms);
+    case 16:
+        return uniform ? occupancy_grid(batch_forward_kernel<16, true>, 0, sms)
+                       : occupancy_grid(batch_forward_kernel<16, false>, 0, sms);
+    case 32:
+        return uniform ? occupancy_grid(batch_forward_kernel<32, true>, 0, sms)
+                       : occupancy_grid(batch_forward_kernel<32, false>, 0, sms);
+    default:
+        return occupancy_grid(batch_forward_kernel<64, true>, 0, sms);
+    }
+}
+
+int batch_adjoint_grid(int q_slab, bool uniform, int n_q, int sms)
+{
+    const int qs = q_slab > 32 ? 32 : (q_slab < 8 ? 8 : q_slab);
+    const size_t smem = (size_t)((n_q + qs - 1) / qs) * qs * 4 * sizeof(float);
+    if (qs == 8)
+        return uniform ? occupancy_grid(batch_adjoint_kernel<8, true>, smem, sms)
+                       : occupancy_grid(batch_adjoint_kernel<8, false>, smem, sms);
+    if (qs == 16)
+        return uniform ? occupancy_grid(batch_adjoint_kernel<16, true>, smem, sms)
+                       : occupancy_grid(batch_adjoint_kernel<16, false>, smem, sms);
+    return uniform ? occupancy_grid(batch_adjoint_kernel<32, true>, smem, sms)
+                   : occupancy_grid(batch_adjoint_kernel<32, false>, smem, sms);
+}
+
+} // namespace rsx

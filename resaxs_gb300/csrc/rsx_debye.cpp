@@ -3,6 +3,7 @@
 // (resaxslib/src/saxs_alg_cl_gpu_pt_wf.cpp) with a CUDA runtime layer: one
 // stream per handle, device-resident bodies in type-sorted order, FP64
 // running curve.
+#include "rsx_autotune.h"
 #include "rsx_host.h"
 
 #include <algorithm>
@@ -133,6 +134,7 @@ struct rsx_debye {
     float dq = 0.f;
     int q_slab = 32;
     int max_items = 16384;
+    bool autotune = false, tuned = false;
 
     // implicit water (caller order)
     float water_weight = 0.f;
@@ -378,6 +380,60 @@ rsx_status read_curve(rsx_debye *h, float *out_iq)
     return RSX_OK;
 }
 
+// Picks the q-slab of the forward kernel for this problem class: the cached
+// winner, or the fastest candidate timed here (two timed runs each, after a
+// warm-up) on the bodies just uploaded.
+rsx_status tune_slab(rsx_debye *h)
+{
+    h->tuned = true;
+    const std::string key = autotune_key(h->device, "forward", h->n, h->n_q, h->n_types,
+                                         h->uniform, has_water(h));
+    int qs = 0;
+    if (autotune_lookup(key, &qs)) {
+        h->q_slab = qs;
+        return RSX_OK;
+    }
+    std::vector<int> cands = {16, 32};
+    if (h->uniform && !has_water(h))
+        cands.push_back(64);
+    cudaEvent_t e0, e1;
+    RSX_TRY_CUDA(cudaEventCreate(&e0), "event");
+    RSX_TRY_CUDA(cudaEventCreate(&e1), "event");
+    float best = 1e30f;
+    int best_qs = h->q_slab;
+    rsx_status st = RSX_OK;
+    const bool timing = h->timing;
+    h->timing = false;
+    for (int c : cands) {
+        h->q_slab = c;
+        float t_min = 1e30f;
+        for (int rep = 0; rep < 3 && st == RSX_OK; ++rep) {
+            cudaEventRecord(e0, h->st);
+            st = forward_device(h);
+            cudaEventRecord(e1, h->st);
+            if (cudaEventSynchronize(e1) != cudaSuccess)
+                st = fail(RSX_CUDA_ERROR, "autotune run failed");
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (rep > 0)
+                t_min = std::min(t_min, ms);
+        }
+        if (st != RSX_OK)
+            break;
+        if (t_min < best) {
+            best = t_min;
+            best_qs = c;
+        }
+    }
+    h->timing = timing;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    h->q_slab = best_qs;
+    if (st == RSX_OK)
+        autotune_store(key, best_qs);
+    return st;
+}
+
 // Full calculation from caller-order bodies.
 rsx_status full_calc(rsx_debye *h, const rsx_body *bodies)
 {
@@ -393,6 +449,8 @@ rsx_status full_calc(rsx_debye *h, const rsx_body *bodies)
                                  cudaMemcpyHostToDevice, h->st),
                  "upload factors");
     RSX_TRY(upload_water(h));
+    if (h->autotune && !h->tuned)
+        RSX_TRY(tune_slab(h));
     RSX_TRY(forward_device(h));
     h->cur.assign(bodies, bodies + h->n);
     h->params_dirty = false;
@@ -586,7 +644,11 @@ rsx_status rsx_debye_create(const float *q, int n_q, const float *t_factors, int
     h->q.assign(q, q + n_q);
     h->ff.assign(t_factors, t_factors + (size_t)n_q * n_factors);
     h->uniform = !o.force_general_q && detect_uniform(h->q, &h->dq);
-    h->q_slab = o.q_slab ? o.q_slab : (n_q >= 64 ? 32 : (n_q >= 16 ? 16 : 8));
+    // default tile: 64 q per slab on long uniform grids (measured fastest on
+    // GB300 for Q >= 128), otherwise 32 / 16 / 8
+    h->q_slab = o.q_slab ? o.q_slab
+                         : (h->uniform && n_q >= 128 ? 64 : (n_q >= 32 ? 32 : (n_q >= 16 ? 16 : 8)));
+    h->autotune = o.autotune != 0 && o.q_slab == 0;
     h->max_items = o.max_items > 0 ? o.max_items : 16384;
     h->timing = o.timing != 0;
     h->rsasa.assign(n_bodies, 0.f);

@@ -175,3 +175,15 @@ def test_full_size_config2_q_subset_vs_oracle(saxs, oracle_lib):
     dq = (q64[-1] - q64[0]) / (len(q64) - 1)
     ref = oracle_lib.debye_f64_uniform(q64[0], 40 * dq, len(sel), w.bodies, w.ff[sel])
     assert rel(out64[sel], ref) < TOL
+
+
+def test_autotuned_slab(saxs, oracle_lib):
+    from resaxs_gb300 import _lib
+    _lib.lib().rsx_autotune_clear()
+    w = W.make_config(2, seed=18, n_override=3000)
+    _, out64, cfg = gpu_curve(saxs, w.q, w.ff, w.bodies, autotune=True)
+    assert cfg["q_slab"] in (16, 32, 64)
+    assert rel(out64, oracle_lib.debye_f64(w.q, w.bodies, w.ff)) < TOL
+    _, again, cfg2 = gpu_curve(saxs, w.q, w.ff, w.bodies, autotune=True)   # cached choice
+    assert cfg2["q_slab"] == cfg["q_slab"]
+    assert rel(again, out64) < 1e-12
