@@ -316,7 +316,7 @@ cudaError_t launch_delta(const DeltaArgs &a, int q_slab, bool uniform, cudaStrea
 {
     if (a.n_blocks == 0 || a.k == 0)
         return cudaSuccess;
-    switch (q_slab) {
+    switch (q_slab > 32 ? 32 : q_slab) { // two chains per pair: at most 32 q per slab
     case 8:
         return delta_qs<8>(a, uniform, st);
     case 16:
@@ -392,7 +392,7 @@ cudaError_t launch_adjoint(const DebyeArgs &a, int q_slab, bool uniform, bool wa
 {
     if (a.n_items == 0)
         return cudaSuccess;
-    switch (q_slab) {
+    switch (q_slab > 32 ? 32 : q_slab) { // the adjoint walks all q per pair in 32-q slabs
     case 8:
         return adjoint_qs<8>(a, uniform, water, st);
     case 16:
