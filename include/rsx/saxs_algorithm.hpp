@@ -1,0 +1,307 @@
+// rsx/saxs_algorithm.hpp -- header-only C++ adapter over the librsx C ABI
+// (include/rsx.h) with the shape of resaxslib's algorithm interface, so that
+// C++ callers of the reference switch by changing includes and the factory:
+//
+//   reference (resaxslib/include/saxs_algorithm.hpp:118-244)   here
+//   resaxs::algorithm::i_saxs<float, cl_base<float>>           rsx::algorithm::i_saxs<float>
+//   saxs_params::initialize(qq, bodies, devices, wf)           same signature (devices: CUDA ordinals)
+//   get_ff_params().access_factors() / set_water_ff_index     same
+//   get_implicit_water_params().set_water_weight / access_rsasa same
+//   initialize(); calc_curve(bodies, out); recalc_curve(...)   same
+//   commit(); revert()                                         same
+//   resaxs::error with codes -1..-6                            rsx::error, same codes
+//   create_saxs_ocl<float>()                                   rsx::algorithm::create_saxs_gpu()
+//   i_rsasa<float>::calc_rsasa / recalc_rsasa                  rsx::algorithm::rsasa_gpu
+//
+// Bodies are rsx_body (4 floats, the reference's cl_float4 layout with the
+// uint32 type bits in .w; utils.hpp:61-88).
+#ifndef RSX_SAXS_ALGORITHM_HPP
+#define RSX_SAXS_ALGORITHM_HPP
+
+#include "../rsx.h"
+
+#include <cstring>
+#include <exception>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace rsx {
+
+// resaxs::error (resaxslib/include/resaxs.hpp:187-221)
+class error : public std::exception {
+public:
+    enum code {
+        SAXS_INVALID_DEVICE = RSX_INVALID_DEVICE,
+        SAXS_ALG_NOT_INITIALIZED = RSX_ALG_NOT_INITIALIZED,
+        SAXS_INVALID_ARG = RSX_INVALID_ARG,
+        SAXS_PROGRAM_NOT_LOADED = RSX_PROGRAM_NOT_LOADED,
+        SAXS_ARGS_NOT_SET = RSX_ARGS_NOT_SET,
+        SAXS_NO_INITIAL_CALC = RSX_NO_INITIAL_CALC,
+    };
+    error(int err, std::string msg) : err_(err), msg_(std::move(msg)) {}
+    const char *what() const noexcept override { return msg_.empty() ? "empty" : msg_.c_str(); }
+    int err() const { return err_; }
+
+private:
+    int err_;
+    std::string msg_;
+};
+
+inline void check(rsx_status s)
+{
+    if (s != RSX_OK)
+        throw error(s, rsx_last_error());
+}
+
+inline void set_factor_index(rsx_body &b, unsigned index) { std::memcpy(&b.w, &index, 4); }
+inline unsigned get_factor_index(const rsx_body &b)
+{
+    unsigned t;
+    std::memcpy(&t, &b.w, 4);
+    return t;
+}
+
+namespace algorithm {
+
+// params_base (resaxslib/include/re_algorithm.hpp:66-89)
+class params_base {
+public:
+    virtual ~params_base() = default;
+    bool is_dirty() const { return dirty_; }
+    void clear_dirty() { dirty_ = false; }
+
+protected:
+    void set_dirty() { dirty_ = true; }
+
+private:
+    bool dirty_ = false;
+};
+
+template <typename FLT_T> class implicit_water_params : public params_base {
+public:
+    FLT_T water_weight_ = 0;
+    bool no_rsasa_recalc_ = false;
+    void set_water_weight(FLT_T w)
+    {
+        if (water_weight_ != w) {
+            water_weight_ = w;
+            this->set_dirty();
+        }
+    }
+    std::vector<FLT_T> &access_rsasa()
+    {
+        this->set_dirty();
+        return rsasa_;
+    }
+    const std::vector<FLT_T> &rsasa() const { return rsasa_; }
+
+private:
+    std::vector<FLT_T> rsasa_;
+};
+
+template <typename FLT_T> class form_factor_params : public params_base {
+public:
+    std::vector<FLT_T> factors_; // row-major [n_q][n_factors]
+    int water_ff_index_ = -1;
+    FLT_T expansion_factor_ = 1;
+    void set_water_ff_index(int index)
+    {
+        if (water_ff_index_ != index) {
+            water_ff_index_ = index;
+            this->set_dirty();
+        }
+    }
+    std::vector<FLT_T> &access_factors()
+    {
+        this->set_dirty();
+        return factors_;
+    }
+};
+
+template <typename FLT_T> struct saxs_params : public params_base {
+    std::vector<FLT_T> qq_;
+    unsigned n_bodies_ = 0;
+    int device_ = -1;
+    unsigned workgroup_size_ = 64; // accepted for interface parity; tiles are fixed
+    void initialize(const std::vector<FLT_T> &qq, const std::vector<rsx_body> &bodies,
+                    const std::vector<int> &devices = {}, unsigned workgroup_size = 64)
+    {
+        qq_ = qq;
+        n_bodies_ = (unsigned)bodies.size();
+        device_ = devices.empty() ? -1 : devices.front();
+        workgroup_size_ = workgroup_size;
+        this->set_dirty();
+    }
+    form_factor_params<FLT_T> &get_ff_params() { return ff_; }
+    implicit_water_params<FLT_T> &get_implicit_water_params() { return water_; }
+
+private:
+    form_factor_params<FLT_T> ff_;
+    implicit_water_params<FLT_T> water_;
+};
+
+// i_saxs<float> (resaxslib/include/saxs_algorithm.hpp:147-183) over rsx_debye
+template <typename FLT_T = float> class i_saxs {
+    static_assert(sizeof(FLT_T) == 4, "librsx computes in FP32 with FP64 reductions");
+
+public:
+    i_saxs() = default;
+    i_saxs(const i_saxs &) = delete;
+    i_saxs &operator=(const i_saxs &) = delete;
+    virtual ~i_saxs()
+    {
+        if (h_)
+            rsx_debye_destroy(h_);
+    }
+
+    saxs_params<FLT_T> &access_params() { return params_; }
+
+    void initialize()
+    {
+        if (params_.qq_.empty())
+            throw error(error::SAXS_ARGS_NOT_SET, "saxs_params::initialize() was not called");
+        auto &ff = params_.get_ff_params();
+        if (ff.factors_.empty() || ff.factors_.size() % params_.qq_.size())
+            throw error(error::SAXS_ARGS_NOT_SET, "form-factor table missing or malformed");
+        if (h_)
+            rsx_debye_destroy(h_);
+        h_ = nullptr;
+        rsx_debye_options o;
+        rsx_debye_default_options(&o);
+        o.device = params_.device_;
+        const int n_f = (int)(ff.factors_.size() / params_.qq_.size());
+        check(rsx_debye_create(params_.qq_.data(), (int)params_.qq_.size(), ff.factors_.data(),
+                               n_f, (int)params_.n_bodies_, &o, &h_));
+        ff.clear_dirty();
+        params_.get_implicit_water_params().set_water_weight(
+            params_.get_implicit_water_params().water_weight_);
+        computing_ = false;
+    }
+
+    void calc_curve(const std::vector<rsx_body> &bodies, std::vector<FLT_T> &out_Iqq)
+    {
+        require(h_ != nullptr, error::SAXS_ARGS_NOT_SET, "initialize() was not called");
+        require(bodies.size() == params_.n_bodies_, error::SAXS_INVALID_ARG,
+                "different number of bodies expected in calc_curve()");
+        push_params();
+        out_Iqq.resize(params_.qq_.size());
+        check(rsx_debye_calc(h_, bodies.data(), out_Iqq.data()));
+        computing_ = true;
+    }
+
+    void recalc_curve(const std::vector<rsx_body> &bodies, unsigned upd_start, unsigned upd_length,
+                      std::vector<FLT_T> &out_Iqq)
+    {
+        require(computing_, error::SAXS_NO_INITIAL_CALC,
+                "recalc_curve() called before an initial call to calc_curve()");
+        require(bodies.size() >= (size_t)upd_start + upd_length, error::SAXS_INVALID_ARG,
+                "bodies vector too small in recalc_curve()");
+        push_params();
+        out_Iqq.resize(params_.qq_.size());
+        check(rsx_debye_recalc_range(h_, bodies.data(), upd_start, upd_length, out_Iqq.data()));
+    }
+
+    void commit()
+    {
+        require(computing_, error::SAXS_NO_INITIAL_CALC,
+                "commit() called before an initial call to calc_curve()");
+        check(rsx_debye_commit(h_));
+    }
+
+    void revert()
+    {
+        require(computing_, error::SAXS_NO_INITIAL_CALC,
+                "revert() called before an initial call to calc_curve()");
+        check(rsx_debye_revert(h_));
+    }
+
+    rsx_debye *handle() { return h_; }
+
+private:
+    static void require(bool c, int code, const char *msg)
+    {
+        if (!c)
+            throw error(code, msg);
+    }
+
+    void push_params()
+    {
+        auto &ff = params_.get_ff_params();
+        auto &w = params_.get_implicit_water_params();
+        if (ff.is_dirty()) {
+            const int n_f = (int)(ff.factors_.size() / params_.qq_.size());
+            check(rsx_debye_set_factors(h_, ff.factors_.data(), n_f));
+            ff.clear_dirty();
+        }
+        if (w.is_dirty()) {
+            const int widx = ff.water_ff_index_ >= 0 ? ff.water_ff_index_ : 0;
+            const auto &rs = w.rsasa();
+            check(rsx_debye_set_water(h_, (float)w.water_weight_, widx,
+                                      rs.size() >= params_.n_bodies_ ? rs.data() : nullptr));
+            w.clear_dirty();
+        }
+    }
+
+    saxs_params<FLT_T> params_;
+    rsx_debye *h_ = nullptr;
+    bool computing_ = false;
+};
+
+// create_saxs_ocl<float>() (saxs_algorithm.hpp:240-244) counterpart
+inline std::unique_ptr<i_saxs<float>> create_saxs_gpu() { return std::make_unique<i_saxs<float>>(); }
+
+// i_rsasa<float> (resaxslib/include/rsasa_algorithm.hpp:42-61) over rsx_sasa,
+// with one radius per body type as the reference (rsasa_cl_gpu_alg.cpp:139-151).
+class rsasa_gpu {
+public:
+    ~rsasa_gpu()
+    {
+        if (h_)
+            rsx_sasa_destroy(h_);
+    }
+    void initialize(unsigned n_atoms, const std::vector<float> &radius_of_type, float probe_radius,
+                    const std::vector<float> &unit_dots, int device = -1)
+    {
+        if (h_)
+            rsx_sasa_destroy(h_);
+        h_ = nullptr;
+        radii_ = radius_of_type;
+        check(rsx_sasa_create((int)n_atoms, unit_dots.data(), (int)(unit_dots.size() / 3),
+                              probe_radius, device, &h_));
+        n_ = n_atoms;
+    }
+    void calc_rsasa(const std::vector<rsx_body> &atoms, std::vector<float> &rsasa)
+    {
+        if (!h_)
+            throw error(error::SAXS_ARGS_NOT_SET, "initialize() was not called");
+        if (rsasa.size() < atoms.size())
+            throw error(error::SAXS_INVALID_ARG, "rsasa vector too small");
+        std::vector<float> r(atoms.size());
+        for (size_t i = 0; i < atoms.size(); ++i) {
+            const unsigned t = get_factor_index(atoms[i]);
+            if (t >= radii_.size())
+                throw error(error::SAXS_INVALID_ARG, "atom type without a radius");
+            r[i] = radii_[t];
+        }
+        check(rsx_sasa_calc(h_, atoms.data(), r.data(), rsasa.data()));
+        computing_ = true;
+    }
+    void recalc_rsasa(const std::vector<rsx_body> &atoms, std::vector<float> &rsasa)
+    {
+        if (!computing_)
+            throw error(error::SAXS_NO_INITIAL_CALC, "recalc_rsasa() before calc_rsasa()");
+        calc_rsasa(atoms, rsasa);
+    }
+
+private:
+    rsx_sasa *h_ = nullptr;
+    unsigned n_ = 0;
+    std::vector<float> radii_;
+    bool computing_ = false;
+};
+
+} // namespace algorithm
+} // namespace rsx
+
+#endif

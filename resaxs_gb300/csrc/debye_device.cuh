@@ -40,7 +40,11 @@ __device__ __forceinline__ void kahan_add(float &acc, float &comp, float x)
 }
 
 // Distance terms of one pair: r and 1/r with r >= 1e-6 (coincident bodies
-// then give sinc = 1, as the reference's device kernel does).
+// then give sinc = 1, as the reference's device kernel does).  Both are
+// correctly rounded (IEEE sqrt and division): the hardware reciprocal square
+// root approximation has a systematic error that, over 1e10 pairs, shifts
+// I(q) at high q by ~1e-4 relative (measured against the FP64 oracle at
+// 50,000 and 200,000 bodies); the rounded forms cost ~10% of the forward.
 __device__ __forceinline__ void pair_r(const float4 &a, const float4 &b, float &r, float &rinv,
                                        float &dx, float &dy, float &dz)
 {
@@ -49,8 +53,8 @@ __device__ __forceinline__ void pair_r(const float4 &a, const float4 &b, float &
     dz = b.z - a.z;
     float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
     r2 = fmaxf(r2, 1e-12f);
-    rinv = rsqrtf(r2);
-    r = r2 * rinv;
+    r = __fsqrt_rn(r2);
+    rinv = __frcp_rn(r);
 }
 
 // ----------------------------------------------------------------------------

