@@ -22,8 +22,8 @@ extern "C" {
  * (resaxslib/src/host_debye.cpp:54-109) without the N*N distance matrix.
  * I(q) = sum_i f_i^2 + 2 sum_{i<j} f_i f_j sinc(q r_ij), sinc = 1 when q*r == 0
  * (gpu_saxs_pt_wf.cl:55 maps the 0/0 case to 1; host_debye.cpp:93 for q == 0).
- * Uses the oracle's own FP64 sine (range reduction + Taylor series, relative
- * error ~1e-16) in vectorisable loops.
+ * Uses the oracle's own FP64 sine (reduction modulo 2*pi + Taylor series;
+ * the curve agrees with the libm form to ~1e-14 relative) in vectorisable loops.
  * Effective factor with the implicit water layer (gpu_saxs_pt_wf.cl:130-138):
  *   f_i(q) = F[q][t_i] + rsasa_i * (F[q][water_index] * water_weight).
  * rsasa may be NULL (no water).  n_threads <= 0 uses every online core. */
