@@ -187,6 +187,23 @@ rsx_status rsx_debye_chi2_backward(rsx_debye *h, const float *target, const floa
 /* Tuning in effect: q-slab, work items, whether the uniform-q recurrence is used. */
 rsx_status rsx_debye_config(rsx_debye *h, int *q_slab, int *n_items, int *uniform_q);
 
+/* Form-factor tables (host side, no GPU): resaxs::atomic_form_factors<float>
+ * (resaxslib/include/ff_coef.hpp:104-212) for the reference's 16 atom types
+ * H C N O P S Zn CH CH2 CH3 NH NH2 NH3 OH OH2 SH (constants.hpp:37-59). ---- */
+
+/* Number of atom types (16) and the index of the water group OH2 (14). */
+int rsx_ff_type_count(void);
+int rsx_ff_water_index(void);
+/* atomic_form_factors::generate(v_q, avg_radius, c, t_factors)
+ * (ff_coef.hpp:112-162): out is [n_q][16], vacuum minus excluded-volume
+ * factors with expansion factor c (1 = none). */
+rsx_status rsx_ff_atomic_table(const float *q, int n_q, float avg_radius, float expansion_factor,
+                               float *out);
+/* atomic_form_factors::calc_radii (ff_coef.hpp:164-188): 16 radii in A. */
+rsx_status rsx_ff_radii(float *out);
+/* atomic_form_factors::calc_avg_radius (ff_coef.hpp:190-198). */
+rsx_status rsx_ff_avg_radius(const rsx_body *bodies, int n, float *out);
+
 /* Dot-sphere SASA: replaces resaxs::algorithm::i_rsasa<float,float,cl_base>
  * implemented by rsasa_cl_gpu (resaxslib/include/rsasa_algorithm.hpp:42-61,
  * resaxslib/src/rsasa_cl_gpu_alg.cpp, kernel rsasa_dot_spheres.cl:94-163) ---- */

@@ -26,3 +26,23 @@ extern "C" void ref_host_debye_dd(const double *q, int n_q, const double *bodies
     resaxs::host_debye<double, double, cl_double4>::calc_curve(
         q, n_q, reinterpret_cast<const cl_double4 *>(bodies), n_bodies, ff, n_factors, out);
 }
+
+// Form-factor tables of the reference (header-only resaxslib/include/ff_coef.hpp:104-212).
+#include "ff_coef.hpp"
+
+extern "C" void ref_ff_generate(const float *q, int n_q, float avg_radius, float expansion,
+                                float *out /* [n_q][16] */)
+{
+    std::vector<float> qq(q, q + n_q), t;
+    resaxs::atomic_form_factors<float>::generate(qq, avg_radius, expansion, t);
+    for (size_t i = 0; i < t.size(); ++i)
+        out[i] = t[i];
+}
+
+extern "C" void ref_ff_radii(float *out /* [16] */)
+{
+    std::vector<float> r;
+    resaxs::atomic_form_factors<float>::calc_radii(r);
+    for (size_t i = 0; i < r.size(); ++i)
+        out[i] = r[i];
+}

@@ -93,6 +93,11 @@ SIGNATURES = [
                                       _vp]),
     ("rsx_debye_config", _st, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i),
                                ctypes.POINTER(_i)]),
+    ("rsx_ff_type_count", _i, []),
+    ("rsx_ff_water_index", _i, []),
+    ("rsx_ff_atomic_table", _st, [_f32p, _i, ctypes.c_float, ctypes.c_float, _f32p]),
+    ("rsx_ff_radii", _st, [_f32p]),
+    ("rsx_ff_avg_radius", _st, [_f32p, _i, ctypes.POINTER(ctypes.c_float)]),
     ("rsx_sasa_fibonacci_dots", _st, [_i, _f32p]),
     ("rsx_sasa_dodeca_icosa_dots", _st, [_f32p]),
     ("rsx_sasa_create", _st, [_i, _f32p, _i, ctypes.c_float, _i, ctypes.POINTER(_vp)]),

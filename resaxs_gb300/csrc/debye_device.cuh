@@ -76,12 +76,16 @@ struct PairSeed {
     bool big;
 };
 
-__device__ __forceinline__ PairSeed pair_seed(float x0, float th, float sc)
+__device__ __forceinline__ PairSeed pair_seed(float q0, float dq, float r, float sc)
 {
     PairSeed p;
     float s0, c0, sh, ch;
-    sincos_rr(x0, s0, c0);
-    sincos_any(0.5f * th, sh, ch);
+    sincos_prod(q0, r, s0, c0);                 // x0 = q0 r, exactly
+    {
+        const float th = dq * r;                // theta = dq r, exactly as th + th_lo
+        const float th_lo = fmaf(dq, r, -th);
+        sincos_rr2(0.5f * th, 0.5f * th_lo, sh, ch);
+    }
     p.big = ch * ch < sh * sh;
     p.s = s0 * sc;
     if (!p.big) {
@@ -234,8 +238,8 @@ __device__ __forceinline__ void forward_item(const DebyeArgs &a, int item_idx, i
                 pair_r(pi, s_pos[jj + 1], r2, ri2, dx, dy, dz);
                 const bool u1 = valid_i && (!diag || jj > tid);
                 const bool u2 = valid_i && (!diag || jj + 1 > tid);
-                const PairSeed p1 = pair_seed(q0 * r1, dq * r1, u1 ? ri1 : 0.f);
-                const PairSeed p2 = pair_seed(q0 * r2, dq * r2, u2 ? ri2 : 0.f);
+                const PairSeed p1 = pair_seed(q0, dq, r1, u1 ? ri1 : 0.f);
+                const PairSeed p2 = pair_seed(q0, dq, r2, u2 ? ri2 : 0.f);
                 if (!p1.big && !p2.big) {
                     pair2_slab<QS>(p1, p2, S);
                 } else {
@@ -251,13 +255,13 @@ __device__ __forceinline__ void forward_item(const DebyeArgs &a, int item_idx, i
             const float sc = use ? rinv : 0.f;
             const float rs_j = WATER ? s_rs[jj] : 0.f;
             if (UNIFORM) {
-                const PairSeed p = pair_seed(q0 * r, dq * r, sc);
+                const PairSeed p = pair_seed(q0, dq, r, sc);
                 pair_slab<QS, WATER>(p, rs_j, S, SW);
             } else {
 #pragma unroll
                 for (int k = 0; k < QS; ++k) {
                     float sk, ck;
-                    sincos_rr(s_q[k] * r, sk, ck);
+                    sincos_prod(s_q[k], r, sk, ck);
                     const float v = sk * sc;
                     S[k] += v;
                     if (WATER)
@@ -386,12 +390,12 @@ __device__ __forceinline__ void adjoint_item(const DebyeArgs &a, int item_idx, i
             float A = 0.f, B = 0.f;
             float sd = 0.f, cd = 1.f;
             if (UNIFORM)
-                sincos_any(dq * r, sd, cd);
+                sincos_prod(dq, r, sd, cd);
             for (int sl = 0; sl < n_slabs; ++sl) {
                 const int kb = sl * QS;
                 if (UNIFORM) {
                     float s, c;
-                    sincos_rr(a.q[min(kb, a.n_q - 1)] * r, s, c);
+                    sincos_prod(a.q[min(kb, a.n_q - 1)], r, s, c);
 #pragma unroll
                     for (int k = 0; k < QS; ++k) {
                         float al, be;
@@ -421,7 +425,7 @@ __device__ __forceinline__ void adjoint_item(const DebyeArgs &a, int item_idx, i
                         if (kk >= a.n_q)
                             break;
                         float s, c;
-                        sincos_rr(a.q[kk] * r, s, c);
+                        sincos_prod(a.q[kk], r, s, c);
                         float al, be;
                         if (WATER) {
                             const float *cf = coef + 8 * kk;

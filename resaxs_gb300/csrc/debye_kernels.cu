@@ -147,8 +147,8 @@ __global__ void __launch_bounds__(kBlockAtoms) delta_kernel(const DeltaArgs a)
             if (UNIFORM) {
                 // the old pair is seeded with -1/r so that the two chains
                 // accumulate new - old directly
-                const PairSeed pn = pair_seed(q0 * rn, dq * rn, scn);
-                const PairSeed po = pair_seed(q0 * ro, dq * ro, -sco);
+                const PairSeed pn = pair_seed(q0, dq, rn, scn);
+                const PairSeed po = pair_seed(q0, dq, ro, -sco);
                 float dummy[1];
                 if (!pn.big && !po.big) {
                     pair2_slab<QS>(pn, po, S);
@@ -160,8 +160,8 @@ __global__ void __launch_bounds__(kBlockAtoms) delta_kernel(const DeltaArgs a)
 #pragma unroll
                 for (int k = 0; k < QS; ++k) {
                     float s1, c1, s2, c2;
-                    sincos_rr(s_q[k] * rn, s1, c1);
-                    sincos_rr(s_q[k] * ro, s2, c2);
+                    sincos_prod(s_q[k], rn, s1, c1);
+                    sincos_prod(s_q[k], ro, s2, c2);
                     S[k] += s1 * scn - s2 * sco;
                 }
             }

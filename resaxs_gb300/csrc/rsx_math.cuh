@@ -51,25 +51,28 @@ __device__ __forceinline__ void sincos_poly(float r, float &s, float &c)
     c = fmaf(r2, pc, 1.0f);
 }
 
-// sin(x), cos(x) with the reduction split in two parts so that no FP32
-// rounding sees a constant offset.  r = x - n*pi/2 is carried as
-// r_hi = x - n*P1 (exact: both terms are multiples of 2^-23 and the
-// difference is below 1 in magnitude) plus r_lo = -n*P2 (P3 lies below FP32
-// resolution here).  Adding r_lo to r_hi directly would round every argument
-// of a binade the same way (r_lo is nearly constant while r_hi sits on the
-// FP32 grid), a bias of ~0.5 ulp that is invisible per term but coherent over
-// 1e10 pair terms.  Instead r_lo enters through the first-order terms
-// sin(r_hi + r_lo) = sin(r_hi) + r_lo cos(r_hi), cos(...) = cos(r_hi) - r_lo sin(r_hi),
-// which are added to the small, continuously varying parts of the series
-// before the single final addition of r_hi (resp. 1).
-// Accuracy: about 1 ulp, mean error over uniformly distributed arguments
+// sin and cos of the unevaluated sum x_hi + x_lo (|x_lo| <= ulp(x_hi)),
+// with the reduction split so that no FP32 rounding sees a constant offset.
+// r = x - n*pi/2 is carried as r_hi = x_hi - n*P1 (exact: both terms are
+// multiples of 2^-23 and the difference is below 1 in magnitude) plus
+// r_lo = x_lo - n*P2 (P3 lies below FP32 resolution here).  Adding r_lo to
+// r_hi directly would round every argument of a binade the same way (r_lo is
+// nearly constant while r_hi sits on the FP32 grid), a bias of ~0.5 ulp that
+// is invisible per term but coherent over 1e10 pair terms.  Instead r_lo
+// enters through the first-order terms
+//   sin(r_hi + r_lo) = sin(r_hi) + r_lo cos(r_hi),  cos(...) = cos(r_hi) - r_lo sin(r_hi),
+// added to the small, continuously varying parts of the series before the
+// single final addition of r_hi (resp. 1).  Callers pass the exact rounding
+// error of the product that formed the argument as x_lo (x = q*r:
+// x_lo = fma(q, r, -x)), which removes the phase rounding the same way.
+// Accuracy about 1 ulp; mean error over uniformly distributed arguments
 // indistinguishable from zero (< 1e-11).  Valid for |x * 2/pi| < 2^22.
-__device__ __forceinline__ void sincos_rr(float x, float &s, float &c)
+__device__ __forceinline__ void sincos_rr2(float x, float x_lo, float &s, float &c)
 {
     const float t = fmaf(x, kTwoOverPi, kRound);
     const float fn = t - kRound;
     const float rh = fmaf(-fn, kPio2P1, x);
-    const float rl = -fn * kPio2P2;
+    const float rl = fmaf(-fn, kPio2P2, x_lo);
     const float r2 = rh * rh;
     float ps = fmaf(r2, kS4, kS3);
     ps = fmaf(r2, ps, kS2);
@@ -94,13 +97,13 @@ __device__ __forceinline__ void sincos_rr(float x, float &s, float &c)
     c = __uint_as_float(__float_as_uint(cv) ^ sgn_c);
 }
 
-// Same, taking the cheap path when the argument is already reduced.
-__device__ __forceinline__ void sincos_any(float x, float &s, float &c)
+__device__ __forceinline__ void sincos_rr(float x, float &s, float &c) { sincos_rr2(x, 0.0f, s, c); }
+
+// sin and cos of the product a*b, its rounding error folded in exactly.
+__device__ __forceinline__ void sincos_prod(float a, float b, float &s, float &c)
 {
-    if (fabsf(x) <= kPio4)
-        sincos_poly(x, s, c);
-    else
-        sincos_rr(x, s, c);
+    const float x = a * b;
+    sincos_rr2(x, fmaf(a, b, -x), s, c);
 }
 
 } // namespace rsx

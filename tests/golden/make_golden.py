@@ -14,6 +14,9 @@ Outputs (committed; the GPU machine has no reference tree):
   ``iq_ref_dd`` = host_debye<double,double>.
 * ``synthetic_ref.npz`` -- small seeded synthetic cases and the outputs of the
   compiled reference host_debye<double,float> and <double,double> on them.
+* ``ff_ref.npz`` -- form-factor tables and radii of the reference's
+  atomic_form_factors (resaxslib/include/ff_coef.hpp) for q = 0..0.75 (500
+  points) and three (expansion factor, mean radius) pairs.
 """
 from __future__ import annotations
 
@@ -79,6 +82,23 @@ def main(ref_root="/root/reference"):
         cases[name + "_iq_ref_df"] = ref_df(w.q, w.bodies, w.ff)
         cases[name + "_iq_ref_dd"] = ref_dd(w.q, w.bodies, w.ff)
     np.savez_compressed(os.path.join(HERE, "synthetic_ref.npz"), **cases)
+    # form-factor tables of the reference (ff_coef.hpp) for the CLI's q grid
+    L = oracle.ref_lib()
+    import ctypes
+    f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+    L.ref_ff_generate.argtypes = [f32p, ctypes.c_int, ctypes.c_float, ctypes.c_float, f32p]
+    L.ref_ff_radii.argtypes = [f32p]
+    qq = np.linspace(0.0, 0.75, 500).astype(np.float32)
+    ff_cases = {"q": qq}
+    for name, c, rm in (("c100", 1.0, 1.6), ("c103", 1.03, 1.65), ("c095", 0.95, 1.5)):
+        out = np.zeros(len(qq) * 16, np.float32)
+        L.ref_ff_generate(qq, len(qq), ctypes.c_float(rm), ctypes.c_float(c), out)
+        ff_cases[name] = out.reshape(len(qq), 16)
+        ff_cases[name + "_args"] = np.array([c, rm], np.float32)
+    radii = np.zeros(16, np.float32)
+    L.ref_ff_radii(radii)
+    ff_cases["radii"] = radii
+    np.savez_compressed(os.path.join(HERE, "ff_ref.npz"), **ff_cases)
     print("wrote", os.listdir(HERE))
 
 
