@@ -87,6 +87,29 @@ rsx_status rsx_calc_saxs_curve_status(const float *v_q, int n_q, const rsx_body 
                                       int n_bodies, const float *t_factors, int n_factors,
                                       float *out_v_Iq);
 
+/* Debye curve without any device allocation, for callers that cannot
+ * allocate: code running inside a host framework that owns all device memory
+ * through its own pool and forbids cudaMalloc from plug-ins, or work queued on
+ * a stream whose scheduler must see no allocator calls.  No counterpart in the
+ * reference.  All pointers are DEVICE pointers the caller owns: d_q (n_q
+ * floats), d_bodies (n_bodies bodies, caller order), d_factors
+ * ([n_q][n_factors]) and d_out_iq (n_q floats); `stream` is a cudaStream_t
+ * (NULL = legacy default stream) on the current device.  Same sum as
+ * rsx_calc_saxs_curve, to the same 1e-5 tolerance, but several times slower
+ * (caller-order bodies, one range-reduced sine per pair and q).
+ * Working memory is one static 8 MiB device array per GPU that loads librsx,
+ * held until process exit; problems need ceil(n_bodies/128) * n_q <= 1048544
+ * (larger ones are rejected with RSX_INVALID_ARG before any launch).
+ * The first call on a device looks up that array's device address (with the
+ * device current); make that first call before any stream capture.  Every
+ * call reuses the array and leaves its contents behind; calls that overlap on
+ * the GPU (several streams, threads or devices sharing a context) race on it
+ * and must be serialised by the caller.  Returns after the stream finished
+ * the call (the error word of the array is read back). */
+rsx_status rsx_calc_saxs_curve_device_noalloc(const float *d_q, int n_q, const rsx_body *d_bodies,
+                                              int n_bodies, const float *d_factors, int n_factors,
+                                              float *d_out_iq, void *stream);
+
 /* Debye algorithm handle: replaces resaxs::algorithm::i_saxs<float, cl_base>
  * implemented by saxs_cl_gpu<float> (resaxslib/include/saxs_algorithm.hpp:147-183,
  * resaxslib/src/saxs_alg_cl_gpu_pt_wf.cpp) ----------------------------- */

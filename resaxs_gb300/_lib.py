@@ -68,6 +68,7 @@ SIGNATURES = [
                                ctypes.POINTER(_i), ctypes.POINTER(_i)]),
     ("rsx_calc_saxs_curve", None, [_f32p, _i, _f32p, _i, _f32p, _i, _f32p]),
     ("rsx_calc_saxs_curve_status", _st, [_f32p, _i, _f32p, _i, _f32p, _i, _f32p]),
+    ("rsx_calc_saxs_curve_device_noalloc", _st, [_vp, _i, _vp, _i, _vp, _i, _vp, _vp]),
     ("rsx_debye_default_options", None, [ctypes.POINTER(DebyeOptions)]),
     ("rsx_autotune_clear", None, []),
     ("rsx_debye_create", _st, [_f32p, _i, _f32p, _i, _i, ctypes.POINTER(DebyeOptions),

@@ -8,18 +8,28 @@
 namespace rsx {
 
 static thread_local std::string t_last_error;
+// set by fail_static (no heap allocation); cleared by fail() and ok()
+static thread_local const char *t_static_error = nullptr;
 static std::mutex g_fault_mu;
 static int g_fault_kind = -1;
 static int g_fault_left = 0;
 
 rsx_status fail(rsx_status st, const std::string &msg)
 {
+    t_static_error = nullptr;
     t_last_error = msg;
+    return st;
+}
+
+rsx_status fail_static(rsx_status st, const char *msg)
+{
+    t_static_error = msg;
     return st;
 }
 
 rsx_status ok()
 {
+    t_static_error = nullptr;
     t_last_error.clear();
     return RSX_OK;
 }
@@ -149,7 +159,10 @@ const char *rsx_version(void)
     return v.c_str();
 }
 
-const char *rsx_last_error(void) { return rsx::t_last_error.c_str(); }
+const char *rsx_last_error(void)
+{
+    return rsx::t_static_error ? rsx::t_static_error : rsx::t_last_error.c_str();
+}
 
 unsigned long long rsx_launch_count(void) { return rsx::launch_count(); }
 

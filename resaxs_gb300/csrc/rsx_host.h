@@ -11,6 +11,8 @@ namespace rsx {
 
 // Records `msg` as this thread's last error and returns `st`.
 rsx_status fail(rsx_status st, const std::string &msg);
+// Records a static message (no heap allocation) and returns `st`.
+rsx_status fail_static(rsx_status st, const char *msg);
 // Clears the last error; returns RSX_OK.
 rsx_status ok();
 // Maps a CUDA error to a status (RSX_OK when e == cudaSuccess).
