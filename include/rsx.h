@@ -43,6 +43,7 @@ typedef int rsx_status;
 #define RSX_TIMEOUT -102           /* a bounded device-side wait gave up */
 #define RSX_NOT_SUPPORTED -103     /* valid request this build does not implement */
 #define RSX_INJECTED_FAULT -104    /* failure produced by the host fault-injection hook */
+#define RSX_PDB_FILE_NOT_FOUND -1100 /* SAXS_PDB_FILE_NOT_FOUND (resaxslib/include/parse_pdb.hpp:30) */
 
 /* Body as 4 floats (x, y, z, type bits). */
 typedef struct rsx_body {
@@ -226,6 +227,19 @@ rsx_status rsx_ff_atomic_table(const float *q, int n_q, float avg_radius, float 
 rsx_status rsx_ff_radii(float *out);
 /* atomic_form_factors::calc_avg_radius (ff_coef.hpp:190-198). */
 rsx_status rsx_ff_avg_radius(const rsx_body *bodies, int n, float *out);
+
+/* PDB input of calc_saxs: parse_pdb<float>::all_models_as_complex_atoms
+ * (resaxslib/include/parse_pdb.hpp:36-53, resaxslib/src/parse_pdb.cpp:63-108,
+ * 309-363).  Every model of the file as complex-atom bodies: waters, hydrogens
+ * and alternate locations other than ' '/'A' are dropped, atoms get their
+ * group type (CH, NH2, ...) from the reference's atom tables.  rsx_pdb_count
+ * gives the sizes; rsx_pdb_read writes the models back to back into out and
+ * their body counts into model_sizes.  verbose >= 1 prints the reference's
+ * warning for unknown elements on stderr.  A missing file returns
+ * RSX_PDB_FILE_NOT_FOUND. */
+rsx_status rsx_pdb_count(const char *path, int *n_models, int *n_bodies);
+rsx_status rsx_pdb_read(const char *path, int verbose, rsx_body *out, int cap_bodies,
+                        int *model_sizes, int max_models);
 
 /* Dot-sphere SASA: replaces resaxs::algorithm::i_rsasa<float,float,cl_base>
  * implemented by rsasa_cl_gpu (resaxslib/include/rsasa_algorithm.hpp:42-61,

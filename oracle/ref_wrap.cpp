@@ -46,3 +46,35 @@ extern "C" void ref_ff_radii(float *out /* [16] */)
     for (size_t i = 0; i < r.size(); ++i)
         out[i] = r[i];
 }
+
+// PDB reader of the reference (resaxslib/src/parse_pdb.cpp:63-108, 309-363 with
+// the atom maps of resaxslib/src/utils.cpp:200-317), compiled from those
+// unmodified files.  Writes the bodies of all models back to back (x, y, z,
+// type bits) and the body count of each model; returns the number of models,
+// -1 when the file cannot be opened, -2 when out or model_sizes is too small.
+#include "parse_pdb.hpp"
+
+extern "C" int ref_parse_pdb(const char *path, float *out, int cap_bodies, int *model_sizes,
+                             int max_models)
+{
+    try {
+        resaxs::parse_pdb<float> p(path);
+        p.set_verbose_level(resaxs::parse_pdb<float>::QUIET);
+        auto models = p.all_models_as_complex_atoms();
+        if ((int)models.size() > max_models)
+            return -2;
+        int k = 0;
+        for (size_t m = 0; m < models.size(); ++m) {
+            model_sizes[m] = (int)models[m].size();
+            for (const auto &b : models[m]) {
+                if (k >= cap_bodies)
+                    return -2;
+                std::memcpy(out + 4 * k, b.s, 16);
+                ++k;
+            }
+        }
+        return (int)models.size();
+    } catch (...) {
+        return -1;
+    }
+}

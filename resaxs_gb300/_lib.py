@@ -26,6 +26,7 @@ RSX_OUT_OF_MEMORY = -101
 RSX_TIMEOUT = -102
 RSX_NOT_SUPPORTED = -103
 RSX_INJECTED_FAULT = -104
+RSX_PDB_FILE_NOT_FOUND = -1100
 
 
 class LibraryNotBuilt(RuntimeError):
@@ -99,6 +100,8 @@ SIGNATURES = [
     ("rsx_ff_atomic_table", _st, [_f32p, _i, ctypes.c_float, ctypes.c_float, _f32p]),
     ("rsx_ff_radii", _st, [_f32p]),
     ("rsx_ff_avg_radius", _st, [_f32p, _i, ctypes.POINTER(ctypes.c_float)]),
+    ("rsx_pdb_count", _st, [ctypes.c_char_p, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
+    ("rsx_pdb_read", _st, [ctypes.c_char_p, _i, _f32p, _i, np.ctypeslib.ndpointer(np.int32), _i]),
     ("rsx_sasa_fibonacci_dots", _st, [_i, _f32p]),
     ("rsx_sasa_dodeca_icosa_dots", _st, [_f32p]),
     ("rsx_sasa_create", _st, [_i, _f32p, _i, ctypes.c_float, _i, ctypes.POINTER(_vp)]),

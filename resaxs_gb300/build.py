@@ -25,7 +25,8 @@ GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 CUDA_SOURCES = ["debye_kernels.cu", "sasa_kernels.cu", "batch_kernels.cu", "calib_kernels.cu",
                 "noalloc_kernels.cu"]
 HOST_SOURCES = ["rsx_common.cpp", "rsx_debye.cpp", "rsx_sasa.cpp", "rsx_batch.cpp",
-                "rsx_ff.cpp", "rsx_autotune.cpp"]
+                "rsx_ff.cpp", "rsx_autotune.cpp",
+                "rsx_pdb.cpp"]
 
 
 def nvcc() -> str:
@@ -74,7 +75,7 @@ def build_cli(verbose: bool = False) -> str | None:
     os.makedirs(BIN_DIR, exist_ok=True)
     exe = os.path.join(BIN_DIR, "calc_saxs")
     cmd = ["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), src,
-           "-o", exe, f"-L{PKG}", "-lrsx", f"-Wl,-rpath,{PKG}", "-lpthread"]
+           "-o", exe, f"-L{PKG}", "-lrsx", "-Wl,-rpath,$ORIGIN/..", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"CLI build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

@@ -214,3 +214,88 @@ def batch_members(n_members: int = 256, seed: int = 0, n_lo: int = 1000, n_hi: i
         xyz = confined_chain(int(n), r, rg * math.sqrt(5 / 3))
         members.append(pack_bodies(xyz, draw_types(int(n), r, TYPE_P5)))
     return q, ff, members
+
+
+# ----------------------------------------------------------------------------
+# synthetic PDB files (input of the calc_saxs CLI)
+# ----------------------------------------------------------------------------
+
+# heavy atoms of the 20 standard residues (PDB atom names)
+RESIDUE_ATOMS = {
+    "ALA": ["CB"], "ARG": ["CB", "CG", "CD", "NE", "CZ", "NH1", "NH2"],
+    "ASN": ["CB", "CG", "OD1", "ND2"], "ASP": ["CB", "CG", "OD1", "OD2"],
+    "CYS": ["CB", "SG"], "GLN": ["CB", "CG", "CD", "OE1", "NE2"],
+    "GLU": ["CB", "CG", "CD", "OE1", "OE2"], "GLY": [],
+    "HIS": ["CB", "CG", "ND1", "CD2", "CE1", "NE2"], "ILE": ["CB", "CG1", "CG2", "CD1"],
+    "LEU": ["CB", "CG", "CD1", "CD2"], "LYS": ["CB", "CG", "CD", "CE", "NZ"],
+    "MET": ["CB", "CG", "SD", "CE"],
+    "PHE": ["CB", "CG", "CD1", "CD2", "CE1", "CE2", "CZ"], "PRO": ["CB", "CG", "CD"],
+    "SER": ["CB", "OG"], "THR": ["CB", "OG1", "CG2"],
+    "TRP": ["CB", "CG", "CD1", "CD2", "NE1", "CE2", "CE3", "CZ2", "CZ3", "CH2"],
+    "TYR": ["CB", "CG", "CD1", "CD2", "CE1", "CE2", "CZ", "OH"],
+    "VAL": ["CB", "CG1", "CG2"],
+}
+
+
+def _pdb_atom_line(rec, serial, name, alt, res, chain, resseq, xyz, element, short=False):
+    # PDB columns: name in 13-16 (1-letter elements start in column 14)
+    nm = (" " + name) if len(name) < 4 and len(element.strip()) <= 1 else name
+    line = (f"{rec:<6}{serial % 100000:>5} {nm:<4}{alt}{res:>3} {chain}{resseq % 10000:>4}    "
+            f"{xyz[0]:8.3f}{xyz[1]:8.3f}{xyz[2]:8.3f}{1.0:6.2f}{20.0:6.2f}")
+    if short:
+        return line
+    return line + " " * 10 + f"{element:>2}  "
+
+
+def write_synthetic_pdb(path: str, n_residues: int = 60, n_models: int = 2, seed: int = 0,
+                        quirks: bool = True) -> None:
+    """Writes a protein-like PDB file: a random-walk backbone of standard
+    residues with their heavy atoms (and some hydrogens) placed around each
+    residue, one MODEL per conformation.  With ``quirks`` it also holds the
+    records and fields the reader must skip or map: waters, alternate
+    locations, hydrogens, a HETATM zinc, an unknown element, a blank element
+    field, lines without element columns and an over-long line."""
+    rng = np.random.default_rng(seed)
+    names = sorted(RESIDUE_ATOMS)
+    seq = [names[i] for i in rng.integers(0, len(names), n_residues)]
+    base = random_walk_chain(n_residues, rng, step=3.8)
+    lines = ["HEADER    SYNTHETIC TEST STRUCTURE", "REMARK   1 GENERATED"]
+    for m in range(n_models):
+        ca = base + rng.normal(0.0, 0.4 * m, base.shape)
+        lines.append(f"MODEL     {m + 1:>4}")
+        serial = 1
+        for r, res in enumerate(seq):
+            atoms = ["N", "CA", "C", "O"] + RESIDUE_ATOMS[res]
+            for a in atoms:
+                xyz = ca[r] + rng.normal(0.0, 1.2, 3)
+                el = "S" if a[0] == "S" else a[0]
+                short = quirks and rng.random() < 0.05
+                if quirks and rng.random() < 0.05:
+                    el = " "  # blank element field
+                lines.append(_pdb_atom_line("ATOM", serial, a, " ", res, "A", r + 1, xyz, el,
+                                            short=short))
+                serial += 1
+            if quirks and r % 7 == 3:  # alternate locations: A kept, B dropped
+                xyz = ca[r] + rng.normal(0.0, 1.2, 3)
+                lines.append(_pdb_atom_line("ATOM", serial, "CB", "A", res, "A", r + 1, xyz, "C"))
+                lines.append(_pdb_atom_line("ATOM", serial + 1, "CB", "B", res, "A", r + 1,
+                                            xyz + 0.3, "C"))
+                serial += 2
+            if quirks and r % 5 == 1:  # hydrogens are skipped
+                lines.append(_pdb_atom_line("ATOM", serial, "HA", " ", res, "A", r + 1,
+                                            ca[r] + 1.0, "H"))
+                serial += 1
+        if quirks:
+            lines.append("TER")
+            lines.append(_pdb_atom_line("HETATM", serial, "ZN", " ", " ZN", "A", 900,
+                                        ca[0] + 2.0, "Zn"))
+            lines.append(_pdb_atom_line("HETATM", serial + 1, "FE", " ", "HEM", "A", 901,
+                                        ca[1] + 2.0, "Fe"))
+            lines.append(_pdb_atom_line("HETATM", serial + 2, "O", " ", "HOH", "A", 950,
+                                        ca[2] + 3.0, "O"))
+            long = _pdb_atom_line("ATOM", serial + 3, "CA", " ", "GLY", "B", 999, ca[3] + 2.5, "C")
+            lines.append(long + " " * 30 + "TRAILING-COLUMNS-BEYOND-99")
+        lines.append("ENDMDL")
+    lines.append("END" + " " * 77)
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")

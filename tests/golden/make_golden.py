@@ -17,6 +17,15 @@ Outputs (committed; the GPU machine has no reference tree):
 * ``ff_ref.npz`` -- form-factor tables and radii of the reference's
   atomic_form_factors (resaxslib/include/ff_coef.hpp) for q = 0..0.75 (500
   points) and three (expansion factor, mean radius) pairs.
+* ``synthetic_a.pdb``, ``synthetic_nonl.pdb`` and ``pdb_ref.npz`` -- two
+  synthetic PDB files (resaxs_gb300.workloads.write_synthetic_pdb: waters,
+  alternate locations, hydrogens, unknown and blank elements, short and
+  over-long lines; the second ends in an ATOM line with no newline) and the
+  bodies the reference's own parse_pdb<float>::all_models_as_complex_atoms
+  (resaxslib/src/parse_pdb.cpp, compiled into oracle/_ref) reads from them.
+
+``python tests/golden/make_golden.py [reference_root] --only pdb`` rewrites
+only the PDB fixtures.
 """
 from __future__ import annotations
 
@@ -66,10 +75,44 @@ def ref_dd(q, bodies, ff):
     return out
 
 
-def main(ref_root="/root/reference"):
+def ref_parse_pdb(path):
+    import ctypes
+    L = oracle.ref_lib()
+    f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+    i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+    L.ref_parse_pdb.argtypes = [ctypes.c_char_p, f32p, ctypes.c_int, i32p, ctypes.c_int]
+    out = np.zeros((100000, 4), np.float32)
+    sizes = np.zeros(64, np.int32)
+    k = L.ref_parse_pdb(path.encode(), out.reshape(-1), len(out), sizes, len(sizes))
+    if k < 0:
+        raise RuntimeError(f"reference parse of {path} failed: {k}")
+    return out[: sizes[:k].sum()].copy(), sizes[:k].copy()
+
+
+def make_pdb_fixtures():
+    a = os.path.join(HERE, "synthetic_a.pdb")
+    W.write_synthetic_pdb(a, n_residues=40, n_models=3, seed=3)
+    b = os.path.join(HERE, "synthetic_nonl.pdb")
+    W.write_synthetic_pdb(b, n_residues=12, n_models=1, seed=5)
+    lines = open(b).read().split("\n")
+    atom = [ln for ln in lines if ln.startswith("ATOM")]
+    body = [ln for ln in lines if not ln.startswith(("ENDMDL", "END "))
+            and ln.strip() != "END" and ln != ""]
+    with open(b, "w") as f:  # last record an ATOM line with no newline
+        f.write("\n".join(body + [atom[0]]))
+    fa, sa = ref_parse_pdb(a)
+    fb, sb = ref_parse_pdb(b)
+    np.savez_compressed(os.path.join(HERE, "pdb_ref.npz"), a_bodies=fa, a_sizes=sa,
+                        nonl_bodies=fb, nonl_sizes=sb)
+
+
+def main(ref_root="/root/reference", only=None):
     oracle.build()
     if oracle.build_ref(ref_root) is None:
         raise SystemExit(f"reference tree not found at {ref_root}")
+    make_pdb_fixtures()
+    if only == "pdb":
+        return
     q, ff, bodies, iq = parse_test1888(ref_root)
     np.savez_compressed(os.path.join(HERE, "test1888.npz"), q=q, ff=ff, bodies=bodies, iq=iq,
                         iq_ref_df=ref_df(q, bodies, ff), iq_ref_dd=ref_dd(q, bodies, ff))
@@ -103,4 +146,9 @@ def main(ref_root="/root/reference"):
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    args = [a for a in sys.argv[1:] if not a.startswith("--only")]
+    only = None
+    if "--only" in sys.argv:
+        only = sys.argv[sys.argv.index("--only") + 1]
+        args = [a for a in args if a != only]
+    main(*args, only=only)
