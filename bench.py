@@ -11,9 +11,12 @@ N(N-1)/2 unordered pairs.
                 write) between timed steps, outside the events.
 * ``e2e``     : the same metric through the C ABI call a user makes
                 (rsx_debye_calc: host bodies in, host curve out, copies inside).
-* ``roofline``: the pair kernel's pair*q/s against the canonical peak of one
-                pair*q per 8 FP32 lane-ops (16 per clock per SM), taken from a
-                measured FMA rate of this GPU (rsx_measure_fp32_fma_rate).
+* ``roofline``: the pair kernel's pair*q/s against the FP32 issue bound of
+                the recurrence: 3 FP32 lane-ops per pair*q (one FMA and one
+                add advance sin(q r), one add accumulates it), at the FP32 FMA
+                rate measured on this GPU (rsx_measure_fp32_fma_rate).  The
+                bound of a direct evaluation (one SFU sine per pair*q, 16 per
+                clock per SM = FMA rate / 8) is reported beside it.
 * ``cpu_baseline``: the reference's host_debye<double,float> loop (port in
                 oracle/, bit-identical to the compiled original on x86) on the
                 host cores, on a bounded q sample, extrapolated to all q.
@@ -247,7 +250,8 @@ def main():
         import ctypes
         fma = ctypes.c_double()
         _lib.check(_lib.lib().rsx_measure_fp32_fma_rate(local, ctypes.byref(fma)))
-        peak = fma.value / 8.0 / 1e9   # canonical: 16 pair*q per 128 FMA lane-ops
+        peak = fma.value / 3.0 / 1e9   # 3 FP32 lane-ops per pair*q
+        sfu_peak = fma.value / 8.0 / 1e9  # one SFU sine per pair*q: 16 per clock per SM
         k_ms = statistics.median(kernel_ms)
         achieved = w.pair_q / (k_ms * 1e-3) / 1e9
         prof = os.path.join(ROOT, "profiles", "debye_forward_traffic.json")
@@ -266,12 +270,14 @@ def main():
                        "q_slab": cfg["q_slab"], "work_items": cfg["n_items"],
                        "uniform_q_recurrence": cfg["uniform_q"],
                        "wall_s_timed_loop": t_wall},
-            "roofline": {"bound": "fp32_issue", "achieved": achieved, "peak": peak,
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak,
                          "unit": UNIT, "frac": achieved / peak, "traffic": traffic,
                          "kernel_ms": k_ms,
-                         "peak_source": "measured FP32 FMA rate of this GPU / 8 lane-ops "
-                                        "per pair*q (16 pair*q per clock per SM)",
-                         "fp32_fma_per_s": fma.value},
+                         "peak_source": "FP32 FMA rate measured on this GPU in this run / "
+                                        "3 FP32 lane-ops per pair*q of the recurrence",
+                         "fp32_fma_per_s": fma.value,
+                         "sfu_direct_peak": sfu_peak,
+                         "frac_of_sfu_direct_peak": achieved / sfu_peak},
             "e2e": e2e,
             "gpu_launches": int(launches),
             "clocks": clk,

@@ -119,7 +119,9 @@ typedef struct rsx_debye rsx_debye;
 
 typedef struct rsx_debye_options {
     int device;          /* CUDA ordinal; -1 = current device */
-    int q_slab;          /* q values per CTA slab: 8, 16, 32, 64; 0 = tuned / default */
+    int q_slab;          /* q values per CTA slab: 8, 16, 32, 64 or 128; 0 = tuned / default.
+                            On uniform grids without water 64 and 128 select the
+                            wide slabs (64 or 112 q per recurrence seed). */
     int max_items;       /* cap on forward work items (scratch = items*n_q*8 B); 0 = default */
     int force_general_q; /* 1: never use the uniform-grid recurrence */
     int timing;          /* 1: record CUDA events around the pair kernel */

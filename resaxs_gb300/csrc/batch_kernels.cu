@@ -154,7 +154,7 @@ static cudaError_t adj_launch(const DebyeArgs &a, const int *order, int n_items,
                               int grid, cudaStream_t st)
 {
     const int n_slabs = (a.n_q + QS - 1) / QS;
-    const size_t smem = (size_t)n_slabs * QS * 4 * sizeof(float);
+    const size_t smem = adjoint_smem_bytes(a.n_q, QS, U, false);
     auto kfn = batch_adjoint_kernel<QS, U>;
     if (smem > 48 * 1024) {
         cudaError_t e =
@@ -236,7 +236,7 @@ int batch_forward_grid(int q_slab, bool uniform, int sms)
 int batch_adjoint_grid(int q_slab, bool uniform, int n_q, int sms)
 {
     const int qs = q_slab > 32 ? 32 : (q_slab < 8 ? 8 : q_slab);
-    const size_t smem = (size_t)((n_q + qs - 1) / qs) * qs * 4 * sizeof(float);
+    const size_t smem = adjoint_smem_bytes(n_q, qs, uniform, false);
     if (qs == 8)
         return uniform ? occupancy_grid(batch_adjoint_kernel<8, true>, smem, sms)
                        : occupancy_grid(batch_adjoint_kernel<8, false>, smem, sms);

@@ -166,6 +166,233 @@ __device__ __forceinline__ void reduce_scatter_any(float (&v)[QS], int lane)
     }
 }
 
+// ----------------------------------------------------------------------------
+// forward, uniform q grid without water: wide slabs
+// ----------------------------------------------------------------------------
+//
+// The per-pair seed (distance, IEEE sqrt and reciprocal, two range-reduced
+// sincos) costs as much as ~40 recurrence steps, so this form runs up to 128 q
+// per seed.  Per J-block each thread sums its pairs in FP32 registers (S[k]);
+// the warp then reduce-scatters S (lane L receives q index 32c + L of chunk c)
+// and adds it to FP64 lane accumulators, so no per-thread compensated
+// accumulators have to be kept for QS q values.
+
+template <int QS>
+struct WideSlab {
+    static constexpr int QP = (QS + 31) / 32 * 32; // padded to whole warps
+    static constexpr int NR = QP / 32;             // q values per lane after the scatter
+};
+
+// Compact seed of the wide path: Reinsch form (s, d, lam) when cos(theta) >= 0,
+// rotation form (s, c, sin theta, cos theta) otherwise; 4 registers per pair
+// either way.
+struct WideSeed {
+    float s, d, l, cd; // Reinsch: s, d, lam; rotation: s, c, sin(theta), cos(theta)
+    bool big;
+};
+
+__device__ __forceinline__ WideSeed wide_seed(float q0, float dq, float r, float sc)
+{
+    WideSeed p;
+    float s0, c0, sh, ch;
+    sincos_prod(q0, r, s0, c0);
+    {
+        const float th = dq * r;
+        const float th_lo = fmaf(dq, r, -th);
+        sincos_rr2(0.5f * th, 0.5f * th_lo, sh, ch);
+    }
+    p.big = ch * ch < sh * sh;
+    p.s = s0 * sc;
+    if (!p.big) {
+        p.l = -4.0f * sh * sh;
+        p.d = 2.0f * sh * fmaf(c0, ch, s0 * sh) * sc;
+        p.cd = 0.f;
+    } else {
+        p.d = c0 * sc;
+        p.l = 2.0f * sh * ch;
+        p.cd = fmaf(-2.0f * sh, sh, 1.0f);
+    }
+    return p;
+}
+
+// One recurrence step of a wide seed in either form.
+__device__ __forceinline__ void wide_step(const WideSeed &p, float &s, float &d)
+{
+    if (p.big) {
+        const float sn = fmaf(d, p.l, s * p.cd);
+        d = fmaf(-s, p.l, d * p.cd);
+        s = sn;
+    } else {
+        d = fmaf(p.l, s, d);
+        s += d;
+    }
+}
+
+// Two pairs on the Reinsch form, interleaved for ILP (the hot loop: 3 FP32
+// lane-ops per pair*q).
+template <int QS, int QP>
+__device__ __forceinline__ void wide_pair2(const WideSeed &a, const WideSeed &b, float (&S)[QP])
+{
+    float sa = a.s, da = a.d, sb = b.s, db = b.d;
+#pragma unroll
+    for (int k = 0; k < QS; ++k) {
+        S[k] += sa + sb;
+        da = fmaf(a.l, sa, da);
+        db = fmaf(b.l, sb, db);
+        sa += da;
+        sb += db;
+    }
+}
+
+// Four pairs on the Reinsch form: more independent chains per warp for when
+// few warps fit on an SM.
+template <int QS, int QP>
+__device__ __forceinline__ void wide_pair4(const WideSeed &a, const WideSeed &b, const WideSeed &c,
+                                           const WideSeed &e, float (&S)[QP])
+{
+    float sa = a.s, da = a.d, sb = b.s, db = b.d, sc = c.s, dc = c.d, se = e.s, de = e.d;
+#pragma unroll
+    for (int k = 0; k < QS; ++k) {
+        S[k] += (sa + sb) + (sc + se);
+        da = fmaf(a.l, sa, da);
+        db = fmaf(b.l, sb, db);
+        dc = fmaf(c.l, sc, dc);
+        de = fmaf(e.l, se, de);
+        sa += da;
+        sb += db;
+        sc += dc;
+        se += de;
+    }
+}
+
+// Two pairs when either needs the rotation form (cos(theta) < 0: far-apart
+// bodies on coarse grids; rare).
+template <int QS, int QP>
+__device__ __forceinline__ void wide_mixed2(const WideSeed &a, const WideSeed &b, float (&S)[QP])
+{
+    float sa = a.s, da = a.d, sb = b.s, db = b.d;
+#pragma unroll
+    for (int k = 0; k < QS; ++k) {
+        S[k] += sa + sb;
+        wide_step(a, sa, da);
+        wide_step(b, sb, db);
+    }
+}
+
+template <int QS, int QP>
+__device__ __forceinline__ void wide_pair1(const WideSeed &p, float (&S)[QP])
+{
+    float s = p.s, d = p.d;
+#pragma unroll
+    for (int k = 0; k < QS; ++k) {
+        S[k] += s;
+        wide_step(p, s, d);
+    }
+}
+
+// Forward pair sums of one work item for q values [k0, k0 + QS) on a uniform
+// grid without water; writes partial[k][item_idx] as forward_item does.
+template <int QS, int IL>
+__device__ __forceinline__ void forward_wide_item(const DebyeArgs &a, int item_idx, int k0)
+{
+    constexpr int QP = WideSlab<QS>::QP, NR = WideSlab<QS>::NR;
+    __shared__ float4 s_pos[kBlockAtoms];
+    __shared__ double s_red[kBlockAtoms / 32][QP];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    __syncthreads(); // a previous item of this CTA may still read shared memory
+    const PairItem it = a.items[item_idx];
+    const BlockDesc bi = a.blocks[it.bi];
+    const int tj = a.blocks[it.bj_begin].type;
+    const int i = bi.start + tid;
+    const bool valid_i = tid < bi.len;
+    const float4 pi = valid_i ? a.pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float q0 = a.q[k0];
+    const float dq = a.dq;
+
+    double acc[NR];
+#pragma unroll
+    for (int c = 0; c < NR; ++c)
+        acc[c] = 0.0;
+
+    for (int b = it.bj_begin; b < it.bj_end; ++b) {
+        const BlockDesc bj = a.blocks[b];
+        __syncthreads();
+        if (tid < bj.len)
+            s_pos[tid] = a.pos[bj.start + tid];
+        __syncthreads();
+        const bool diag = (b == it.bi);
+        float S[QP];
+#pragma unroll
+        for (int k = 0; k < QP; ++k)
+            S[k] = 0.f;
+        int jj = 0;
+        if (IL == 4) {
+            for (; jj + 3 < bj.len; jj += 4) {
+                WideSeed p[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    float r, ri, dx, dy, dz;
+                    pair_r(pi, s_pos[jj + u], r, ri, dx, dy, dz);
+                    const bool use = valid_i && (!diag || jj + u > tid);
+                    p[u] = wide_seed(q0, dq, r, use ? ri : 0.f);
+                }
+                if (!(p[0].big || p[1].big || p[2].big || p[3].big)) {
+                    wide_pair4<QS, QP>(p[0], p[1], p[2], p[3], S);
+                } else {
+                    wide_mixed2<QS, QP>(p[0], p[1], S);
+                    wide_mixed2<QS, QP>(p[2], p[3], S);
+                }
+            }
+        }
+        for (; jj + 1 < bj.len; jj += 2) {
+            float r1, ri1, r2, ri2, dx, dy, dz;
+            pair_r(pi, s_pos[jj], r1, ri1, dx, dy, dz);
+            pair_r(pi, s_pos[jj + 1], r2, ri2, dx, dy, dz);
+            const bool u1 = valid_i && (!diag || jj > tid);
+            const bool u2 = valid_i && (!diag || jj + 1 > tid);
+            const WideSeed p1 = wide_seed(q0, dq, r1, u1 ? ri1 : 0.f);
+            const WideSeed p2 = wide_seed(q0, dq, r2, u2 ? ri2 : 0.f);
+            if (!p1.big && !p2.big)
+                wide_pair2<QS, QP>(p1, p2, S);
+            else
+                wide_mixed2<QS, QP>(p1, p2, S);
+        }
+        if (jj < bj.len) {
+            float r, rinv, dx, dy, dz;
+            pair_r(pi, s_pos[jj], r, rinv, dx, dy, dz);
+            const bool use = valid_i && (!diag || jj > tid);
+            wide_pair1<QS, QP>(wide_seed(q0, dq, r, use ? rinv : 0.f), S);
+        }
+#pragma unroll
+        for (int c = 0; c < NR; ++c) {
+            float v[32];
+#pragma unroll
+            for (int k = 0; k < 32; ++k)
+                v[k] = S[32 * c + k];
+            warp_reduce_scatter<32>(v, lane);
+            acc[c] += (double)v[0];
+        }
+    }
+
+#pragma unroll
+    for (int c = 0; c < NR; ++c)
+        s_red[warp][32 * c + lane] = acc[c];
+    __syncthreads();
+    for (int k = tid; k < QS; k += kBlockAtoms) {
+        const int kk = k0 + k;
+        if (kk >= a.n_q)
+            continue;
+        double s = 0.0;
+#pragma unroll
+        for (int w = 0; w < kBlockAtoms / 32; ++w)
+            s += s_red[w][k];
+        const double fi = a.ff[(size_t)kk * a.n_types + bi.type];
+        const double fj = a.ff[(size_t)kk * a.n_types + tj];
+        a.partial[(size_t)kk * a.n_items + item_idx] = s * fi * fj;
+    }
+}
+
 // Forward pair sums of one work item for q values [k0, k0 + QS): writes
 // partial[k][item_idx] = sum over the item's pairs of f_i f_j sin(q_k r)/r.
 // Called once per CTA by the grid kernel and repeatedly by the persistent
@@ -316,10 +543,294 @@ __device__ __forceinline__ void forward_item(const DebyeArgs &a, int item_idx, i
     }
 }
 
-// Adjoint of one work item (all q): adds dL/dx of the item's pairs to the
-// FP64 gradient.  The item's member (PairItem::pad) selects its dL/dI row.
+// ----------------------------------------------------------------------------
+// adjoint, uniform q grid without water
+// ----------------------------------------------------------------------------
+//
+// Per pair the gradient needs A = sum_k alpha_k cos(x_k) and
+// B = sum_k beta_k sin(x_k), x_k = q_k r, alpha_k = lambda_k f_i f_j,
+// beta_k = alpha_k / q_k.  Both come from one two-term recurrence, the
+// "magic circle" form of the sine/cosine oscillator:
+//     e_{k+1} = e_k - a s_k,   s_{k+1} = s_k + a e_{k+1},   a = 2 sin(theta/2)
+// with s_k = sin(x_k) and e_k = cos(x_k - theta/2) (exact in real arithmetic:
+// cos(x + h) - cos(x - h) = -2 sin(x) sin(h), sin(x + 2h) - sin(x) =
+// 2 cos(x + h) sin(h)).  Its errors stay at the rounding level for small theta,
+// where the plain rotation's cos(theta) ~ 1 loses them.  Since
+// cos(x_k) = (e_k + e_{k+1}) / (2 cos(theta/2)), summation by parts gives
+//     A = sum_{m=0..L} delta_m e_m / (2 cos(theta/2)),
+//     delta_m = alpha_m + alpha_{m-1}   (alpha outside the slab = 0),
+// so a pair costs four FMAs per q: two for the recurrence and one for each
+// sum.  The recurrence is reseeded from sin/cos(q_0 r) every kAdjSlab q.
+// Pairs with theta > pi/2 (cos(theta/2)^2 < 1/2, far-apart bodies on coarse
+// grids) take the rotation form with alpha directly.
+
+constexpr int kAdjSlab = 64;   // q values between reseeds
+constexpr int kAdjStride = 65; // table entries per slab (delta has L + 1)
+
+// Table entry m of slab sl: (delta_m, beta_m, alpha_m, 0).
+__device__ __forceinline__ void adjoint_uniform_table(const DebyeArgs &a, float4 *tab, int n_slabs,
+                                                      const float *lambda, int ti, int tj)
+{
+    const int n = n_slabs * kAdjStride;
+    for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+        const int sl = idx / kAdjStride, m = idx - sl * kAdjStride;
+        const int kb = sl * kAdjSlab;
+        const int len = min(kAdjSlab, a.n_q - kb);
+        auto alpha = [&](int k, float *beta) {
+            // alpha_k, and beta_k = alpha_k / q_k (0 at q = 0, where d sinc/dr = 0)
+            if (k < 0 || k >= len) {
+                *beta = 0.f;
+                return 0.f;
+            }
+            const int kk = kb + k;
+            const float qk = a.q[kk];
+            if (qk == 0.f) {
+                *beta = 0.f;
+                return 0.f;
+            }
+            const float al =
+                lambda[kk] * a.ff[(size_t)kk * a.n_types + ti] * a.ff[(size_t)kk * a.n_types + tj];
+            *beta = al / qk;
+            return al;
+        };
+        float b0, bm1;
+        const float a0 = alpha(m, &b0);
+        const float am1 = alpha(m - 1, &bm1);
+        tab[idx] = make_float4(a0 + am1, b0, a0, 0.f);
+    }
+}
+
+// One pair over one slab of L q values (L a multiple of 8): P += sum delta e,
+// Q += sum beta s.
+__device__ __forceinline__ void adj_circle_slab(const float4 *t, int L, float s, float e, float ac,
+                                                float &P, float &Q)
+{
+    for (int c = 0; c < L; c += 8) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const float2 cf = *reinterpret_cast<const float2 *>(t + c + u);
+            P = fmaf(cf.x, e, P);
+            Q = fmaf(cf.y, s, Q);
+            e = fmaf(-ac, s, e);
+            s = fmaf(ac, e, s);
+        }
+    }
+    P = fmaf(t[L].x, e, P);
+}
+
+// Two pairs interleaved (both on the magic-circle form): one table load feeds
+// both.
+__device__ __forceinline__ void adj_circle_slab2(const float4 *t, int L, float s1, float e1,
+                                                 float a1, float s2, float e2, float a2, float &P1,
+                                                 float &Q1, float &P2, float &Q2)
+{
+    for (int c = 0; c < L; c += 8) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const float2 cf = *reinterpret_cast<const float2 *>(t + c + u);
+            P1 = fmaf(cf.x, e1, P1);
+            Q1 = fmaf(cf.y, s1, Q1);
+            P2 = fmaf(cf.x, e2, P2);
+            Q2 = fmaf(cf.y, s2, Q2);
+            e1 = fmaf(-a1, s1, e1);
+            e2 = fmaf(-a2, s2, e2);
+            s1 = fmaf(a1, e1, s1);
+            s2 = fmaf(a2, e2, s2);
+        }
+    }
+    const float d = t[L].x;
+    P1 = fmaf(d, e1, P1);
+    P2 = fmaf(d, e2, P2);
+}
+
+// Rotation form for one pair over one slab: A += sum alpha cos, B += sum beta sin.
+__device__ __forceinline__ void adj_rotate_slab(const float4 *t, int L, float s, float c, float sd,
+                                                float cd, float &A, float &B)
+{
+    for (int k = 0; k < L; ++k) {
+        const float4 cf = t[k];
+        A = fmaf(cf.z, c, A);
+        B = fmaf(cf.y, s, B);
+        const float sn = fmaf(c, sd, s * cd);
+        const float cn = fmaf(-s, sd, c * cd);
+        s = sn;
+        c = cn;
+    }
+}
+
+// Per-pair constants of the uniform adjoint.
+struct AdjPair {
+    float r, rinv, dx, dy, dz;
+    float sh, ch; // sin, cos of theta / 2
+    bool circle;  // magic-circle form (theta <= pi/2)
+};
+
+__device__ __forceinline__ AdjPair adj_pair(const float4 &pi, const float4 &pj, float dq)
+{
+    AdjPair p;
+    pair_r(pi, pj, p.r, p.rinv, p.dx, p.dy, p.dz);
+    const float th = dq * p.r;
+    const float th_lo = fmaf(dq, p.r, -th);
+    sincos_rr2(0.5f * th, 0.5f * th_lo, p.sh, p.ch);
+    p.circle = 2.0f * p.ch * p.ch >= 1.0f;
+    return p;
+}
+
+// Sums A (cosine side) and B (sine side) of one pair over all slabs.
+__device__ __forceinline__ void adj_pair_sums(const DebyeArgs &a, const float4 *tab, int n_slabs,
+                                              const AdjPair &p, float &A, float &B)
+{
+    float P = 0.f, Q = 0.f;
+    for (int sl = 0; sl < n_slabs; ++sl) {
+        const int kb = sl * kAdjSlab;
+        const int L = (min(kAdjSlab, a.n_q - kb) + 7) & ~7;
+        const float4 *t = tab + sl * kAdjStride;
+        float s0, c0;
+        sincos_prod(a.q[kb], p.r, s0, c0);
+        if (p.circle) {
+            adj_circle_slab(t, L, s0, fmaf(c0, p.ch, s0 * p.sh), 2.0f * p.sh, P, Q);
+        } else {
+            const float sd = 2.0f * p.sh * p.ch, cd = fmaf(-2.0f * p.sh, p.sh, 1.0f);
+            adj_rotate_slab(t, L, s0, c0, sd, cd, P, Q);
+        }
+    }
+    A = p.circle ? P * (0.5f / p.ch) : P;
+    B = Q;
+}
+
+__device__ __forceinline__ void adj_pair2_sums(const DebyeArgs &a, const float4 *tab, int n_slabs,
+                                               const AdjPair &p1, const AdjPair &p2, float &A1,
+                                               float &B1, float &A2, float &B2)
+{
+    float P1 = 0.f, Q1 = 0.f, P2 = 0.f, Q2 = 0.f;
+    for (int sl = 0; sl < n_slabs; ++sl) {
+        const int kb = sl * kAdjSlab;
+        const int L = (min(kAdjSlab, a.n_q - kb) + 7) & ~7;
+        const float4 *t = tab + sl * kAdjStride;
+        const float q0 = a.q[kb];
+        float s1, c1, s2, c2;
+        sincos_prod(q0, p1.r, s1, c1);
+        sincos_prod(q0, p2.r, s2, c2);
+        adj_circle_slab2(t, L, s1, fmaf(c1, p1.ch, s1 * p1.sh), 2.0f * p1.sh, s2,
+                         fmaf(c2, p2.ch, s2 * p2.sh), 2.0f * p2.sh, P1, Q1, P2, Q2);
+    }
+    A1 = P1 * (0.5f / p1.ch);
+    B1 = Q1;
+    A2 = P2 * (0.5f / p2.ch);
+    B2 = Q2;
+}
+
+// Scatters one pair's gradient: the I side into the thread's registers, the J
+// side (summed over the warp) into shared memory.
+__device__ __forceinline__ void adj_scatter(const AdjPair &p, float A, float B, bool use,
+                                            float &gi0, float &gi1, float &gi2, float (*s_gj)[3],
+                                            int jj, int lane)
+{
+    // G = 2 / r^2 * (A - B / r); the J side gets +G*d, the I side -G*d
+    float G = 2.0f * p.rinv * p.rinv * fmaf(-B, p.rinv, A);
+    G = use ? G : 0.f;
+    float gx = G * p.dx, gy = G * p.dy, gz = G * p.dz;
+    gi0 -= gx;
+    gi1 -= gy;
+    gi2 -= gz;
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) {
+        gx += __shfl_xor_sync(0xffffffffu, gx, m);
+        gy += __shfl_xor_sync(0xffffffffu, gy, m);
+        gz += __shfl_xor_sync(0xffffffffu, gz, m);
+    }
+    if (lane == 0) {
+        atomicAdd(&s_gj[jj][0], gx);
+        atomicAdd(&s_gj[jj][1], gy);
+        atomicAdd(&s_gj[jj][2], gz);
+    }
+}
+
+// Dynamic shared memory of the adjoint kernels for n_q values.
+__host__ __device__ inline size_t adjoint_smem_bytes(int n_q, int qs, bool uniform, bool water)
+{
+    if (uniform && !water)
+        return (size_t)((n_q + kAdjSlab - 1) / kAdjSlab) * kAdjStride * sizeof(float4);
+    const int n_slabs = (n_q + qs - 1) / qs;
+    return (size_t)n_slabs * qs * (water ? 8 : 4) * sizeof(float);
+}
+
+__device__ __forceinline__ void adjoint_uniform_item(const DebyeArgs &a, int item_idx)
+{
+    extern __shared__ float4 s_dyn[];
+    __shared__ float4 s_pos[kBlockAtoms];
+    __shared__ float s_gj[kBlockAtoms][3];
+
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    __syncthreads(); // a previous item of this CTA may still read shared memory
+    const PairItem it = a.items[item_idx];
+    const float *lambda = a.lambda + (size_t)it.pad * a.n_q;
+    const BlockDesc bi = a.blocks[it.bi];
+    const int tj = a.blocks[it.bj_begin].type;
+    const int n_slabs = (a.n_q + kAdjSlab - 1) / kAdjSlab;
+    float4 *tab = s_dyn;
+    adjoint_uniform_table(a, tab, n_slabs, lambda, bi.type, tj);
+
+    const int i = bi.start + tid;
+    const bool valid_i = tid < bi.len;
+    const float4 pi = valid_i ? a.pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float gi0 = 0.f, gi1 = 0.f, gi2 = 0.f;
+    const float dq = a.dq;
+
+    for (int b = it.bj_begin; b < it.bj_end; ++b) {
+        const BlockDesc bj = a.blocks[b];
+        __syncthreads();
+        if (tid < bj.len)
+            s_pos[tid] = a.pos[bj.start + tid];
+        s_gj[tid][0] = 0.f;
+        s_gj[tid][1] = 0.f;
+        s_gj[tid][2] = 0.f;
+        __syncthreads();
+        const bool diag = (b == it.bi);
+        int jj = 0;
+        for (; jj + 1 < bj.len; jj += 2) {
+            const AdjPair p1 = adj_pair(pi, s_pos[jj], dq);
+            const AdjPair p2 = adj_pair(pi, s_pos[jj + 1], dq);
+            float A1, B1, A2, B2;
+            if (p1.circle && p2.circle) {
+                adj_pair2_sums(a, tab, n_slabs, p1, p2, A1, B1, A2, B2);
+            } else {
+                adj_pair_sums(a, tab, n_slabs, p1, A1, B1);
+                adj_pair_sums(a, tab, n_slabs, p2, A2, B2);
+            }
+            adj_scatter(p1, A1, B1, valid_i && (!diag || jj > tid), gi0, gi1, gi2, s_gj, jj, lane);
+            adj_scatter(p2, A2, B2, valid_i && (!diag || jj + 1 > tid), gi0, gi1, gi2, s_gj,
+                        jj + 1, lane);
+        }
+        for (; jj < bj.len; ++jj) {
+            const AdjPair p = adj_pair(pi, s_pos[jj], dq);
+            float A, B;
+            adj_pair_sums(a, tab, n_slabs, p, A, B);
+            adj_scatter(p, A, B, valid_i && (!diag || jj > tid), gi0, gi1, gi2, s_gj, jj, lane);
+        }
+        __syncthreads();
+        if (tid < bj.len) {
+            double *g = a.grad + 3 * (size_t)(bj.start + tid);
+            atomicAdd(g + 0, (double)s_gj[tid][0]);
+            atomicAdd(g + 1, (double)s_gj[tid][1]);
+            atomicAdd(g + 2, (double)s_gj[tid][2]);
+        }
+    }
+    if (valid_i) {
+        double *g = a.grad + 3 * (size_t)i;
+        atomicAdd(g + 0, (double)gi0);
+        atomicAdd(g + 1, (double)gi1);
+        atomicAdd(g + 2, (double)gi2);
+    }
+}
+
+// Adjoint of one work item (all q), general form: rotation per pair and
+// per-pair water factors, for non-uniform grids and for water.  Adds dL/dx of
+// the item's pairs to the FP64 gradient; the item's member (PairItem::pad)
+// selects its dL/dI row.
 template <int QS, bool UNIFORM, bool WATER>
-__device__ __forceinline__ void adjoint_item(const DebyeArgs &a, int item_idx, int n_slabs)
+__device__ __forceinline__ void adjoint_general_item(const DebyeArgs &a, int item_idx, int n_slabs)
 {
     extern __shared__ float4 s_dyn[]; // [n_slabs*QS] coefficients (a0, b0, a1, b1)
     __shared__ float4 s_pos[kBlockAtoms];
@@ -474,6 +985,15 @@ __device__ __forceinline__ void adjoint_item(const DebyeArgs &a, int item_idx, i
         atomicAdd(g + 1, (double)gi1);
         atomicAdd(g + 2, (double)gi2);
     }
+}
+
+template <int QS, bool UNIFORM, bool WATER>
+__device__ __forceinline__ void adjoint_item(const DebyeArgs &a, int item_idx, int n_slabs)
+{
+    if constexpr (UNIFORM && !WATER)
+        adjoint_uniform_item(a, item_idx);
+    else
+        adjoint_general_item<QS, UNIFORM, WATER>(a, item_idx, n_slabs);
 }
 
 } // namespace rsx

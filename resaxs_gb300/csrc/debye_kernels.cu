@@ -22,6 +22,7 @@
 #include "debye_device.cuh"
 
 #include <atomic>
+#include <cstdlib>
 
 namespace rsx {
 
@@ -33,6 +34,13 @@ template <int QS, bool UNIFORM, bool WATER>
 __global__ void __launch_bounds__(kBlockAtoms, QS >= 64 ? 3 : 1) forward_kernel(const DebyeArgs a)
 {
     forward_item<QS, UNIFORM, WATER>(a, blockIdx.x, a.k_base + blockIdx.y * QS);
+}
+
+// up to 64 q: <= 168 registers, 3 CTAs per SM; wider: <= 255, 2 CTAs per SM
+template <int QS, int IL>
+__global__ void __launch_bounds__(kBlockAtoms, QS <= 64 ? 3 : 2) forward_wide_kernel(const DebyeArgs a)
+{
+    forward_wide_item<QS, IL>(a, blockIdx.x, a.k_base + blockIdx.y * QS);
 }
 
 // ----------------------------------------------------------------------------
@@ -271,13 +279,80 @@ static cudaError_t forward_dispatch(const DebyeArgs &a, int qs, int k_base, int 
     }
 }
 
-// Full slabs of q_slab values, then the remainder in the smallest slab of
-// 8 / 16 / 32 that covers it (a second launch on the same stream).
+template <int QS, int IL = 2>
+static cudaError_t wide_launch(DebyeArgs a, int k_base, int n_slabs, cudaStream_t st)
+{
+    a.k_base = k_base;
+    const dim3 grid(a.n_items, n_slabs);
+    forward_wide_kernel<QS, IL><<<grid, kBlockAtoms, 0, st>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+static cudaError_t wide_tail(const DebyeArgs &a, int k0, int len, cudaStream_t st)
+{
+    switch ((len + 15) / 16) {
+    case 1:
+        return wide_launch<16>(a, k0, 1, st);
+    case 2:
+        return wide_launch<32>(a, k0, 1, st);
+    case 3:
+        return wide_launch<48>(a, k0, 1, st);
+    case 4:
+        return wide_launch<64>(a, k0, 1, st);
+    case 5:
+        return wide_launch<80>(a, k0, 1, st);
+    case 6:
+        return wide_launch<96>(a, k0, 1, st);
+    default:
+        return wide_launch<112>(a, k0, 1, st);
+    }
+}
+
+static int env_int(const char *name, int dflt)
+{
+    const char *v = getenv(name);
+    return v ? atoi(v) : dflt;
+}
+
+// Uniform grid without water: full slabs of `main` q (64 or 112), then the
+// remainder in one slab of the next multiple of 16 (a second launch on the
+// same stream).
+static cudaError_t launch_forward_wide(const DebyeArgs &a, int main, cudaStream_t st)
+{
+    static const int il = env_int("RSX_WIDE_IL", 2);
+    static const int merge = env_int("RSX_WIDE_MERGE", 0);
+    int full = a.n_q / main;
+    int rest = a.n_q - full * main;
+    if (merge && main == 64 && full > 0 && rest > 0 && rest <= 48) {
+        --full; // the last full slab and the remainder run as one slab of <= 112
+        rest += 64;
+    }
+    if (full > 0) {
+        cudaError_t e;
+        if (main == 64)
+            e = il == 4 ? wide_launch<64, 4>(a, 0, full, st) : wide_launch<64, 2>(a, 0, full, st);
+        else
+            e = il == 4 ? wide_launch<112, 4>(a, 0, full, st) : wide_launch<112, 2>(a, 0, full, st);
+        if (e != cudaSuccess)
+            return e;
+    }
+    if (rest == 0)
+        return cudaSuccess;
+    return wide_tail(a, full * main, rest, st);
+}
+
+// Uniform grids without water and q_slab 64 / 128 take the wide slabs (64 or
+// 112 q per seed); otherwise full slabs of q_slab values, then the remainder
+// in the smallest slab of 8 / 16 / 32 that covers it (a second launch on the
+// same stream).
 cudaError_t launch_forward(const DebyeArgs &a, int q_slab, bool uniform, bool water,
                            cudaStream_t st)
 {
     if (a.n_items == 0)
         return cudaSuccess;
+    if (uniform && !water && q_slab >= 64)
+        return launch_forward_wide(a, q_slab >= 128 ? 112 : 64, st);
     const int full = a.n_q / q_slab;
     const int rest = a.n_q - full * q_slab;
     if (full > 0) {
@@ -360,7 +435,7 @@ template <int QS>
 static cudaError_t adjoint_qs(const DebyeArgs &a, bool uniform, bool water, cudaStream_t st)
 {
     const int n_slabs = (a.n_q + QS - 1) / QS;
-    const size_t smem = (size_t)n_slabs * QS * (water ? 8 : 4) * sizeof(float);
+    const size_t smem = adjoint_smem_bytes(a.n_q, QS, uniform, water);
     const dim3 grid(a.n_items);
     cudaError_t e = cudaSuccess;
 #define RSX_ADJ(U, W)                                                                      \

@@ -239,7 +239,7 @@ int slab_for(const rsx_debye *h)
     if (has_water(h) && qs > 16)
         qs = 16; // water keeps two accumulator sets in registers
     if (!h->uniform && qs > 32)
-        qs = 32; // the direct-sine path has no 64-wide variant
+        qs = 32; // the direct-sine path has no wide variant
     return qs;
 }
 
@@ -254,7 +254,7 @@ rsx_status update_layout(rsx_debye *h, const rsx_body *bodies)
         return RSX_OK;
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
-    build_layout(h->L, bodies, h->n, h->n_types, h->max_items, sms * 8);
+    build_layout(h->L, bodies, h->n, h->n_types, h->max_items, sms * 64);
     RSX_TRY(ensure(&h->d_blocks, h->blocks_cap, h->L.blocks.size(), "blocks"));
     RSX_TRY(ensure(&h->d_items, h->items_cap, h->L.items.size(), "items"));
     RSX_TRY(ensure(&h->d_adj_items, h->adj_cap, h->L.adj_items.size(), "adjoint items"));
@@ -394,8 +394,10 @@ rsx_status tune_slab(rsx_debye *h)
         return RSX_OK;
     }
     std::vector<int> cands = {16, 32};
-    if (h->uniform && !has_water(h))
+    if (h->uniform && !has_water(h)) {
         cands.push_back(64);
+        cands.push_back(128);
+    }
     cudaEvent_t e0, e1;
     RSX_TRY_CUDA(cudaEventCreate(&e0), "event");
     RSX_TRY_CUDA(cudaEventCreate(&e1), "event");
@@ -630,8 +632,9 @@ rsx_status rsx_debye_create(const float *q, int n_q, const float *t_factors, int
     rsx_debye_default_options(&o);
     if (opts)
         o = *opts;
-    if (o.q_slab != 0 && o.q_slab != 8 && o.q_slab != 16 && o.q_slab != 32 && o.q_slab != 64)
-        return fail(RSX_INVALID_ARG, "q_slab must be 0, 8, 16, 32 or 64");
+    if (o.q_slab != 0 && o.q_slab != 8 && o.q_slab != 16 && o.q_slab != 32 && o.q_slab != 64 &&
+        o.q_slab != 128)
+        return fail(RSX_INVALID_ARG, "q_slab must be 0, 8, 16, 32, 64 or 128");
     int dev = -1;
     RSX_TRY(select_device(o.device, &dev));
     DeviceGuard g(dev);
@@ -644,10 +647,10 @@ rsx_status rsx_debye_create(const float *q, int n_q, const float *t_factors, int
     h->q.assign(q, q + n_q);
     h->ff.assign(t_factors, t_factors + (size_t)n_q * n_factors);
     h->uniform = !o.force_general_q && detect_uniform(h->q, &h->dq);
-    // default tile: 64 q per slab on long uniform grids (measured fastest on
-    // GB300 for Q >= 128), otherwise 32 / 16 / 8
+    // default tile: the wide slabs (112 q per seed) on uniform grids of 64 q
+    // or more, otherwise 32 / 16 / 8
     h->q_slab = o.q_slab ? o.q_slab
-                         : (h->uniform && n_q >= 128 ? 64 : (n_q >= 32 ? 32 : (n_q >= 16 ? 16 : 8)));
+                         : (h->uniform && n_q >= 64 ? 128 : (n_q >= 32 ? 32 : (n_q >= 16 ? 16 : 8)));
     h->autotune = o.autotune != 0 && o.q_slab == 0;
     h->max_items = o.max_items > 0 ? o.max_items : 16384;
     h->timing = o.timing != 0;

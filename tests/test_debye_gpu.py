@@ -39,12 +39,25 @@ def test_forward_configs_vs_oracle(saxs, oracle_lib, idx, n):
     assert rel(out, ref) < TOL
 
 
-@pytest.mark.parametrize("q_slab", [8, 16, 32])
+@pytest.mark.parametrize("q_slab", [8, 16, 32, 64, 128])
 def test_forward_slab_sizes(saxs, oracle_lib, q_slab):
     w = W.make_config(1, seed=12, n_override=700)
     _, out64, cfg = gpu_curve(saxs, w.q, w.ff, w.bodies, q_slab=q_slab)
     assert cfg["q_slab"] == q_slab
     assert rel(out64, oracle_lib.debye_f64(w.q, w.bodies, w.ff)) < TOL
+
+
+@pytest.mark.parametrize("q_slab", [64, 128])
+@pytest.mark.parametrize("n_q", [5, 16, 33, 47, 64, 65, 80, 100, 111, 112, 113, 130, 201, 240])
+def test_wide_slab_tails(saxs, oracle_lib, q_slab, n_q):
+    # every tail width of the wide uniform path (16..112 after full slabs)
+    rng = np.random.default_rng(n_q)
+    w = W.make_config(2, seed=19, n_override=300)
+    q = W.q_grid(n_q, 0.5)
+    ff = W.exp_form_factors(q, W.Z5, rng.uniform(0.5, 2.0, 5))
+    _, out64, cfg = gpu_curve(saxs, q, ff, w.bodies, q_slab=q_slab)
+    assert cfg["uniform_q"] or n_q < 3
+    assert rel(out64, oracle_lib.debye_f64(q, w.bodies, ff)) < TOL
 
 
 def test_forward_general_q_path(saxs, oracle_lib):
@@ -182,7 +195,7 @@ def test_autotuned_slab(saxs, oracle_lib):
     _lib.lib().rsx_autotune_clear()
     w = W.make_config(2, seed=18, n_override=3000)
     _, out64, cfg = gpu_curve(saxs, w.q, w.ff, w.bodies, autotune=True)
-    assert cfg["q_slab"] in (16, 32, 64)
+    assert cfg["q_slab"] in (16, 32, 64, 128)
     assert rel(out64, oracle_lib.debye_f64(w.q, w.bodies, w.ff)) < TOL
     _, again, cfg2 = gpu_curve(saxs, w.q, w.ff, w.bodies, autotune=True)   # cached choice
     assert cfg2["q_slab"] == cfg["q_slab"]
