@@ -10,6 +10,8 @@
 // the counter only hands out work, so a CTA finishes as soon as the units
 // run out.
 #include "debye_device.cuh"
+
+#include <algorithm>
 #include "rsx_batch_internal.h"
 
 namespace rsx {
@@ -30,6 +32,26 @@ __global__ void __launch_bounds__(kBlockAtoms, QS >= 64 ? 3 : 1)
             break;
         const int item = work_order[w / n_slabs];
         forward_item<QS, UNIFORM, false>(a, item, k_base + (w % n_slabs) * QS);
+    }
+}
+
+// Wide uniform slabs (no water), as forward_wide_kernel.
+template <int QS, int IL>
+__global__ void __launch_bounds__(kBlockAtoms, QS <= 64 ? 3 : 2)
+    batch_wide_kernel(const DebyeArgs a, const int *work_order, int n_units, int n_slabs,
+                      int k_base, int *counter)
+{
+    __shared__ int s_w;
+    for (;;) {
+        if (threadIdx.x == 0)
+            s_w = atomicAdd(counter, 1);
+        __syncthreads();
+        const int w = s_w;
+        __syncthreads();
+        if (w >= n_units)
+            break;
+        const int item = work_order[w / n_slabs];
+        forward_wide_item<QS, IL>(a, item, k_base + (w % n_slabs) * QS);
     }
 }
 
@@ -149,6 +171,60 @@ cudaError_t launch_batch_forward(const DebyeArgs &a, const int *work_order, int 
 #undef RSX_BF
 }
 
+template <class K>
+static int occupancy_grid(K kfn, size_t smem, int sms);
+
+template <int QS, int IL = 2>
+static cudaError_t wide_batch_launch(const DebyeArgs &a, const int *order, int n_items,
+                                     int n_slabs, int k_base, int *counter, int sms,
+                                     cudaStream_t st)
+{
+    auto kfn = batch_wide_kernel<QS, IL>;
+    const int grid = std::min(occupancy_grid(kfn, 0, sms), n_items * n_slabs);
+    kfn<<<grid, kBlockAtoms, 0, st>>>(a, order, n_items * n_slabs, n_slabs, k_base, counter);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_forward_wide(const DebyeArgs &a, const int *work_order,
+                                      int n_work_items, int q_slab, int *counters, int sms,
+                                      cudaStream_t st)
+{
+    if (n_work_items == 0)
+        return cudaSuccess;
+    const WidePlan p = wide_plan(a.n_q, q_slab);
+    if (p.full > 0) {
+        cudaError_t e;
+        e = p.main == 64 ? wide_batch_launch<64, 2>(a, work_order, n_work_items, p.full, 0,
+                                                    counters, sms, st)
+                         : wide_batch_launch<112, 4>(a, work_order, n_work_items, p.full, 0,
+                                                     counters, sms, st);
+        if (e != cudaSuccess)
+            return e;
+    }
+    if (p.tail_len == 0)
+        return cudaSuccess;
+#define RSX_BW(QS)                                                                         \
+    return wide_batch_launch<QS>(a, work_order, n_work_items, 1, p.tail_k0, counters + 1, sms, st)
+    switch ((p.tail_len + 15) / 16) {
+    case 1:
+        RSX_BW(16);
+    case 2:
+        RSX_BW(32);
+    case 3:
+        RSX_BW(48);
+    case 4:
+        RSX_BW(64);
+    case 5:
+        RSX_BW(80);
+    case 6:
+        RSX_BW(96);
+    default:
+        RSX_BW(112);
+    }
+#undef RSX_BW
+}
+
 template <int QS, bool U>
 static cudaError_t adj_launch(const DebyeArgs &a, const int *order, int n_items, int *counter,
                               int grid, cudaStream_t st)
@@ -228,8 +304,12 @@ int batch_forward_grid(int q_slab, bool uniform, int sms)
     case 32:
         return uniform ? occupancy_grid(batch_forward_kernel<32, true>, 0, sms)
                        : occupancy_grid(batch_forward_kernel<32, false>, 0, sms);
+    case 64:
+        return uniform ? occupancy_grid(batch_wide_kernel<64, 2>, 0, sms)
+                       : occupancy_grid(batch_forward_kernel<32, false>, 0, sms);
     default:
-        return occupancy_grid(batch_forward_kernel<64, true>, 0, sms);
+        return uniform ? occupancy_grid(batch_wide_kernel<112, 4>, 0, sms)
+                       : occupancy_grid(batch_forward_kernel<32, false>, 0, sms);
     }
 }
 

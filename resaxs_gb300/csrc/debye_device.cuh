@@ -564,8 +564,8 @@ __device__ __forceinline__ void forward_item(const DebyeArgs &a, int item_idx, i
 // Pairs with theta > pi/2 (cos(theta/2)^2 < 1/2, far-apart bodies on coarse
 // grids) take the rotation form with alpha directly.
 
-constexpr int kAdjSlab = 64;   // q values between reseeds
-constexpr int kAdjStride = 65; // table entries per slab (delta has L + 1)
+constexpr int kAdjSlab = 128;   // q values between reseeds
+constexpr int kAdjStride = 129; // table entries per slab (delta has L + 1)
 
 // Table entry m of slab sl: (delta_m, beta_m, alpha_m, 0).
 __device__ __forceinline__ void adjoint_uniform_table(const DebyeArgs &a, float4 *tab, int n_slabs,
@@ -641,6 +641,34 @@ __device__ __forceinline__ void adj_circle_slab2(const float4 *t, int L, float s
     const float d = t[L].x;
     P1 = fmaf(d, e1, P1);
     P2 = fmaf(d, e2, P2);
+}
+
+// Four pairs interleaved (all on the magic-circle form).
+__device__ __forceinline__ void adj_circle_slab4(const float4 *t, int L, float (&s)[4],
+                                                 float (&e)[4], const float (&ac)[4],
+                                                 float (&P)[4], float (&Q)[4])
+{
+    for (int c = 0; c < L; c += 8) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const float2 cf = *reinterpret_cast<const float2 *>(t + c + u);
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                P[v] = fmaf(cf.x, e[v], P[v]);
+                Q[v] = fmaf(cf.y, s[v], Q[v]);
+            }
+#pragma unroll
+            for (int v = 0; v < 4; ++v)
+                e[v] = fmaf(-ac[v], s[v], e[v]);
+#pragma unroll
+            for (int v = 0; v < 4; ++v)
+                s[v] = fmaf(ac[v], e[v], s[v]);
+        }
+    }
+    const float d = t[L].x;
+#pragma unroll
+    for (int v = 0; v < 4; ++v)
+        P[v] = fmaf(d, e[v], P[v]);
 }
 
 // Rotation form for one pair over one slab: A += sum alpha cos, B += sum beta sin.
@@ -720,6 +748,34 @@ __device__ __forceinline__ void adj_pair2_sums(const DebyeArgs &a, const float4 
     B2 = Q2;
 }
 
+__device__ __forceinline__ void adj_pair4_sums(const DebyeArgs &a, const float4 *tab, int n_slabs,
+                                               const AdjPair (&p)[4], float (&A)[4],
+                                               float (&B)[4])
+{
+    float P[4] = {0.f, 0.f, 0.f, 0.f}, Q[4] = {0.f, 0.f, 0.f, 0.f}, ac[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v)
+        ac[v] = 2.0f * p[v].sh;
+    for (int sl = 0; sl < n_slabs; ++sl) {
+        const int kb = sl * kAdjSlab;
+        const int L = (min(kAdjSlab, a.n_q - kb) + 7) & ~7;
+        const float q0 = a.q[kb];
+        float s[4], e[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            float c;
+            sincos_prod(q0, p[v].r, s[v], c);
+            e[v] = fmaf(c, p[v].ch, s[v] * p[v].sh);
+        }
+        adj_circle_slab4(tab + sl * kAdjStride, L, s, e, ac, P, Q);
+    }
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        A[v] = P[v] * (0.5f / p[v].ch);
+        B[v] = Q[v];
+    }
+}
+
 // Scatters one pair's gradient: the I side into the thread's registers, the J
 // side (summed over the warp) into shared memory.
 __device__ __forceinline__ void adj_scatter(const AdjPair &p, float A, float B, bool use,
@@ -755,6 +811,9 @@ __host__ __device__ inline size_t adjoint_smem_bytes(int n_q, int qs, bool unifo
     return (size_t)n_slabs * qs * (water ? 8 : 4) * sizeof(float);
 }
 
+// IL pairs per thread step together (4: measured 18 % faster than 2 at
+// N = 50,000, 256 q; 71 registers).
+template <int IL>
 __device__ __forceinline__ void adjoint_uniform_item(const DebyeArgs &a, int item_idx)
 {
     extern __shared__ float4 s_dyn[];
@@ -789,6 +848,26 @@ __device__ __forceinline__ void adjoint_uniform_item(const DebyeArgs &a, int ite
         __syncthreads();
         const bool diag = (b == it.bi);
         int jj = 0;
+        if (IL == 4) {
+            for (; jj + 3 < bj.len; jj += 4) {
+                AdjPair p[4];
+#pragma unroll
+                for (int v = 0; v < 4; ++v)
+                    p[v] = adj_pair(pi, s_pos[jj + v], dq);
+                float A[4], B[4];
+                if (p[0].circle && p[1].circle && p[2].circle && p[3].circle) {
+                    adj_pair4_sums(a, tab, n_slabs, p, A, B);
+                } else {
+#pragma unroll
+                    for (int v = 0; v < 4; ++v)
+                        adj_pair_sums(a, tab, n_slabs, p[v], A[v], B[v]);
+                }
+#pragma unroll
+                for (int v = 0; v < 4; ++v)
+                    adj_scatter(p[v], A[v], B[v], valid_i && (!diag || jj + v > tid), gi0, gi1,
+                                gi2, s_gj, jj + v, lane);
+            }
+        }
         for (; jj + 1 < bj.len; jj += 2) {
             const AdjPair p1 = adj_pair(pi, s_pos[jj], dq);
             const AdjPair p2 = adj_pair(pi, s_pos[jj + 1], dq);
@@ -991,7 +1070,7 @@ template <int QS, bool UNIFORM, bool WATER>
 __device__ __forceinline__ void adjoint_item(const DebyeArgs &a, int item_idx, int n_slabs)
 {
     if constexpr (UNIFORM && !WATER)
-        adjoint_uniform_item(a, item_idx);
+        adjoint_uniform_item<4>(a, item_idx);
     else
         adjoint_general_item<QS, UNIFORM, WATER>(a, item_idx, n_slabs);
 }

@@ -22,7 +22,6 @@
 #include "debye_device.cuh"
 
 #include <atomic>
-#include <cstdlib>
 
 namespace rsx {
 
@@ -309,37 +308,53 @@ static cudaError_t wide_tail(const DebyeArgs &a, int k0, int len, cudaStream_t s
     }
 }
 
-static int env_int(const char *name, int dflt)
+// Relative cost of one slab per pair on GB300 (CUDA-event times of the
+// wide kernels at N = 20,000 and 50,000, in units of ~10 ns per 1e6 pairs):
+// full slabs of 64 q (2 pairs interleaved, 3 CTAs/SM) and of 112 q (4 pairs
+// interleaved, 2 CTAs/SM), and a single tail slab of 16..112 q.
+static constexpr float kCostMain64 = 1.88f, kCostMain112 = 3.30f;
+static constexpr float kCostTail[7] = {1.10f, 1.40f, 1.65f, 1.88f, 2.81f, 2.80f, 3.40f};
+
+static float tail_cost(int len) { return len > 0 ? kCostTail[(len + 15) / 16 - 1] : 0.f; }
+
+// The cheapest of: 64-q slabs and a tail; 64-q slabs with a short remainder
+// (<= 48 q) folded into the last slab; 112-q slabs and a tail.
+WidePlan wide_plan(int n_q, int q_slab)
 {
-    const char *v = getenv(name);
-    return v ? atoi(v) : dflt;
+    WidePlan best{};
+    float best_cost = 3.4e38f;
+    auto consider = [&](int main, int full, int rest, float cost) {
+        if (cost < best_cost) {
+            best_cost = cost;
+            best = WidePlan{main, full, full * main, rest, main == 112 ? 4 : 2};
+        }
+    };
+    const int f64 = n_q / 64, r64 = n_q - 64 * f64;
+    consider(64, f64, r64, f64 * kCostMain64 + tail_cost(r64));
+    if (f64 > 0 && r64 > 0 && r64 <= 48)
+        consider(64, f64 - 1, r64 + 64, (f64 - 1) * kCostMain64 + tail_cost(r64 + 64));
+    if (q_slab >= 128) {
+        const int f112 = n_q / 112, r112 = n_q - 112 * f112;
+        consider(112, f112, r112, f112 * kCostMain112 + tail_cost(r112));
+    }
+    return best;
 }
 
-// Uniform grid without water: full slabs of `main` q (64 or 112), then the
-// remainder in one slab of the next multiple of 16 (a second launch on the
-// same stream).
-static cudaError_t launch_forward_wide(const DebyeArgs &a, int main, cudaStream_t st)
+// Uniform grid without water: full slabs of the plan's main width, then the
+// tail slab (a second launch on the same stream).
+static cudaError_t launch_forward_wide(const DebyeArgs &a, int q_slab, cudaStream_t st)
 {
-    static const int il = env_int("RSX_WIDE_IL", 2);
-    static const int merge = env_int("RSX_WIDE_MERGE", 0);
-    int full = a.n_q / main;
-    int rest = a.n_q - full * main;
-    if (merge && main == 64 && full > 0 && rest > 0 && rest <= 48) {
-        --full; // the last full slab and the remainder run as one slab of <= 112
-        rest += 64;
-    }
-    if (full > 0) {
+    const WidePlan p = wide_plan(a.n_q, q_slab);
+    if (p.full > 0) {
         cudaError_t e;
-        if (main == 64)
-            e = il == 4 ? wide_launch<64, 4>(a, 0, full, st) : wide_launch<64, 2>(a, 0, full, st);
-        else
-            e = il == 4 ? wide_launch<112, 4>(a, 0, full, st) : wide_launch<112, 2>(a, 0, full, st);
+        e = p.main == 64 ? wide_launch<64, 2>(a, 0, p.full, st)
+                         : wide_launch<112, 4>(a, 0, p.full, st);
         if (e != cudaSuccess)
             return e;
     }
-    if (rest == 0)
+    if (p.tail_len == 0)
         return cudaSuccess;
-    return wide_tail(a, full * main, rest, st);
+    return wide_tail(a, p.tail_k0, p.tail_len, st);
 }
 
 // Uniform grids without water and q_slab 64 / 128 take the wide slabs (64 or
@@ -352,7 +367,7 @@ cudaError_t launch_forward(const DebyeArgs &a, int q_slab, bool uniform, bool wa
     if (a.n_items == 0)
         return cudaSuccess;
     if (uniform && !water && q_slab >= 64)
-        return launch_forward_wide(a, q_slab >= 128 ? 112 : 64, st);
+        return launch_forward_wide(a, q_slab, st);
     const int full = a.n_q / q_slab;
     const int rest = a.n_q - full * q_slab;
     if (full > 0) {

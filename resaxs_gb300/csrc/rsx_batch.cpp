@@ -278,8 +278,16 @@ rsx_status enqueue_pass(rsx_batch *h, bool with_adjoint, int q_slab)
                  "batch bodies");
     RSX_TRY_CUDA(cudaMemsetAsync(h->d_counter, 0, sizeof(int) * 4, h->st), "counters");
     const DebyeArgs a = batch_args(h, false);
-    const int full = h->n_q / q_slab, rest = h->n_q - full * q_slab;
     const int n_items = (int)h->items.size();
+    const bool wide = h->uniform && q_slab >= 64;
+    if (wide) {
+        int sms = 152;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+        RSX_TRY_CUDA(launch_batch_forward_wide(a, h->d_order, n_items, q_slab, h->d_counter, sms,
+                                               h->st),
+                     "batch forward");
+    }
+    const int full = wide ? 0 : h->n_q / q_slab, rest = wide ? 0 : h->n_q - full * q_slab;
     if (full > 0)
         RSX_TRY_CUDA(launch_batch_forward(a, h->d_order, n_items, q_slab, full, 0, h->uniform,
                                           h->d_counter + 0, h->fwd_grid, h->st),
@@ -392,11 +400,11 @@ rsx_status run_graph(rsx_batch *h, cudaGraphExec_t g)
 // Times one forward pass with each candidate q-slab and keeps the fastest.
 rsx_status tune(rsx_batch *h)
 {
-    const int candidates[] = {32, 64};
+    const int candidates[] = {32, 64, 128};
     float best = 1e30f;
     int best_qs = h->q_slab;
     for (int qs : candidates) {
-        if (qs == 64 && !h->uniform)
+        if (qs >= 64 && !h->uniform)
             continue;
         h->q_slab = qs;
         cudaGraphExec_t g = nullptr;
@@ -436,8 +444,9 @@ rsx_status rsx_batch_create(const float *q, int n_q, const float *t_factors, int
     rsx_debye_default_options(&o);
     if (opts)
         o = *opts;
-    if (o.q_slab != 0 && o.q_slab != 8 && o.q_slab != 16 && o.q_slab != 32 && o.q_slab != 64)
-        return fail(RSX_INVALID_ARG, "q_slab must be 0, 8, 16, 32 or 64");
+    if (o.q_slab != 0 && o.q_slab != 8 && o.q_slab != 16 && o.q_slab != 32 && o.q_slab != 64 &&
+        o.q_slab != 128)
+        return fail(RSX_INVALID_ARG, "q_slab must be 0, 8, 16, 32, 64 or 128");
     long long total = 0;
     for (int m = 0; m < n_members; ++m) {
         if (member_sizes[m] < 0)
@@ -472,7 +481,7 @@ rsx_status rsx_batch_create(const float *q, int n_q, const float *t_factors, int
             h->uniform = std::fabs((double)q[k] - (q0 + k * step)) <= 4e-7 * std::fabs((double)q[k]) + 1e-30;
         h->dq = (float)step;
     }
-    h->q_slab = o.q_slab ? o.q_slab : (h->uniform && n_q >= 128 ? 64 : 32);
+    h->q_slab = o.q_slab ? o.q_slab : (h->uniform && n_q >= 64 ? 128 : 32);
     if (!h->uniform && h->q_slab > 32)
         h->q_slab = 32;
     h->autotune = o.autotune != 0 && o.q_slab == 0;

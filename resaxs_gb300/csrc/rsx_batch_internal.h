@@ -31,6 +31,11 @@ struct BatchLossArgs {
 cudaError_t launch_batch_forward(const DebyeArgs &a, const int *work_order, int n_work_items,
                                  int q_slab, int n_slabs, int k_base, bool uniform,
                                  int *counter, int grid, cudaStream_t st);
+// Wide uniform slabs (no water, q_slab 64 / 128): persistent main and tail
+// launches over counters[0] and counters[1].
+cudaError_t launch_batch_forward_wide(const DebyeArgs &a, const int *work_order,
+                                      int n_work_items, int q_slab, int *counters, int sms,
+                                      cudaStream_t st);
 cudaError_t launch_batch_adjoint(const DebyeArgs &a, const int *work_order, int n_work_items,
                                  int q_slab, bool uniform, int *counter, int grid,
                                  cudaStream_t st);

@@ -73,6 +73,15 @@ struct DeltaArgs {
 };
 
 // launchers (debye_kernels.cu); all asynchronous on `st`
+// Slab plan of the wide uniform forward: `full` slabs of `main` q from q 0,
+// then one tail slab [tail_k0, tail_k0 + tail_len) (tail_len 0: none); `il`
+// pairs interleaved per thread in the main slabs.  q_slab 64 restricts the
+// plan to 64-q main slabs; 128 also allows 112-q slabs.
+struct WidePlan {
+    int main, full, tail_k0, tail_len, il;
+};
+WidePlan wide_plan(int n_q, int q_slab);
+
 cudaError_t launch_forward(const DebyeArgs &a, int q_slab, bool uniform, bool water,
                            cudaStream_t st);
 cudaError_t launch_assemble(const AssembleArgs &a, cudaStream_t st);
