@@ -71,6 +71,12 @@ rsx_status rsx_debug_layout(const rsx_body *bodies, int n_bodies, int n_factors,
                             int min_adj_items, int *n_blocks, int *n_items, int *n_adj_items,
                             int *pairs_covered_ok);
 
+/* Host-only check of the shard split used by rsx_debye_calc_shard: item
+ * bounds[0..n_shards] (shard s = items [bounds[s], bounds[s+1])) and, if
+ * pairs is not NULL, the body pairs of each shard. */
+rsx_status rsx_debug_shard_items(const rsx_body *bodies, int n_bodies, int n_factors,
+                                 int max_items, int n_shards, int *bounds, double *pairs);
+
 /* Measures the sustained FP32 FMA rate of `device` (-1 = current) with a
  * register-resident FMA-chain kernel on every SM: *fma_per_s = lane FMAs per
  * second.  The denominator of the pair*q roofline. */
@@ -158,6 +164,16 @@ rsx_status rsx_debye_set_water(rsx_debye *h, float weight, int water_index, cons
 /* i_saxs::calc_curve (saxs_algorithm.hpp:162; saxs_alg_cl_gpu_pt_wf.cpp:414-458):
  * full I(q) of n_bodies bodies. */
 rsx_status rsx_debye_calc(rsx_debye *h, const rsx_body *bodies, float *out_iq);
+
+/* One shard of the full forward, for sharding one structure over ranks (no
+ * reference counterpart; the reference runs one device per structure).  The
+ * forward work items are split into n_shards contiguous runs balanced by pair
+ * count; shard `shard` computes its run and writes its additive FP64
+ * contribution to I(q) (shard 0 also carries the self terms and I(0)), so the
+ * sum over shards -- one all-reduce of n_q doubles -- is the curve of
+ * rsx_debye_calc.  Afterwards recalc needs a full rsx_debye_calc first. */
+rsx_status rsx_debye_calc_shard(rsx_debye *h, const rsx_body *bodies, int shard, int n_shards,
+                                double *out_iq);
 
 /* i_saxs::recalc_curve (saxs_algorithm.hpp:172; saxs_alg_cl_gpu_pt_wf.cpp:468-577):
  * bodies is the full caller vector; bodies [upd_start, upd_start+upd_length)

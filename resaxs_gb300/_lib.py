@@ -78,6 +78,9 @@ SIGNATURES = [
     ("rsx_debye_set_factors", _st, [_vp, _f32p, _i]),
     ("rsx_debye_set_water", _st, [_vp, ctypes.c_float, _i, _vp]),
     ("rsx_debye_calc", _st, [_vp, _f32p, _f32p]),
+    ("rsx_debye_calc_shard", _st, [_vp, _f32p, _i, _i, _f64p]),
+    ("rsx_debug_shard_items", _st, [_f32p, _i, _i, _i, _i, np.ctypeslib.ndpointer(np.int32),
+                                    _vp]),
     ("rsx_debye_recalc_range", _st, [_vp, _f32p, _u, _u, _f32p]),
     ("rsx_debye_recalc_indices", _st, [_vp, _f32p, _u32p, _u, _f32p]),
     ("rsx_debye_commit", _st, [_vp]),

@@ -191,16 +191,33 @@ struct WideSeed {
     bool big;
 };
 
-__device__ __forceinline__ WideSeed wide_seed(float q0, float dq, float r, float sc)
+// sin/cos(q0 r) (exactly 0 and 1 when q0 = 0, as sincos_prod gives) and
+// sin/cos(theta/2); `small_theta` (uniform over the launch) promises
+// |theta/2| < pi/4, where the reduction is the identity (sincos_small2 gives
+// sincos_rr2's results bit for bit).  Both tests are uniform branches.
+__device__ __forceinline__ void seed_angles(float q0, float dq, float r, bool small_theta,
+                                            float &s0, float &c0, float &sh, float &ch)
+{
+    if (q0 == 0.f) {
+        s0 = 0.f;
+        c0 = 1.f;
+    } else {
+        sincos_prod(q0, r, s0, c0);
+    }
+    const float th = dq * r;
+    const float th_lo = fmaf(dq, r, -th);
+    if (small_theta)
+        sincos_small2(0.5f * th, 0.5f * th_lo, sh, ch);
+    else
+        sincos_rr2(0.5f * th, 0.5f * th_lo, sh, ch);
+}
+
+__device__ __forceinline__ WideSeed wide_seed(float q0, float dq, float r, float sc,
+                                              bool small_theta = false)
 {
     WideSeed p;
     float s0, c0, sh, ch;
-    sincos_prod(q0, r, s0, c0);
-    {
-        const float th = dq * r;
-        const float th_lo = fmaf(dq, r, -th);
-        sincos_rr2(0.5f * th, 0.5f * th_lo, sh, ch);
-    }
+    seed_angles(q0, dq, r, small_theta, s0, c0, sh, ch);
     p.big = ch * ch < sh * sh;
     p.s = s0 * sc;
     if (!p.big) {
@@ -309,6 +326,7 @@ __device__ __forceinline__ void forward_wide_item(const DebyeArgs &a, int item_i
     const float4 pi = valid_i ? a.pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float q0 = a.q[k0];
     const float dq = a.dq;
+    const bool small_th = a.small_theta != 0;
 
     double acc[NR];
 #pragma unroll
@@ -335,7 +353,7 @@ __device__ __forceinline__ void forward_wide_item(const DebyeArgs &a, int item_i
                     float r, ri, dx, dy, dz;
                     pair_r(pi, s_pos[jj + u], r, ri, dx, dy, dz);
                     const bool use = valid_i && (!diag || jj + u > tid);
-                    p[u] = wide_seed(q0, dq, r, use ? ri : 0.f);
+                    p[u] = wide_seed(q0, dq, r, use ? ri : 0.f, small_th);
                 }
                 if (!(p[0].big || p[1].big || p[2].big || p[3].big)) {
                     wide_pair4<QS, QP>(p[0], p[1], p[2], p[3], S);
@@ -351,8 +369,8 @@ __device__ __forceinline__ void forward_wide_item(const DebyeArgs &a, int item_i
             pair_r(pi, s_pos[jj + 1], r2, ri2, dx, dy, dz);
             const bool u1 = valid_i && (!diag || jj > tid);
             const bool u2 = valid_i && (!diag || jj + 1 > tid);
-            const WideSeed p1 = wide_seed(q0, dq, r1, u1 ? ri1 : 0.f);
-            const WideSeed p2 = wide_seed(q0, dq, r2, u2 ? ri2 : 0.f);
+            const WideSeed p1 = wide_seed(q0, dq, r1, u1 ? ri1 : 0.f, small_th);
+            const WideSeed p2 = wide_seed(q0, dq, r2, u2 ? ri2 : 0.f, small_th);
             if (!p1.big && !p2.big)
                 wide_pair2<QS, QP>(p1, p2, S);
             else
@@ -362,7 +380,7 @@ __device__ __forceinline__ void forward_wide_item(const DebyeArgs &a, int item_i
             float r, rinv, dx, dy, dz;
             pair_r(pi, s_pos[jj], r, rinv, dx, dy, dz);
             const bool use = valid_i && (!diag || jj > tid);
-            wide_pair1<QS, QP>(wide_seed(q0, dq, r, use ? rinv : 0.f), S);
+            wide_pair1<QS, QP>(wide_seed(q0, dq, r, use ? rinv : 0.f, small_th), S);
         }
 #pragma unroll
         for (int c = 0; c < NR; ++c) {
@@ -693,6 +711,8 @@ struct AdjPair {
     bool circle;  // magic-circle form (theta <= pi/2)
 };
 
+// (The reduction-free sincos of small theta is not used here: its branch
+// costs this kernel 8 registers and a CTA per SM, more than it saves.)
 __device__ __forceinline__ AdjPair adj_pair(const float4 &pi, const float4 &pj, float dq)
 {
     AdjPair p;
@@ -702,6 +722,17 @@ __device__ __forceinline__ AdjPair adj_pair(const float4 &pi, const float4 &pj, 
     sincos_rr2(0.5f * th, 0.5f * th_lo, p.sh, p.ch);
     p.circle = 2.0f * p.ch * p.ch >= 1.0f;
     return p;
+}
+
+// sin/cos(q0 r) of a slab seed: exactly (0, 1) at q0 = 0, as sincos_prod gives.
+__device__ __forceinline__ void slab_seed(float q0, float r, float &s, float &c)
+{
+    if (q0 == 0.f) {
+        s = 0.f;
+        c = 1.f;
+    } else {
+        sincos_prod(q0, r, s, c);
+    }
 }
 
 // Sums A (cosine side) and B (sine side) of one pair over all slabs.
@@ -714,7 +745,7 @@ __device__ __forceinline__ void adj_pair_sums(const DebyeArgs &a, const float4 *
         const int L = (min(kAdjSlab, a.n_q - kb) + 7) & ~7;
         const float4 *t = tab + sl * kAdjStride;
         float s0, c0;
-        sincos_prod(a.q[kb], p.r, s0, c0);
+        slab_seed(a.q[kb], p.r, s0, c0);
         if (p.circle) {
             adj_circle_slab(t, L, s0, fmaf(c0, p.ch, s0 * p.sh), 2.0f * p.sh, P, Q);
         } else {
@@ -737,8 +768,8 @@ __device__ __forceinline__ void adj_pair2_sums(const DebyeArgs &a, const float4 
         const float4 *t = tab + sl * kAdjStride;
         const float q0 = a.q[kb];
         float s1, c1, s2, c2;
-        sincos_prod(q0, p1.r, s1, c1);
-        sincos_prod(q0, p2.r, s2, c2);
+        slab_seed(q0, p1.r, s1, c1);
+        slab_seed(q0, p2.r, s2, c2);
         adj_circle_slab2(t, L, s1, fmaf(c1, p1.ch, s1 * p1.sh), 2.0f * p1.sh, s2,
                          fmaf(c2, p2.ch, s2 * p2.sh), 2.0f * p2.sh, P1, Q1, P2, Q2);
     }
@@ -764,7 +795,7 @@ __device__ __forceinline__ void adj_pair4_sums(const DebyeArgs &a, const float4 
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
             float c;
-            sincos_prod(q0, p[v].r, s[v], c);
+            slab_seed(q0, p[v].r, s[v], c);
             e[v] = fmaf(c, p[v].ch, s[v] * p[v].sh);
         }
         adj_circle_slab4(tab + sl * kAdjStride, L, s, e, ac, P, Q);

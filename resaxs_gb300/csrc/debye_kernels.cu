@@ -21,6 +21,7 @@
 //    shuffles (lane k ends with q index k).  Across warps and CTAs: FP64.
 #include "debye_device.cuh"
 
+#include <algorithm>
 #include <atomic>
 
 namespace rsx {
@@ -208,6 +209,98 @@ __global__ void mark_moved_kernel(int *slot, const int *moved_idx, int k, int se
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m < k)
         slot[moved_idx[m]] = set ? m : -1;
+}
+
+// Incremental delta on a uniform grid with wide slabs: as delta_kernel, but
+// QS up to 112 q per seed pair, FP32 per-tile sums reduce-scattered into FP64
+// lane accumulators (forward_wide_item's scheme).  The two chains of a pair
+// (new position, old position seeded with -1/r) run interleaved.
+template <int QS>
+__global__ void __launch_bounds__(kBlockAtoms, QS <= 64 ? 3 : 2) delta_wide_kernel(const DeltaArgs a,
+                                                                                  int k_base)
+{
+    constexpr int QP = WideSlab<QS>::QP, NR = WideSlab<QS>::NR;
+    __shared__ float4 s_new[kBlockAtoms], s_old[kBlockAtoms];
+    __shared__ int s_idx[kBlockAtoms];
+    __shared__ float s_fx[QP];
+    __shared__ double s_red[kBlockAtoms / 32][QP];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const BlockDesc by = a.blocks[blockIdx.x];
+    const int k0 = k_base + blockIdx.y * QS;
+    // moved tiles z, z + G, ... of this CTA (G = gridDim.z groups split the
+    // moved list, so a few static blocks still give enough CTAs)
+    const int group = blockIdx.z, n_groups = gridDim.z;
+    const int y = by.start + tid;
+    const bool valid = tid < by.len;
+    const float4 py_old = valid ? a.pos_old[y] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int slot = valid ? a.moved_slot[y] : -1;
+    const float4 py_new = slot >= 0 ? a.moved_new[slot] : py_old;
+    // pairs with a static body are met once (weight 1); pairs inside the moved
+    // list are met from both ends (weight 1/2 each)
+    const float mult = !valid ? 0.f : (slot >= 0 ? 0.5f : 1.0f);
+    const float q0 = a.q[k0];
+    const float dq = a.dq;
+
+    double acc[NR];
+#pragma unroll
+    for (int c = 0; c < NR; ++c)
+        acc[c] = 0.0;
+    for (int mt = group; mt < a.n_mtiles; mt += n_groups) {
+        const BlockDesc tile = a.mtiles[mt];
+        __syncthreads();
+        if (tid < tile.len) {
+            const int m = tile.start + tid;
+            const int idx = a.moved_idx[m];
+            s_new[tid] = a.moved_new[m];
+            s_old[tid] = a.pos_old[idx];
+            s_idx[tid] = idx;
+        }
+        for (int k = tid; k < QP; k += kBlockAtoms)
+            s_fx[k] = (k < QS && k0 + k < a.n_q) ? a.ff[(size_t)(k0 + k) * a.n_types + tile.type]
+                                                 : 0.f;
+        __syncthreads();
+        float S[QP];
+#pragma unroll
+        for (int k = 0; k < QP; ++k)
+            S[k] = 0.f;
+        for (int jj = 0; jj < tile.len; ++jj) {
+            const bool use = valid && s_idx[jj] != y;
+            float rn, rninv, ro, roinv, dx, dy, dz;
+            pair_r(py_new, s_new[jj], rn, rninv, dx, dy, dz);
+            pair_r(py_old, s_old[jj], ro, roinv, dx, dy, dz);
+            const WideSeed pn = wide_seed(q0, dq, rn, use ? mult * rninv : 0.f);
+            const WideSeed po = wide_seed(q0, dq, ro, use ? -mult * roinv : 0.f);
+            if (!pn.big && !po.big)
+                wide_pair2<QS, QP>(pn, po, S);
+            else
+                wide_mixed2<QS, QP>(pn, po, S);
+        }
+#pragma unroll
+        for (int c = 0; c < NR; ++c) {
+            float v[32];
+#pragma unroll
+            for (int k = 0; k < 32; ++k)
+                v[k] = s_fx[32 * c + k] * S[32 * c + k];
+            warp_reduce_scatter<32>(v, lane);
+            acc[c] += (double)v[0];
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < NR; ++c)
+        s_red[warp][32 * c + lane] = acc[c];
+    __syncthreads();
+    for (int k = tid; k < QS; k += kBlockAtoms) {
+        const int kk = k0 + k;
+        if (kk >= a.n_q)
+            continue;
+        double s = 0.0;
+#pragma unroll
+        for (int w = 0; w < kBlockAtoms / 32; ++w)
+            s += s_red[w][k];
+        a.partial[(size_t)kk * a.n_blocks * n_groups + (size_t)group * a.n_blocks + blockIdx.x] =
+            s * (double)a.ff[(size_t)kk * a.n_types + by.type];
+    }
 }
 
 __global__ void f64_to_f32_kernel(const double *src, float *dst, int n)
@@ -402,10 +495,63 @@ static cudaError_t delta_qs(const DeltaArgs &a, bool uniform, cudaStream_t st)
     return cudaGetLastError();
 }
 
+template <int QS>
+static cudaError_t delta_wide_launch(const DeltaArgs &a, int k_base, int n_slabs,
+                                     cudaStream_t st)
+{
+    delta_wide_kernel<QS><<<dim3(a.n_blocks, n_slabs, delta_groups(a)), kBlockAtoms, 0, st>>>(
+        a, k_base);
+    count_launch();
+    return cudaGetLastError();
+}
+
+int delta_groups(const DeltaArgs &a)
+{
+    return std::max(1, std::min(std::min(kDeltaGroups, a.n_mtiles), a.max_groups));
+}
+
+// Uniform grids and q_slab 64 / 128: the forward's wide slab plan restricted
+// to 64-q main slabs (the two chains of a pair already interleave).
+static cudaError_t launch_delta_wide(const DeltaArgs &a, cudaStream_t st)
+{
+    const WidePlan p = wide_plan(a.n_q, 64);
+    if (p.full > 0) {
+        cudaError_t e = p.main == 64 ? delta_wide_launch<64>(a, 0, p.full, st)
+                                     : delta_wide_launch<112>(a, 0, p.full, st);
+        if (e != cudaSuccess)
+            return e;
+    }
+    if (p.tail_len == 0)
+        return cudaSuccess;
+    switch ((p.tail_len + 15) / 16) {
+    case 1:
+        return delta_wide_launch<16>(a, p.tail_k0, 1, st);
+    case 2:
+        return delta_wide_launch<32>(a, p.tail_k0, 1, st);
+    case 3:
+        return delta_wide_launch<48>(a, p.tail_k0, 1, st);
+    case 4:
+        return delta_wide_launch<64>(a, p.tail_k0, 1, st);
+    case 5:
+        return delta_wide_launch<80>(a, p.tail_k0, 1, st);
+    case 6:
+        return delta_wide_launch<96>(a, p.tail_k0, 1, st);
+    default:
+        return delta_wide_launch<112>(a, p.tail_k0, 1, st);
+    }
+}
+
+int delta_parts(const DeltaArgs &a, int q_slab, bool uniform)
+{
+    return (uniform && q_slab >= 64) ? a.n_blocks * delta_groups(a) : a.n_blocks;
+}
+
 cudaError_t launch_delta(const DeltaArgs &a, int q_slab, bool uniform, cudaStream_t st)
 {
     if (a.n_blocks == 0 || a.k == 0)
         return cudaSuccess;
+    if (uniform && q_slab >= 64)
+        return launch_delta_wide(a, st);
     switch (q_slab > 32 ? 32 : q_slab) { // two chains per pair: at most 32 q per slab
     case 8:
         return delta_qs<8>(a, uniform, st);

@@ -56,6 +56,32 @@ std::vector<PairItem> make_items(const std::vector<BlockDesc> &blocks, int jchun
     return items;
 }
 
+// Item range [lo, hi) of shard `shard` of `n_shards`: contiguous runs of the
+// forward items balanced by pair count (|I-block| x sum of |J-blocks|), so a
+// shard's work differs from the mean by at most one item's.
+std::pair<int, int> shard_items(const Layout &L, int shard, int n_shards)
+{
+    const int n = (int)L.items.size();
+    std::vector<double> prefix(n + 1, 0.0);
+    for (int i = 0; i < n; ++i) {
+        const PairItem &it = L.items[i];
+        double w = 0.0;
+        for (int b = it.bj_begin; b < it.bj_end; ++b)
+            w += (double)L.blocks[b].len;
+        prefix[i + 1] = prefix[i] + w * L.blocks[it.bi].len;
+    }
+    auto bound = [&](int s) {
+        if (s <= 0)
+            return 0;
+        if (s >= n_shards)
+            return n;
+        const double target = prefix[n] * s / n_shards;
+        return (int)(std::lower_bound(prefix.begin(), prefix.end(), target) - prefix.begin());
+    };
+    const int lo = std::min(bound(shard), n), hi = std::min(bound(shard + 1), n);
+    return {lo, std::max(lo, hi)};
+}
+
 void build_layout(Layout &L, const rsx_body *bodies, int n, int n_types, int max_items,
                   int min_adj_items)
 {
@@ -132,6 +158,7 @@ struct rsx_debye {
     std::vector<float> q, ff;
     bool uniform = false;
     float dq = 0.f;
+    float lo[3] = {0.f, 0.f, 0.f}, hi[3] = {0.f, 0.f, 0.f}; // extent of the device bodies
     int q_slab = 32;
     int max_items = 16384;
     bool autotune = false, tuned = false;
@@ -259,7 +286,7 @@ rsx_status update_layout(rsx_debye *h, const rsx_body *bodies)
     RSX_TRY(ensure(&h->d_items, h->items_cap, h->L.items.size(), "items"));
     RSX_TRY(ensure(&h->d_adj_items, h->adj_cap, h->L.adj_items.size(), "adjoint items"));
     const size_t need = h->L.items.size() * (size_t)h->n_q;
-    const size_t need_delta = h->L.blocks.size() * (size_t)h->n_q;
+    const size_t need_delta = h->L.blocks.size() * (size_t)kDeltaGroups * h->n_q;
     RSX_TRY(ensure(&h->d_partial, h->partial_cap, std::max(need, need_delta), "partial sums"));
     RSX_TRY_CUDA(cudaMemcpyAsync(h->d_blocks, h->L.blocks.data(),
                                  sizeof(BlockDesc) * h->L.blocks.size(), cudaMemcpyHostToDevice,
@@ -299,6 +326,50 @@ rsx_status upload_water(rsx_debye *h)
     return RSX_OK;
 }
 
+// Bounding box of the bodies on the device: reset by a full upload, grown by
+// moves (never shrunk until the next full upload, so it stays an upper bound).
+void reset_extent(rsx_debye *h, const rsx_body *b, int n)
+{
+    for (int d = 0; d < 3; ++d) {
+        h->lo[d] = 3.4e38f;
+        h->hi[d] = -3.4e38f;
+    }
+    for (int i = 0; i < n; ++i) {
+        const float x[3] = {b[i].x, b[i].y, b[i].z};
+        for (int d = 0; d < 3; ++d) {
+            h->lo[d] = std::min(h->lo[d], x[d]);
+            h->hi[d] = std::max(h->hi[d], x[d]);
+        }
+    }
+}
+
+void grow_extent(rsx_debye *h, const rsx_body *b, unsigned n)
+{
+    for (unsigned i = 0; i < n; ++i) {
+        const float x[3] = {b[i].x, b[i].y, b[i].z};
+        for (int d = 0; d < 3; ++d) {
+            h->lo[d] = std::min(h->lo[d], x[d]);
+            h->hi[d] = std::max(h->hi[d], x[d]);
+        }
+    }
+}
+
+// 1 when every pair has |theta/2| = |dq r / 2| <= 0.7 < pi/4 (the seeds may
+// then skip the range reduction; the result is the same bit for bit).
+int small_theta(const rsx_debye *h)
+{
+    if (!h->uniform || h->n < 2)
+        return 0;
+    double d2 = 0.0;
+    for (int d = 0; d < 3; ++d) {
+        const double e = (double)h->hi[d] - (double)h->lo[d];
+        if (!(e >= 0.0) || !std::isfinite(e))
+            return 0;
+        d2 += e * e;
+    }
+    return std::fabs((double)h->dq) * std::sqrt(d2) * 1.0001 <= 1.4 ? 1 : 0;
+}
+
 DebyeArgs debye_args(rsx_debye *h)
 {
     DebyeArgs a{};
@@ -314,6 +385,7 @@ DebyeArgs debye_args(rsx_debye *h)
     a.n_types = h->n_types;
     a.n_items = (int)h->L.items.size();
     a.dq = h->dq;
+    a.small_theta = small_theta(h);
     a.water_weight = h->water_weight;
     a.water_index = h->water_index;
     return a;
@@ -437,9 +509,10 @@ rsx_status tune_slab(rsx_debye *h)
 }
 
 // Full calculation from caller-order bodies.
-rsx_status full_calc(rsx_debye *h, const rsx_body *bodies)
+rsx_status upload_all(rsx_debye *h, const rsx_body *bodies)
 {
     RSX_TRY(update_layout(h, bodies));
+    reset_extent(h, bodies, h->n);
     for (int s = 0; s < h->n; ++s) {
         const rsx_body &b = bodies[h->L.perm[s]];
         h->h_pos[s] = make_float4(b.x, b.y, b.z, b.w);
@@ -451,6 +524,12 @@ rsx_status full_calc(rsx_debye *h, const rsx_body *bodies)
                                  cudaMemcpyHostToDevice, h->st),
                  "upload factors");
     RSX_TRY(upload_water(h));
+    return RSX_OK;
+}
+
+rsx_status full_calc(rsx_debye *h, const rsx_body *bodies)
+{
+    RSX_TRY(upload_all(h, bodies));
     if (h->autotune && !h->tuned)
         RSX_TRY(tune_slab(h));
     RSX_TRY(forward_device(h));
@@ -531,6 +610,7 @@ rsx_status delta_update(rsx_debye *h, const rsx_body *moved, const unsigned *idx
     a.n_types = h->n_types;
     a.n_blocks = (int)h->L.blocks.size();
     a.n_mtiles = (int)tiles.size();
+    a.max_groups = kDeltaGroups;
     a.dq = h->dq;
     int *d_idx = reinterpret_cast<int *>(h->d_moved + off_idx);
     RSX_LAUNCH(launch_mark_moved(h->d_slot, d_idx, (int)k, 1, h->st), "mark moved");
@@ -539,7 +619,9 @@ rsx_status delta_update(rsx_debye *h, const rsx_body *moved, const unsigned *idx
     RSX_LAUNCH(launch_delta(a, slab_for(h), h->uniform, h->st), "delta kernel");
     if (h->timing)
         RSX_TRY_CUDA(cudaEventRecord(h->ev_k1, h->st), "event");
-    RSX_LAUNCH(launch_assemble(assemble_args(h, a.n_blocks, 1), h->st), "assemble delta");
+    RSX_LAUNCH(launch_assemble(assemble_args(h, delta_parts(a, slab_for(h), h->uniform), 1),
+                               h->st),
+               "assemble delta");
     RSX_LAUNCH(launch_apply_moves(h->d_pos, a.moved_new, d_idx, (int)k, h->st), "apply moves");
     RSX_LAUNCH(launch_mark_moved(h->d_slot, d_idx, (int)k, 0, h->st), "unmark moved");
     return RSX_OK;
@@ -573,6 +655,7 @@ rsx_status recalc_common(rsx_debye *h, const rsx_body *moved, const unsigned *id
         RSX_TRY(full_calc(h, next.data()));
     } else if (k > 0) {
         RSX_TRY(delta_update(h, moved, idx, k));
+        grow_extent(h, moved, k);
         for (unsigned m = 0; m < k; ++m)
             h->cur[idx[m]] = moved[m];
     }
@@ -752,6 +835,70 @@ rsx_status rsx_debye_calc(rsx_debye *h, const rsx_body *bodies, float *out_iq)
     return ok();
 }
 
+rsx_status rsx_debye_calc_shard(rsx_debye *h, const rsx_body *bodies, int shard, int n_shards,
+                                double *out_iq)
+{
+    RSX_TRY(begin_call(h));
+    if (!bodies && h->n > 0)
+        return fail(RSX_INVALID_ARG, "bodies is null");
+    if (!out_iq || n_shards < 1 || shard < 0 || shard >= n_shards)
+        return fail(RSX_INVALID_ARG, "need out_iq and 0 <= shard < n_shards");
+    RSX_TRY(check_bodies(h, bodies, h->n));
+    RSX_TRY(upload_all(h, bodies));
+    // the device positions no longer hold a computed state: an incremental
+    // call needs a full calc first
+    h->computing = false;
+    const auto range = shard_items(h->L, shard, n_shards);
+    DebyeArgs a = debye_args(h);
+    a.items = h->d_items + range.first;
+    a.n_items = range.second - range.first;
+    if (a.n_items > 0)
+        RSX_LAUNCH(launch_forward(a, slab_for(h), h->uniform, has_water(h), h->st),
+                   "forward kernel");
+    if (shard == 0) {
+        RSX_LAUNCH(launch_assemble(assemble_args(h, a.n_items, 0), h->st), "assemble kernel");
+    } else {
+        RSX_TRY_CUDA(cudaMemsetAsync(h->d_iq64, 0, sizeof(double) * h->n_q, h->st), "clear");
+        RSX_LAUNCH(launch_assemble(assemble_args(h, a.n_items, 1), h->st), "assemble kernel");
+    }
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->h_iq64, h->d_iq64, sizeof(double) * h->n_q,
+                                 cudaMemcpyDeviceToHost, h->st),
+                 "read shard");
+    RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "calc shard");
+    std::memcpy(out_iq, h->h_iq64, sizeof(double) * h->n_q);
+    return ok();
+}
+
+rsx_status rsx_debug_shard_items(const rsx_body *bodies, int n_bodies, int n_factors,
+                                 int max_items, int n_shards, int *bounds, double *pairs)
+{
+    if ((!bodies && n_bodies > 0) || n_bodies < 0 || n_factors <= 0 || n_factors > kMaxTypes ||
+        max_items <= 0 || n_shards < 1 || !bounds)
+        return fail(RSX_INVALID_ARG, "bad shard arguments");
+    for (int i = 0; i < n_bodies; ++i)
+        if (type_of(bodies[i]) >= (unsigned)n_factors)
+            return fail(RSX_INVALID_ARG, "type out of range");
+    Layout L;
+    build_layout(L, bodies, n_bodies, n_factors, max_items, 1);
+    for (int sh = 0; sh < n_shards; ++sh) {
+        const auto r = shard_items(L, sh, n_shards);
+        bounds[sh] = r.first;
+        bounds[sh + 1] = r.second;
+        if (pairs) {
+            // unordered pairs of distinct bodies in the shard's items
+            double c = 0.0;
+            for (int i = r.first; i < r.second; ++i) {
+                const PairItem &it = L.items[i];
+                const double li = L.blocks[it.bi].len;
+                for (int b = it.bj_begin; b < it.bj_end; ++b)
+                    c += (b == it.bi) ? li * (li - 1) / 2 : li * L.blocks[b].len;
+            }
+            pairs[sh] = c;
+        }
+    }
+    return ok();
+}
+
 rsx_status rsx_debye_recalc_range(rsx_debye *h, const rsx_body *bodies, unsigned upd_start,
                                   unsigned upd_length, float *out_iq)
 {
@@ -826,6 +973,7 @@ rsx_status rsx_debye_revert(rsx_debye *h)
                                      cudaMemcpyHostToDevice, h->st),
                      "restore factors");
         h->cur = h->saved_bodies;
+        grow_extent(h, h->cur.data(), (unsigned)h->cur.size());
         RSX_TRY(upload_water(h));
         RSX_LAUNCH(launch_f64_to_f32(h->d_iq64, h->d_iq32, h->n_q, h->st), "curve f32");
         RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "revert");

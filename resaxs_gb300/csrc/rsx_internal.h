@@ -33,6 +33,7 @@ struct DebyeArgs {
     int n, n_q, n_types, n_items;
     int k_base;              // first q index of the launch (set by the launcher)
     float dq;                // uniform q step (rotation path)
+    int small_theta;         // 1: dq * (largest pair distance) <= 1.4, so |theta/2| < pi/4
     float water_weight;      // w (water path)
     int water_index;         // column of the water factor
     // adjoint
@@ -69,8 +70,11 @@ struct DeltaArgs {
     const float *ff, *q;
     double *partial;         // [n_q][n_blocks]
     int n, k, n_q, n_types, n_blocks, n_mtiles;
+    int max_groups;          // cap on the moved-list groups (partial holds n_blocks * groups rows)
     float dq;
 };
+
+constexpr int kDeltaGroups = 8; // moved-list groups of the wide delta kernel
 
 // launchers (debye_kernels.cu); all asynchronous on `st`
 // Slab plan of the wide uniform forward: `full` slabs of `main` q from q 0,
@@ -86,6 +90,9 @@ cudaError_t launch_forward(const DebyeArgs &a, int q_slab, bool uniform, bool wa
                            cudaStream_t st);
 cudaError_t launch_assemble(const AssembleArgs &a, cudaStream_t st);
 cudaError_t launch_delta(const DeltaArgs &a, int q_slab, bool uniform, cudaStream_t st);
+// partial sums per q that launch_delta writes (the assembly's n_parts)
+int delta_parts(const DeltaArgs &a, int q_slab, bool uniform);
+int delta_groups(const DeltaArgs &a);
 cudaError_t launch_apply_moves(float4 *pos, const float4 *moved_new, const int *moved_idx,
                                int k, cudaStream_t st);
 cudaError_t launch_mark_moved(int *slot, const int *moved_idx, int k, int set, cudaStream_t st);

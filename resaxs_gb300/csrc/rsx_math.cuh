@@ -97,6 +97,26 @@ __device__ __forceinline__ void sincos_rr2(float x, float x_lo, float &s, float 
     c = __uint_as_float(__float_as_uint(cv) ^ sgn_c);
 }
 
+// sincos_rr2 for |x| < pi/4, where the reduction step is the identity (n = 0):
+// the same operations without the reduction and quadrant logic, so the
+// results are bit-identical to sincos_rr2's on that range.
+__device__ __forceinline__ void sincos_small2(float x, float x_lo, float &s, float &c)
+{
+    const float r2 = x * x;
+    float ps = fmaf(r2, kS4, kS3);
+    ps = fmaf(r2, ps, kS2);
+    ps = fmaf(r2, ps, kS1);
+    float pc = fmaf(r2, kC5, kC4);
+    pc = fmaf(r2, pc, kC3);
+    pc = fmaf(r2, pc, kC2);
+    pc = fmaf(r2, pc, kC1);
+    const float r3 = x * r2;
+    const float sp = fmaf(r3, ps, x);
+    const float cp = fmaf(r2, pc, 1.0f);
+    s = x + fmaf(r3, ps, x_lo * cp);
+    c = 1.0f + fmaf(r2, pc, -x_lo * sp);
+}
+
 __device__ __forceinline__ void sincos_rr(float x, float &s, float &c) { sincos_rr2(x, 0.0f, s, c); }
 
 // sin and cos of the product a*b, its rounding error folded in exactly.

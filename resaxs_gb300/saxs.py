@@ -104,6 +104,15 @@ class Debye:
         check(lib().rsx_debye_calc(self._h, bodies.reshape(-1), out))
         return out
 
+    def calc_shard(self, bodies, shard: int, n_shards: int) -> np.ndarray:
+        """This shard's additive FP64 contribution to I(q) (rsx_debye_calc_shard);
+        the sum over shards 0..n_shards-1 is the full curve."""
+        bodies = _f32(bodies)
+        out = np.zeros(self.n_q, np.float64)
+        check(lib().rsx_debye_calc_shard(self._h, bodies.reshape(-1), int(shard), int(n_shards),
+                                         out))
+        return out
+
     def recalc_range(self, bodies, start: int, length: int) -> np.ndarray:
         bodies = _f32(bodies)
         out = np.zeros(self.n_q, np.float32)

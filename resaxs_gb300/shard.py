@@ -1,5 +1,11 @@
-"""Ensembles over several GPUs: one process per GPU, members sharded across
-ranks, no collective on the data path.
+"""Work over several GPUs: one process per GPU, no collective on the data
+path, one all-reduce of n_q doubles at the end.
+
+* Ensembles: members sharded across ranks (below).
+* One structure: ``Debye.calc_shard(bodies, rank, world)`` computes a
+  contiguous run of the forward work items (balanced by pair count) and
+  returns its additive FP64 contribution to I(q); ``combine_shards`` sums
+  the contributions over ranks.
 
 Members of an ensemble are independent structures, so each rank runs its own
 share through one ``DebyeBatch`` (one graph-captured persistent pass) and the
@@ -62,3 +68,19 @@ def ensemble_average(local_sum: np.ndarray, local_count: int, group=None) -> np.
     dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
     t = t.cpu().numpy()
     return t[:-1] / max(t[-1], 1.0)
+
+
+def combine_shards(local_contrib: np.ndarray, group=None) -> np.ndarray:
+    """I(q) of one structure from each rank's ``Debye.calc_shard`` output:
+    their sum (one all-reduce of n_q doubles).  Without an initialised
+    process group it returns the local contribution."""
+    import torch
+    import torch.distributed as dist
+
+    local_contrib = np.asarray(local_contrib, np.float64)
+    if not (dist.is_available() and dist.is_initialized()):
+        return local_contrib
+    dev = "cuda" if dist.get_backend(group) == "nccl" else "cpu"
+    t = torch.from_numpy(local_contrib.copy()).to(dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+    return t.cpu().numpy()

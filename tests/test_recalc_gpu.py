@@ -21,21 +21,27 @@ def S():
     return saxs
 
 
-def test_recalc_indices_matches_full_recompute(S, oracle_lib):
+@pytest.mark.parametrize("q_slab,n_q", [(0, 201), (32, 201), (16, 201), (128, 101),
+                                         (128, 256), (64, 150), (64, 40)])
+def test_recalc_indices_matches_full_recompute(S, oracle_lib, q_slab, n_q):
     """Config-2 style moves (k random bodies, Gaussian sigma 0.5 A) at a size the
-    oracle recomputes quickly; every step is checked."""
+    oracle recomputes quickly; every step is checked.  The slab sizes and q
+    counts cover the wide delta slabs (64-q main slabs, every tail shape) and
+    the 16 / 32-q kernel."""
     w = W.make_config(2, seed=21, n_override=1200)
+    q = W.q_grid(n_q, 0.5)
+    ff = W.exp_form_factors(q, W.Z5, np.random.default_rng(n_q).uniform(0.5, 2.0, 5))
     rng = np.random.default_rng(1)
     bodies = w.bodies.copy()
-    with S.Debye(w.q, w.ff, w.n) as d:
+    with S.Debye(q, ff, w.n, q_slab=q_slab) as d:
         d.calc(bodies)
-        for step in range(6):
+        for step in range(4):
             idx = rng.choice(w.n, size=50, replace=False).astype(np.uint32)
             moved = bodies[idx].copy()
             moved[:, :3] += rng.normal(0, 0.5, (50, 3)).astype(np.float32)
             out = d.recalc_indices(moved, idx)
             bodies[idx] = moved
-            ref = oracle_lib.debye_f64(w.q, bodies, w.ff)
+            ref = oracle_lib.debye_f64(q, bodies, ff)
             assert rel(d.curve_f64(), ref) < TOL, step
             assert rel(out, ref) < TOL
 
