@@ -17,7 +17,7 @@
 namespace rsx {
 
 template <int QS, bool UNIFORM>
-__global__ void __launch_bounds__(kBlockAtoms, QS >= 64 ? 3 : 1)
+__global__ void __launch_bounds__(kBlockAtoms)
     batch_forward_kernel(const DebyeArgs a, const int *work_order, int n_units, int n_slabs,
                          int k_base, int *counter)
 {
@@ -160,12 +160,7 @@ cudaError_t launch_batch_forward(const DebyeArgs &a, const int *work_order, int 
         RSX_BF(16);
     case 32:
         RSX_BF(32);
-    case 64:
-        if (!uniform)
-            return cudaErrorInvalidValue;
-        return fwd_launch<64, true>(a, work_order, n_work_items, n_slabs, k_base, counter, grid,
-                                    st);
-    default:
+    default: // 64 and wider: launch_batch_forward_wide
         return cudaErrorInvalidValue;
     }
 #undef RSX_BF

@@ -31,7 +31,7 @@ void count_launch(int n) { g_launches += (unsigned long long)n; }
 unsigned long long launch_count() { return g_launches.load(); }
 
 template <int QS, bool UNIFORM, bool WATER>
-__global__ void __launch_bounds__(kBlockAtoms, QS >= 64 ? 3 : 1) forward_kernel(const DebyeArgs a)
+__global__ void __launch_bounds__(kBlockAtoms) forward_kernel(const DebyeArgs a)
 {
     forward_item<QS, UNIFORM, WATER>(a, blockIdx.x, a.k_base + blockIdx.y * QS);
 }
@@ -363,10 +363,7 @@ static cudaError_t forward_dispatch(const DebyeArgs &a, int qs, int k_base, int 
         return forward_qs<16>(a, k_base, n_slabs, uniform, water, st);
     case 32:
         return forward_qs<32>(a, k_base, n_slabs, uniform, water, st);
-    case 64: // uniform grid without water only (register budget)
-        return (uniform && !water) ? forward_launch<64, true, false>(a, k_base, n_slabs, st)
-                                   : cudaErrorInvalidValue;
-    default:
+    default: // 64 and wider: the wide kernels (launch_forward_wide)
         return cudaErrorInvalidValue;
     }
 }

@@ -60,6 +60,19 @@ def test_wide_slab_tails(saxs, oracle_lib, q_slab, n_q):
     assert rel(out64, oracle_lib.debye_f64(q, w.bodies, ff)) < TOL
 
 
+def test_seed_paths_both_sides_of_the_small_theta_bound(saxs, oracle_lib):
+    """A compact structure lets every seed skip the range reduction of
+    theta/2 (dq * extent <= 1.4); moving two bodies 900 A away switches that
+    off for the whole launch.  Both must match the oracle, and the compact
+    structure's pairs must give the same sums either way."""
+    w = W.make_config(2, seed=31, n_override=900)
+    far = w.bodies.copy()
+    far[:2, 0] += np.float32(900.0)
+    for bodies in (w.bodies, far):
+        _, out64, _ = gpu_curve(saxs, w.q, w.ff, bodies)
+        assert rel(out64, oracle_lib.debye_f64(w.q, bodies, w.ff)) < TOL
+
+
 def test_forward_general_q_path(saxs, oracle_lib):
     w = W.make_config(2, seed=13, n_override=800)
     rng = np.random.default_rng(3)
