@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(kBlockAtoms)
 }
 
 // Wide uniform slabs (no water), as forward_wide_kernel.
-template <int QS, int IL>
+template <int QS, int IL, bool SIGNED = true>
 __global__ void __launch_bounds__(kBlockAtoms, QS <= 64 ? 3 : 2)
     batch_wide_kernel(const DebyeArgs a, const int *work_order, int n_units, int n_slabs,
                       int k_base, int *counter)
@@ -51,11 +51,11 @@ __global__ void __launch_bounds__(kBlockAtoms, QS <= 64 ? 3 : 2)
         if (w >= n_units)
             break;
         const int item = work_order[w / n_slabs];
-        forward_wide_item<QS, IL>(a, item, k_base + (w % n_slabs) * QS);
+        forward_wide_item<QS, IL, SIGNED>(a, item, k_base + (w % n_slabs) * QS);
     }
 }
 
-template <int QS, bool UNIFORM>
+template <int QS, bool UNIFORM, bool SMALL = false>
 __global__ void __launch_bounds__(kBlockAtoms)
     batch_adjoint_kernel(const DebyeArgs a, const int *work_order, int n_units, int n_slabs,
                          int *counter)
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(kBlockAtoms)
         __syncthreads();
         if (w >= n_units)
             break;
-        adjoint_item<QS, UNIFORM, false>(a, work_order[w], n_slabs);
+        adjoint_item<QS, UNIFORM, false, SMALL>(a, work_order[w], n_slabs);
     }
 }
 
@@ -174,7 +174,7 @@ static cudaError_t wide_batch_launch(const DebyeArgs &a, const int *order, int n
                                      int n_slabs, int k_base, int *counter, int sms,
                                      cudaStream_t st)
 {
-    auto kfn = batch_wide_kernel<QS, IL>;
+    auto kfn = a.small_theta ? batch_wide_kernel<QS, IL, false> : batch_wide_kernel<QS, IL, true>;
     const int grid = std::min(occupancy_grid(kfn, 0, sms), n_items * n_slabs);
     kfn<<<grid, kBlockAtoms, 0, st>>>(a, order, n_items * n_slabs, n_slabs, k_base, counter);
     count_launch();
@@ -190,10 +190,12 @@ cudaError_t launch_batch_forward_wide(const DebyeArgs &a, const int *work_order,
     const WidePlan p = wide_plan(a.n_q, q_slab);
     if (p.full > 0) {
         cudaError_t e;
-        e = p.main == 64 ? wide_batch_launch<64, 2>(a, work_order, n_work_items, p.full, 0,
-                                                    counters, sms, st)
-                         : wide_batch_launch<112, 4>(a, work_order, n_work_items, p.full, 0,
-                                                     counters, sms, st);
+        e = p.main == 64    ? wide_batch_launch<64, 2>(a, work_order, n_work_items, p.full, 0,
+                                                       counters, sms, st)
+            : p.main == 112 ? wide_batch_launch<112, 4>(a, work_order, n_work_items, p.full, 0,
+                                                        counters, sms, st)
+                            : wide_batch_launch<128, 4>(a, work_order, n_work_items, p.full, 0,
+                                                        counters, sms, st);
         if (e != cudaSuccess)
             return e;
     }
@@ -214,8 +216,10 @@ cudaError_t launch_batch_forward_wide(const DebyeArgs &a, const int *work_order,
         RSX_BW(80);
     case 6:
         RSX_BW(96);
-    default:
+    case 7:
         RSX_BW(112);
+    default:
+        RSX_BW(128);
     }
 #undef RSX_BW
 }
@@ -226,7 +230,7 @@ static cudaError_t adj_launch(const DebyeArgs &a, const int *order, int n_items,
 {
     const int n_slabs = (a.n_q + QS - 1) / QS;
     const size_t smem = adjoint_smem_bytes(a.n_q, QS, U, false);
-    auto kfn = batch_adjoint_kernel<QS, U>;
+    auto kfn = (U && a.small_theta) ? batch_adjoint_kernel<QS, U, true> : batch_adjoint_kernel<QS, U, false>;
     if (smem > 48 * 1024) {
         cudaError_t e =
             cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -183,14 +183,6 @@ struct WideSlab {
     static constexpr int NR = QP / 32;             // q values per lane after the scatter
 };
 
-// Compact seed of the wide path: Reinsch form (s, d, lam) when cos(theta) >= 0,
-// rotation form (s, c, sin theta, cos theta) otherwise; 4 registers per pair
-// either way.
-struct WideSeed {
-    float s, d, l, cd; // Reinsch: s, d, lam; rotation: s, c, sin(theta), cos(theta)
-    bool big;
-};
-
 // sin/cos(q0 r) (exactly 0 and 1 when q0 = 0, as sincos_prod gives) and
 // sin/cos(theta/2); `small_theta` (uniform over the launch) promises
 // |theta/2| < pi/4, where the reduction is the identity (sincos_small2 gives
@@ -212,48 +204,55 @@ __device__ __forceinline__ void seed_angles(float q0, float dq, float r, bool sm
         sincos_rr2(0.5f * th, 0.5f * th_lo, sh, ch);
 }
 
+// Seed of the wide path: Reinsch's recurrence on a folded angle, branch-free
+// for every theta.  The step angle theta = dq r enters the recurrence only
+// through lam, so any theta is equivalent to its value mod 2 pi; where
+// cos^2(theta/2) < sin^2(theta/2) (theta mod 2 pi in (pi/2, 3 pi/2), where the
+// form loses accuracy as theta -> pi) the recurrence runs instead on
+//     t_k = (-1)^k s_k = sin(x0 + k (theta - pi)),
+// whose angle theta - pi lies in (-pi/2, pi/2):
+//     lam = -4 cos^2(theta/2),  d_0 = t_0 - t_{-1} = 2 cos(theta/2) sin(x0 - theta/2),
+// and the odd steps are accumulated with the sign sg = -1.  So every pair
+// steps an angle of magnitude <= pi/2 with the same three operations, and no
+// warp diverges on far-apart pairs.
+struct WideSeed {
+    float s, d, l, sg; // t_0 / r, d_0 / r, lam, sign of the odd steps (+1 or -1)
+};
+
 __device__ __forceinline__ WideSeed wide_seed(float q0, float dq, float r, float sc,
                                               bool small_theta = false)
 {
     WideSeed p;
     float s0, c0, sh, ch;
     seed_angles(q0, dq, r, small_theta, s0, c0, sh, ch);
-    p.big = ch * ch < sh * sh;
     p.s = s0 * sc;
-    if (!p.big) {
+    if (ch * ch >= sh * sh) {
         p.l = -4.0f * sh * sh;
         p.d = 2.0f * sh * fmaf(c0, ch, s0 * sh) * sc;
-        p.cd = 0.f;
+        p.sg = 1.0f;
     } else {
-        p.d = c0 * sc;
-        p.l = 2.0f * sh * ch;
-        p.cd = fmaf(-2.0f * sh, sh, 1.0f);
+        p.l = -4.0f * ch * ch;
+        p.d = 2.0f * ch * fmaf(s0, ch, -c0 * sh) * sc;
+        p.sg = -1.0f;
     }
     return p;
 }
 
-// One recurrence step of a wide seed in either form.
-__device__ __forceinline__ void wide_step(const WideSeed &p, float &s, float &d)
-{
-    if (p.big) {
-        const float sn = fmaf(d, p.l, s * p.cd);
-        d = fmaf(-s, p.l, d * p.cd);
-        s = sn;
-    } else {
-        d = fmaf(p.l, s, d);
-        s += d;
-    }
-}
-
-// Two pairs on the Reinsch form, interleaved for ILP (the hot loop: 3 FP32
-// lane-ops per pair*q).
-template <int QS, int QP>
-__device__ __forceinline__ void wide_pair2(const WideSeed &a, const WideSeed &b, float (&S)[QP])
+// Two pairs, interleaved for ILP (the hot loop: 3 FP32 lane-ops per pair*q).
+// SIGNED adds the odd steps with the pairs' signs (FMAs); warps whose pairs
+// all have sign +1 (compact structures: all of them) take the plain adds,
+// which the FMA chain would slow by ~9 %.
+template <int QS, int QP, bool SIGNED>
+__device__ __forceinline__ void wide_pair2_body(const WideSeed &a, const WideSeed &b,
+                                                float (&S)[QP])
 {
     float sa = a.s, da = a.d, sb = b.s, db = b.d;
 #pragma unroll
     for (int k = 0; k < QS; ++k) {
-        S[k] += sa + sb;
+        if (SIGNED && (k & 1))
+            S[k] = fmaf(a.sg, sa, fmaf(b.sg, sb, S[k]));
+        else
+            S[k] += sa + sb;
         da = fmaf(a.l, sa, da);
         db = fmaf(b.l, sb, db);
         sa += da;
@@ -261,16 +260,28 @@ __device__ __forceinline__ void wide_pair2(const WideSeed &a, const WideSeed &b,
     }
 }
 
-// Four pairs on the Reinsch form: more independent chains per warp for when
-// few warps fit on an SM.
 template <int QS, int QP>
-__device__ __forceinline__ void wide_pair4(const WideSeed &a, const WideSeed &b, const WideSeed &c,
-                                           const WideSeed &e, float (&S)[QP])
+__device__ __forceinline__ void wide_pair2(const WideSeed &a, const WideSeed &b, float (&S)[QP])
+{
+    if (__any_sync(0xffffffffu, a.sg < 0.f || b.sg < 0.f))
+        wide_pair2_body<QS, QP, true>(a, b, S);
+    else
+        wide_pair2_body<QS, QP, false>(a, b, S);
+}
+
+// Four pairs: more independent chains per warp for when few warps fit on an SM.
+template <int QS, int QP, bool SIGNED>
+__device__ __forceinline__ void wide_pair4_body(const WideSeed &a, const WideSeed &b,
+                                                const WideSeed &c, const WideSeed &e,
+                                                float (&S)[QP])
 {
     float sa = a.s, da = a.d, sb = b.s, db = b.d, sc = c.s, dc = c.d, se = e.s, de = e.d;
 #pragma unroll
     for (int k = 0; k < QS; ++k) {
-        S[k] += (sa + sb) + (sc + se);
+        if (SIGNED && (k & 1))
+            S[k] = fmaf(a.sg, sa, fmaf(b.sg, sb, fmaf(c.sg, sc, fmaf(e.sg, se, S[k]))));
+        else
+            S[k] += (sa + sb) + (sc + se);
         da = fmaf(a.l, sa, da);
         db = fmaf(b.l, sb, db);
         dc = fmaf(c.l, sc, dc);
@@ -282,18 +293,14 @@ __device__ __forceinline__ void wide_pair4(const WideSeed &a, const WideSeed &b,
     }
 }
 
-// Two pairs when either needs the rotation form (cos(theta) < 0: far-apart
-// bodies on coarse grids; rare).
 template <int QS, int QP>
-__device__ __forceinline__ void wide_mixed2(const WideSeed &a, const WideSeed &b, float (&S)[QP])
+__device__ __forceinline__ void wide_pair4(const WideSeed &a, const WideSeed &b, const WideSeed &c,
+                                           const WideSeed &e, float (&S)[QP])
 {
-    float sa = a.s, da = a.d, sb = b.s, db = b.d;
-#pragma unroll
-    for (int k = 0; k < QS; ++k) {
-        S[k] += sa + sb;
-        wide_step(a, sa, da);
-        wide_step(b, sb, db);
-    }
+    if (__any_sync(0xffffffffu, a.sg < 0.f || b.sg < 0.f || c.sg < 0.f || e.sg < 0.f))
+        wide_pair4_body<QS, QP, true>(a, b, c, e, S);
+    else
+        wide_pair4_body<QS, QP, false>(a, b, c, e, S);
 }
 
 template <int QS, int QP>
@@ -302,14 +309,18 @@ __device__ __forceinline__ void wide_pair1(const WideSeed &p, float (&S)[QP])
     float s = p.s, d = p.d;
 #pragma unroll
     for (int k = 0; k < QS; ++k) {
-        S[k] += s;
-        wide_step(p, s, d);
+        S[k] = (k & 1) ? fmaf(p.sg, s, S[k]) : S[k] + s;
+        d = fmaf(p.l, s, d);
+        s += d;
     }
 }
 
 // Forward pair sums of one work item for q values [k0, k0 + QS) on a uniform
 // grid without water; writes partial[k][item_idx] as forward_item does.
-template <int QS, int IL>
+// SIGNED = false: the launch promises small theta (every pair has
+// |theta/2| < pi/4, so every sign is +1), and the pair loop keeps only the
+// plain adds.
+template <int QS, int IL, bool SIGNED = true>
 __device__ __forceinline__ void forward_wide_item(const DebyeArgs &a, int item_idx, int k0)
 {
     constexpr int QP = WideSlab<QS>::QP, NR = WideSlab<QS>::NR;
@@ -326,7 +337,7 @@ __device__ __forceinline__ void forward_wide_item(const DebyeArgs &a, int item_i
     const float4 pi = valid_i ? a.pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float q0 = a.q[k0];
     const float dq = a.dq;
-    const bool small_th = a.small_theta != 0;
+    const bool small_th = !SIGNED || a.small_theta != 0;
 
     double acc[NR];
 #pragma unroll
@@ -355,12 +366,10 @@ __device__ __forceinline__ void forward_wide_item(const DebyeArgs &a, int item_i
                     const bool use = valid_i && (!diag || jj + u > tid);
                     p[u] = wide_seed(q0, dq, r, use ? ri : 0.f, small_th);
                 }
-                if (!(p[0].big || p[1].big || p[2].big || p[3].big)) {
+                if constexpr (SIGNED)
                     wide_pair4<QS, QP>(p[0], p[1], p[2], p[3], S);
-                } else {
-                    wide_mixed2<QS, QP>(p[0], p[1], S);
-                    wide_mixed2<QS, QP>(p[2], p[3], S);
-                }
+                else
+                    wide_pair4_body<QS, QP, false>(p[0], p[1], p[2], p[3], S);
             }
         }
         for (; jj + 1 < bj.len; jj += 2) {
@@ -371,10 +380,10 @@ __device__ __forceinline__ void forward_wide_item(const DebyeArgs &a, int item_i
             const bool u2 = valid_i && (!diag || jj + 1 > tid);
             const WideSeed p1 = wide_seed(q0, dq, r1, u1 ? ri1 : 0.f, small_th);
             const WideSeed p2 = wide_seed(q0, dq, r2, u2 ? ri2 : 0.f, small_th);
-            if (!p1.big && !p2.big)
+            if constexpr (SIGNED)
                 wide_pair2<QS, QP>(p1, p2, S);
             else
-                wide_mixed2<QS, QP>(p1, p2, S);
+                wide_pair2_body<QS, QP, false>(p1, p2, S);
         }
         if (jj < bj.len) {
             float r, rinv, dx, dy, dz;
@@ -582,8 +591,8 @@ __device__ __forceinline__ void forward_item(const DebyeArgs &a, int item_idx, i
 // Pairs with theta > pi/2 (cos(theta/2)^2 < 1/2, far-apart bodies on coarse
 // grids) take the rotation form with alpha directly.
 
-constexpr int kAdjSlab = 128;   // q values between reseeds
-constexpr int kAdjStride = 129; // table entries per slab (delta has L + 1)
+constexpr int kAdjSlab = 256;   // q values between reseeds
+constexpr int kAdjStride = 257; // table entries per slab (delta has L + 1)
 
 // Table entry m of slab sl: (delta_m, beta_m, alpha_m, 0).
 __device__ __forceinline__ void adjoint_uniform_table(const DebyeArgs &a, float4 *tab, int n_slabs,
@@ -711,15 +720,20 @@ struct AdjPair {
     bool circle;  // magic-circle form (theta <= pi/2)
 };
 
-// (The reduction-free sincos of small theta is not used here: its branch
-// costs this kernel 8 registers and a CTA per SM, more than it saves.)
+// SMALL: the launch promises |theta/2| < pi/4 for every pair, so the
+// reduction-free sincos applies (a template choice: as a runtime branch it
+// cost this kernel 8 registers and a CTA per SM).
+template <bool SMALL>
 __device__ __forceinline__ AdjPair adj_pair(const float4 &pi, const float4 &pj, float dq)
 {
     AdjPair p;
     pair_r(pi, pj, p.r, p.rinv, p.dx, p.dy, p.dz);
     const float th = dq * p.r;
     const float th_lo = fmaf(dq, p.r, -th);
-    sincos_rr2(0.5f * th, 0.5f * th_lo, p.sh, p.ch);
+    if constexpr (SMALL)
+        sincos_small2(0.5f * th, 0.5f * th_lo, p.sh, p.ch);
+    else
+        sincos_rr2(0.5f * th, 0.5f * th_lo, p.sh, p.ch);
     p.circle = 2.0f * p.ch * p.ch >= 1.0f;
     return p;
 }
@@ -844,7 +858,7 @@ __host__ __device__ inline size_t adjoint_smem_bytes(int n_q, int qs, bool unifo
 
 // IL pairs per thread step together (4: measured 18 % faster than 2 at
 // N = 50,000, 256 q; 71 registers).
-template <int IL>
+template <int IL, bool SMALL>
 __device__ __forceinline__ void adjoint_uniform_item(const DebyeArgs &a, int item_idx)
 {
     extern __shared__ float4 s_dyn[];
@@ -884,7 +898,7 @@ __device__ __forceinline__ void adjoint_uniform_item(const DebyeArgs &a, int ite
                 AdjPair p[4];
 #pragma unroll
                 for (int v = 0; v < 4; ++v)
-                    p[v] = adj_pair(pi, s_pos[jj + v], dq);
+                    p[v] = adj_pair<SMALL>(pi, s_pos[jj + v], dq);
                 float A[4], B[4];
                 if (p[0].circle && p[1].circle && p[2].circle && p[3].circle) {
                     adj_pair4_sums(a, tab, n_slabs, p, A, B);
@@ -900,8 +914,8 @@ __device__ __forceinline__ void adjoint_uniform_item(const DebyeArgs &a, int ite
             }
         }
         for (; jj + 1 < bj.len; jj += 2) {
-            const AdjPair p1 = adj_pair(pi, s_pos[jj], dq);
-            const AdjPair p2 = adj_pair(pi, s_pos[jj + 1], dq);
+            const AdjPair p1 = adj_pair<SMALL>(pi, s_pos[jj], dq);
+            const AdjPair p2 = adj_pair<SMALL>(pi, s_pos[jj + 1], dq);
             float A1, B1, A2, B2;
             if (p1.circle && p2.circle) {
                 adj_pair2_sums(a, tab, n_slabs, p1, p2, A1, B1, A2, B2);
@@ -914,7 +928,7 @@ __device__ __forceinline__ void adjoint_uniform_item(const DebyeArgs &a, int ite
                         jj + 1, lane);
         }
         for (; jj < bj.len; ++jj) {
-            const AdjPair p = adj_pair(pi, s_pos[jj], dq);
+            const AdjPair p = adj_pair<SMALL>(pi, s_pos[jj], dq);
             float A, B;
             adj_pair_sums(a, tab, n_slabs, p, A, B);
             adj_scatter(p, A, B, valid_i && (!diag || jj > tid), gi0, gi1, gi2, s_gj, jj, lane);
@@ -1097,11 +1111,11 @@ __device__ __forceinline__ void adjoint_general_item(const DebyeArgs &a, int ite
     }
 }
 
-template <int QS, bool UNIFORM, bool WATER>
+template <int QS, bool UNIFORM, bool WATER, bool SMALL = false>
 __device__ __forceinline__ void adjoint_item(const DebyeArgs &a, int item_idx, int n_slabs)
 {
     if constexpr (UNIFORM && !WATER)
-        adjoint_uniform_item<4>(a, item_idx);
+        adjoint_uniform_item<4, SMALL>(a, item_idx);
     else
         adjoint_general_item<QS, UNIFORM, WATER>(a, item_idx, n_slabs);
 }

@@ -37,10 +37,10 @@ __global__ void __launch_bounds__(kBlockAtoms) forward_kernel(const DebyeArgs a)
 }
 
 // up to 64 q: <= 168 registers, 3 CTAs per SM; wider: <= 255, 2 CTAs per SM
-template <int QS, int IL>
+template <int QS, int IL, bool SIGNED>
 __global__ void __launch_bounds__(kBlockAtoms, QS <= 64 ? 3 : 2) forward_wide_kernel(const DebyeArgs a)
 {
-    forward_wide_item<QS, IL>(a, blockIdx.x, a.k_base + blockIdx.y * QS);
+    forward_wide_item<QS, IL, SIGNED>(a, blockIdx.x, a.k_base + blockIdx.y * QS);
 }
 
 // ----------------------------------------------------------------------------
@@ -271,10 +271,7 @@ __global__ void __launch_bounds__(kBlockAtoms, QS <= 64 ? 3 : 2) delta_wide_kern
             pair_r(py_old, s_old[jj], ro, roinv, dx, dy, dz);
             const WideSeed pn = wide_seed(q0, dq, rn, use ? mult * rninv : 0.f);
             const WideSeed po = wide_seed(q0, dq, ro, use ? -mult * roinv : 0.f);
-            if (!pn.big && !po.big)
-                wide_pair2<QS, QP>(pn, po, S);
-            else
-                wide_mixed2<QS, QP>(pn, po, S);
+            wide_pair2<QS, QP>(pn, po, S);
         }
 #pragma unroll
         for (int c = 0; c < NR; ++c) {
@@ -320,10 +317,10 @@ __global__ void f64_to_f32_kernel(const double *src, float *dst, int n)
 // a pair is complete before it is scattered.
 // ----------------------------------------------------------------------------
 
-template <int QS, bool UNIFORM, bool WATER>
+template <int QS, bool UNIFORM, bool WATER, bool SMALL = false>
 __global__ void __launch_bounds__(kBlockAtoms) adjoint_kernel(const DebyeArgs a, int n_slabs)
 {
-    adjoint_item<QS, UNIFORM, WATER>(a, blockIdx.x, n_slabs);
+    adjoint_item<QS, UNIFORM, WATER, SMALL>(a, blockIdx.x, n_slabs);
 }
 
 // ----------------------------------------------------------------------------
@@ -373,7 +370,10 @@ static cudaError_t wide_launch(DebyeArgs a, int k_base, int n_slabs, cudaStream_
 {
     a.k_base = k_base;
     const dim3 grid(a.n_items, n_slabs);
-    forward_wide_kernel<QS, IL><<<grid, kBlockAtoms, 0, st>>>(a);
+    if (a.small_theta)
+        forward_wide_kernel<QS, IL, false><<<grid, kBlockAtoms, 0, st>>>(a);
+    else
+        forward_wide_kernel<QS, IL, true><<<grid, kBlockAtoms, 0, st>>>(a);
     count_launch();
     return cudaGetLastError();
 }
@@ -393,17 +393,21 @@ static cudaError_t wide_tail(const DebyeArgs &a, int k0, int len, cudaStream_t s
         return wide_launch<80>(a, k0, 1, st);
     case 6:
         return wide_launch<96>(a, k0, 1, st);
-    default:
+    case 7:
         return wide_launch<112>(a, k0, 1, st);
+    default:
+        return wide_launch<128>(a, k0, 1, st);
     }
 }
 
 // Relative cost of one slab per pair on GB300 (CUDA-event times of the
-// wide kernels at N = 20,000 and 50,000, in units of ~10 ns per 1e6 pairs):
-// full slabs of 64 q (2 pairs interleaved, 3 CTAs/SM) and of 112 q (4 pairs
-// interleaved, 2 CTAs/SM), and a single tail slab of 16..112 q.
-static constexpr float kCostMain64 = 1.88f, kCostMain112 = 3.30f;
-static constexpr float kCostTail[7] = {1.10f, 1.40f, 1.65f, 1.88f, 2.81f, 2.80f, 3.40f};
+// wide kernels at N = 20,000 / 50,000 / 100,000 on compact structures, in ms
+// per 2e8 pairs): full slabs of 64 q (2 pairs interleaved, 3 CTAs/SM), of
+// 112 and 128 q (4 pairs interleaved, 2 CTAs/SM), and a single tail slab of
+// 16..128 q.  The seed of a slab costs about as much as 40 steps, so short
+// tails are dear per q.
+static constexpr float kCostMain64 = 1.885f, kCostMain112 = 2.92f, kCostMain128 = 3.16f;
+static constexpr float kCostTail[8] = {1.10f, 1.15f, 1.50f, 1.885f, 2.60f, 2.79f, 2.92f, 3.16f};
 
 static float tail_cost(int len) { return len > 0 ? kCostTail[(len + 15) / 16 - 1] : 0.f; }
 
@@ -416,7 +420,7 @@ WidePlan wide_plan(int n_q, int q_slab)
     auto consider = [&](int main, int full, int rest, float cost) {
         if (cost < best_cost) {
             best_cost = cost;
-            best = WidePlan{main, full, full * main, rest, main == 112 ? 4 : 2};
+            best = WidePlan{main, full, full * main, rest, main >= 112 ? 4 : 2};
         }
     };
     const int f64 = n_q / 64, r64 = n_q - 64 * f64;
@@ -426,6 +430,8 @@ WidePlan wide_plan(int n_q, int q_slab)
     if (q_slab >= 128) {
         const int f112 = n_q / 112, r112 = n_q - 112 * f112;
         consider(112, f112, r112, f112 * kCostMain112 + tail_cost(r112));
+        const int f128 = n_q / 128, r128 = n_q - 128 * f128;
+        consider(128, f128, r128, f128 * kCostMain128 + tail_cost(r128));
     }
     return best;
 }
@@ -437,8 +443,9 @@ static cudaError_t launch_forward_wide(const DebyeArgs &a, int q_slab, cudaStrea
     const WidePlan p = wide_plan(a.n_q, q_slab);
     if (p.full > 0) {
         cudaError_t e;
-        e = p.main == 64 ? wide_launch<64, 2>(a, 0, p.full, st)
-                         : wide_launch<112, 4>(a, 0, p.full, st);
+        e = p.main == 64    ? wide_launch<64, 2>(a, 0, p.full, st)
+            : p.main == 112 ? wide_launch<112, 4>(a, 0, p.full, st)
+                            : wide_launch<128, 4>(a, 0, p.full, st);
         if (e != cudaSuccess)
             return e;
     }
@@ -596,6 +603,15 @@ static cudaError_t adjoint_qs(const DebyeArgs &a, bool uniform, bool water, cuda
     const size_t smem = adjoint_smem_bytes(a.n_q, QS, uniform, water);
     const dim3 grid(a.n_items);
     cudaError_t e = cudaSuccess;
+#define RSX_ADJ_SMALL()                                                                    \
+    do {                                                                                   \
+        auto kfn = adjoint_kernel<QS, true, false, true>;                                  \
+        if (smem > 48 * 1024)                                                              \
+            e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,     \
+                                     (int)smem);                                           \
+        if (e == cudaSuccess)                                                              \
+            kfn<<<grid, kBlockAtoms, smem, st>>>(a, n_slabs);                              \
+    } while (0)
 #define RSX_ADJ(U, W)                                                                      \
     do {                                                                                   \
         auto kfn = adjoint_kernel<QS, U, W>;                                               \
@@ -605,7 +621,9 @@ static cudaError_t adjoint_qs(const DebyeArgs &a, bool uniform, bool water, cuda
         if (e == cudaSuccess)                                                              \
             kfn<<<grid, kBlockAtoms, smem, st>>>(a, n_slabs);                              \
     } while (0)
-    if (uniform && !water)
+    if (uniform && !water && a.small_theta)
+        RSX_ADJ_SMALL();
+    else if (uniform && !water)
         RSX_ADJ(true, false);
     else if (uniform && water)
         RSX_ADJ(true, true);
@@ -614,6 +632,7 @@ static cudaError_t adjoint_qs(const DebyeArgs &a, bool uniform, bool water, cuda
     else
         RSX_ADJ(false, true);
 #undef RSX_ADJ
+#undef RSX_ADJ_SMALL
     if (e != cudaSuccess)
         return e;
     count_launch();

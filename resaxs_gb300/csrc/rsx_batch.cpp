@@ -35,6 +35,7 @@ struct rsx_batch {
     std::vector<int> sizes, offsets; // caller layout of the concatenated bodies
     bool uniform = false;
     float dq = 0.f;
+    int small_theta = 0; // flag the captured graphs were built with
     int q_slab = 64;
     bool autotune = false, tuned = false;
 
@@ -264,6 +265,7 @@ DebyeArgs batch_args(rsx_batch *h, bool adjoint)
     a.n_types = h->n_types;
     a.n_items = (int)(adjoint ? h->adj_items.size() : h->items.size());
     a.dq = h->dq;
+    a.small_theta = h->small_theta;
     a.lambda = h->d_lambda;
     a.grad = h->d_grad;
     return a;
@@ -381,6 +383,35 @@ rsx_status stage_bodies(rsx_batch *h, const rsx_body *bodies)
     for (int s = 0; s < h->n_total; ++s) {
         const rsx_body &b = bodies[h->perm[s]];
         h->h_pos[s] = make_float4(b.x, b.y, b.z, b.w);
+    }
+    // 1 when every member's pairs have |theta/2| = |dq r / 2| <= 0.7 < pi/4:
+    // the seeds may skip the range reduction (same results bit for bit).  The
+    // flag is a kernel argument of the captured graphs, so they are captured
+    // again when it changes.
+    double worst = 0.0;
+    for (int m = 0; m < h->n_members; ++m) {
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (int i = h->offsets[m]; i < h->offsets[m] + h->sizes[m]; ++i) {
+            const double x[3] = {bodies[i].x, bodies[i].y, bodies[i].z};
+            for (int d = 0; d < 3; ++d) {
+                lo[d] = std::min(lo[d], x[d]);
+                hi[d] = std::max(hi[d], x[d]);
+            }
+        }
+        if (h->sizes[m] > 1) {
+            double d2 = 0.0;
+            for (int d = 0; d < 3; ++d)
+                d2 += (hi[d] - lo[d]) * (hi[d] - lo[d]);
+            worst = std::max(worst, std::sqrt(d2));
+        }
+    }
+    const int small = (h->uniform && std::isfinite(worst) &&
+                       std::fabs((double)h->dq) * worst * 1.0001 <= 1.4)
+                          ? 1
+                          : 0;
+    if (small != h->small_theta) {
+        drop_graphs(h);
+        h->small_theta = small;
     }
     return RSX_OK;
 }

@@ -14,8 +14,16 @@
 //
 // Mapping: one CTA of 128 threads per atom.  The CTA gathers the candidate
 // neighbours from the 27 surrounding cells into a shared-memory list (in
-// chunks of kNbCap), then every thread tests its dots against the list,
-// skipping dots that are already occluded.
+// chunks of kNbCap), walking the atom's own cell first, then the face, edge
+// and corner neighbours, so the list runs roughly nearest first.  Dots are
+// then tested in two phases:
+//  * every thread tests each of its dots against the first kPhaseA entries
+//    (most buried dots meet an occluder there);
+//  * the dots still open are taken one at a time by their warp, which tests
+//    32 further neighbours per step (one per lane) until a ballot finds an
+//    occluder or the list ends.
+// A thread-per-dot loop over the whole list would run each warp as long as
+// its slowest dot (an exposed dot scans every candidate).
 #include "rsx_internal.h"
 #include "rsx_sasa_internal.h"
 
@@ -23,6 +31,15 @@ namespace rsx {
 
 constexpr int kSasaThreads = 128;
 constexpr int kNbCap = 1024;
+constexpr int kPhaseA = 96; // neighbours every thread tests per dot before the warp takes over
+
+// The 27 cell offsets (dx, dy, dz) in order of distance: own cell, faces,
+// edges, corners.
+__constant__ signed char c_cell_order[27][3] = {
+    {0, 0, 0},   {-1, 0, 0},  {1, 0, 0},   {0, -1, 0},  {0, 1, 0},   {0, 0, -1},  {0, 0, 1},
+    {-1, -1, 0}, {-1, 1, 0},  {1, -1, 0},  {1, 1, 0},   {-1, 0, -1}, {-1, 0, 1},  {1, 0, -1},
+    {1, 0, 1},   {0, -1, -1}, {0, -1, 1},  {0, 1, -1},  {0, 1, 1},   {-1, -1, -1}, {-1, -1, 1},
+    {-1, 1, -1}, {-1, 1, 1},  {1, -1, -1}, {1, -1, 1},  {1, 1, -1},  {1, 1, 1}};
 
 __device__ __forceinline__ bool occludes(float sx, float sy, float sz, float4 b)
 {
@@ -78,7 +95,8 @@ __global__ void __launch_bounds__(kSasaThreads) sasa_kernel(const SasaArgs a)
             int begin = 0, end = 0;
             bool found = false;
             while (cell_idx < 27) {
-                const int ox = cell_idx / 9 - 1, oy = (cell_idx / 3) % 3 - 1, oz = cell_idx % 3 - 1;
+                const int ox = c_cell_order[cell_idx][0], oy = c_cell_order[cell_idx][1],
+                          oz = c_cell_order[cell_idx][2];
                 const int x = cx + ox, y = cy + oy, z = cz + oz;
                 if (x >= 0 && y >= 0 && z >= 0 && x < a.dims[0] && y < a.dims[1] && z < a.dims[2]) {
                     const int c = (x * a.dims[1] + y) * a.dims[2] + z;
@@ -120,7 +138,10 @@ __global__ void __launch_bounds__(kSasaThreads) sasa_kernel(const SasaArgs a)
         }
         __syncthreads();
         const int n_nb = s_count;
-        // test every not-yet-occluded dot of this thread against the list
+        const int n_a = min(n_nb, kPhaseA);
+        const int lane = tid & 31, warp_base = tid & ~31;
+        // phase A: every thread, its own dots, the first n_a neighbours
+        unsigned open = 0; // bit t: dot t still open after phase A
         for (int t = 0; t < dots_per_thread; ++t) {
             if (occluded & (1u << t))
                 continue;
@@ -129,7 +150,7 @@ __global__ void __launch_bounds__(kSasaThreads) sasa_kernel(const SasaArgs a)
             const float sy = __fadd_rn(__fmul_rn(a.unit[3 * k + 1], ext), pi.y);
             const float sz = __fadd_rn(__fmul_rn(a.unit[3 * k + 2], ext), pi.z);
             int n = 0;
-            for (; n < n_nb; ++n) {
+            for (; n < n_a; ++n) {
                 if (occludes(sx, sy, sz, s_nb[n])) {
                     occluded |= 1u << t;
                     ++n;
@@ -137,6 +158,34 @@ __global__ void __launch_bounds__(kSasaThreads) sasa_kernel(const SasaArgs a)
                 }
             }
             tests += (unsigned long long)n;
+            if (!(occluded & (1u << t)) && n_nb > n_a)
+                open |= 1u << t;
+        }
+        // phase B: the warp takes its open dots one at a time, 32 neighbours a step
+        for (int t = 0; t < dots_per_thread; ++t) {
+            unsigned pending = __ballot_sync(0xffffffffu, (open >> t) & 1u);
+            while (pending) {
+                const int owner = __ffs(pending) - 1;
+                pending &= pending - 1;
+                const int k = warp_base + owner + t * kSasaThreads;
+                const float sx = __fadd_rn(__fmul_rn(a.unit[3 * k + 0], ext), pi.x);
+                const float sy = __fadd_rn(__fmul_rn(a.unit[3 * k + 1], ext), pi.y);
+                const float sz = __fadd_rn(__fmul_rn(a.unit[3 * k + 2], ext), pi.z);
+                int tested = n_nb - n_a;
+                for (int j0 = n_a; j0 < n_nb; j0 += 32) {
+                    const int j = j0 + lane;
+                    const bool hit = j < n_nb && occludes(sx, sy, sz, s_nb[j]);
+                    const unsigned ball = __ballot_sync(0xffffffffu, hit);
+                    if (ball) {
+                        tested = j0 - n_a + __ffs(ball);
+                        if (lane == owner)
+                            occluded |= 1u << t;
+                        break;
+                    }
+                }
+                if (lane == owner)
+                    tests += (unsigned long long)tested;
+            }
         }
     }
     unsigned exposed = 0;
