@@ -169,12 +169,14 @@ cudaError_t launch_batch_forward(const DebyeArgs &a, const int *work_order, int 
 template <class K>
 static int occupancy_grid(K kfn, size_t smem, int sms);
 
-template <int QS, int IL = 2>
+template <int QS>
 static cudaError_t wide_batch_launch(const DebyeArgs &a, const int *order, int n_items,
                                      int n_slabs, int k_base, int *counter, int sms,
                                      cudaStream_t st)
 {
-    auto kfn = a.small_theta ? batch_wide_kernel<QS, IL, false> : batch_wide_kernel<QS, IL, true>;
+    // pairs per thread step as in the single-structure launcher
+    constexpr int IL_PLAIN = QS > 64 ? 4 : 2;
+    auto kfn = a.small_theta ? batch_wide_kernel<QS, IL_PLAIN, false> : batch_wide_kernel<QS, 2, true>;
     const int grid = std::min(occupancy_grid(kfn, 0, sms), n_items * n_slabs);
     kfn<<<grid, kBlockAtoms, 0, st>>>(a, order, n_items * n_slabs, n_slabs, k_base, counter);
     count_launch();
@@ -190,12 +192,12 @@ cudaError_t launch_batch_forward_wide(const DebyeArgs &a, const int *work_order,
     const WidePlan p = wide_plan(a.n_q, q_slab);
     if (p.full > 0) {
         cudaError_t e;
-        e = p.main == 64    ? wide_batch_launch<64, 2>(a, work_order, n_work_items, p.full, 0,
-                                                       counters, sms, st)
-            : p.main == 112 ? wide_batch_launch<112, 4>(a, work_order, n_work_items, p.full, 0,
-                                                        counters, sms, st)
-                            : wide_batch_launch<128, 4>(a, work_order, n_work_items, p.full, 0,
-                                                        counters, sms, st);
+        e = p.main == 64    ? wide_batch_launch<64>(a, work_order, n_work_items, p.full, 0,
+                                                    counters, sms, st)
+            : p.main == 112 ? wide_batch_launch<112>(a, work_order, n_work_items, p.full, 0,
+                                                     counters, sms, st)
+                            : wide_batch_launch<128>(a, work_order, n_work_items, p.full, 0,
+                                                     counters, sms, st);
         if (e != cudaSuccess)
             return e;
     }
@@ -304,10 +306,10 @@ int batch_forward_grid(int q_slab, bool uniform, int sms)
         return uniform ? occupancy_grid(batch_forward_kernel<32, true>, 0, sms)
                        : occupancy_grid(batch_forward_kernel<32, false>, 0, sms);
     case 64:
-        return uniform ? occupancy_grid(batch_wide_kernel<64, 2>, 0, sms)
+        return uniform ? occupancy_grid(batch_wide_kernel<64, 2, true>, 0, sms)
                        : occupancy_grid(batch_forward_kernel<32, false>, 0, sms);
     default:
-        return uniform ? occupancy_grid(batch_wide_kernel<112, 4>, 0, sms)
+        return uniform ? occupancy_grid(batch_wide_kernel<112, 2, true>, 0, sms)
                        : occupancy_grid(batch_forward_kernel<32, false>, 0, sms);
     }
 }

@@ -365,15 +365,20 @@ static cudaError_t forward_dispatch(const DebyeArgs &a, int qs, int k_base, int 
     }
 }
 
-template <int QS, int IL = 2>
+// Pairs per thread step: 4 in the plain (small-theta) instantiations of slabs
+// wider than 64 q (2 CTAs/SM: fewer warps need more independent chains), 2
+// otherwise; the signed loop measured slower with 4 (its odd steps chain four
+// FMAs on one accumulator).
+template <int QS>
 static cudaError_t wide_launch(DebyeArgs a, int k_base, int n_slabs, cudaStream_t st)
 {
+    constexpr int IL_PLAIN = QS > 64 ? 4 : 2;
     a.k_base = k_base;
     const dim3 grid(a.n_items, n_slabs);
     if (a.small_theta)
-        forward_wide_kernel<QS, IL, false><<<grid, kBlockAtoms, 0, st>>>(a);
+        forward_wide_kernel<QS, IL_PLAIN, false><<<grid, kBlockAtoms, 0, st>>>(a);
     else
-        forward_wide_kernel<QS, IL, true><<<grid, kBlockAtoms, 0, st>>>(a);
+        forward_wide_kernel<QS, 2, true><<<grid, kBlockAtoms, 0, st>>>(a);
     count_launch();
     return cudaGetLastError();
 }
@@ -407,7 +412,7 @@ static cudaError_t wide_tail(const DebyeArgs &a, int k0, int len, cudaStream_t s
 // 16..128 q.  The seed of a slab costs about as much as 40 steps, so short
 // tails are dear per q.
 static constexpr float kCostMain64 = 1.885f, kCostMain112 = 2.92f, kCostMain128 = 3.16f;
-static constexpr float kCostTail[8] = {1.10f, 1.15f, 1.50f, 1.885f, 2.60f, 2.79f, 2.92f, 3.16f};
+static constexpr float kCostTail[8] = {1.10f, 1.15f, 1.50f, 1.885f, 2.48f, 2.65f, 2.92f, 3.16f};
 
 static float tail_cost(int len) { return len > 0 ? kCostTail[(len + 15) / 16 - 1] : 0.f; }
 
@@ -443,9 +448,9 @@ static cudaError_t launch_forward_wide(const DebyeArgs &a, int q_slab, cudaStrea
     const WidePlan p = wide_plan(a.n_q, q_slab);
     if (p.full > 0) {
         cudaError_t e;
-        e = p.main == 64    ? wide_launch<64, 2>(a, 0, p.full, st)
-            : p.main == 112 ? wide_launch<112, 4>(a, 0, p.full, st)
-                            : wide_launch<128, 4>(a, 0, p.full, st);
+        e = p.main == 64    ? wide_launch<64>(a, 0, p.full, st)
+            : p.main == 112 ? wide_launch<112>(a, 0, p.full, st)
+                            : wide_launch<128>(a, 0, p.full, st);
         if (e != cudaSuccess)
             return e;
     }
