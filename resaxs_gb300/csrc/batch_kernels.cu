@@ -37,7 +37,7 @@ __global__ void __launch_bounds__(kBlockAtoms)
 
 // Wide uniform slabs (no water), as forward_wide_kernel.
 template <int QS, int IL, bool SIGNED = true>
-__global__ void __launch_bounds__(kBlockAtoms, QS <= 64 ? 3 : 2)
+__global__ void __launch_bounds__(kBlockAtoms, (QS <= 64 || !SIGNED) ? 3 : 2)
     batch_wide_kernel(const DebyeArgs a, const int *work_order, int n_units, int n_slabs,
                       int k_base, int *counter)
 {
@@ -174,9 +174,8 @@ static cudaError_t wide_batch_launch(const DebyeArgs &a, const int *order, int n
                                      int n_slabs, int k_base, int *counter, int sms,
                                      cudaStream_t st)
 {
-    // pairs per thread step as in the single-structure launcher
-    constexpr int IL_PLAIN = QS > 64 ? 4 : 2;
-    auto kfn = a.small_theta ? batch_wide_kernel<QS, IL_PLAIN, false> : batch_wide_kernel<QS, 2, true>;
+    // instantiations as in the single-structure launcher
+    auto kfn = a.small_theta ? batch_wide_kernel<QS, 2, false> : batch_wide_kernel<QS, 2, true>;
     const int grid = std::min(occupancy_grid(kfn, 0, sms), n_items * n_slabs);
     kfn<<<grid, kBlockAtoms, 0, st>>>(a, order, n_items * n_slabs, n_slabs, k_base, counter);
     count_launch();
@@ -205,7 +204,7 @@ cudaError_t launch_batch_forward_wide(const DebyeArgs &a, const int *work_order,
         return cudaSuccess;
 #define RSX_BW(QS)                                                                         \
     return wide_batch_launch<QS>(a, work_order, n_work_items, 1, p.tail_k0, counters + 1, sms, st)
-    switch ((p.tail_len + 15) / 16) {
+    switch (p.tail_w / 16) {
     case 1:
         RSX_BW(16);
     case 2:

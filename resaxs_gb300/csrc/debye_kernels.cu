@@ -38,7 +38,8 @@ __global__ void __launch_bounds__(kBlockAtoms) forward_kernel(const DebyeArgs a)
 
 // up to 64 q: <= 168 registers, 3 CTAs per SM; wider: <= 255, 2 CTAs per SM
 template <int QS, int IL, bool SIGNED>
-__global__ void __launch_bounds__(kBlockAtoms, QS <= 64 ? 3 : 2) forward_wide_kernel(const DebyeArgs a)
+__global__ void __launch_bounds__(kBlockAtoms, (QS <= 64 || !SIGNED) ? 3 : 2)
+    forward_wide_kernel(const DebyeArgs a)
 {
     forward_wide_item<QS, IL, SIGNED>(a, blockIdx.x, a.k_base + blockIdx.y * QS);
 }
@@ -365,27 +366,47 @@ static cudaError_t forward_dispatch(const DebyeArgs &a, int qs, int k_base, int 
     }
 }
 
-// Pairs per thread step: 4 in the plain (small-theta) instantiations of slabs
-// wider than 64 q (2 CTAs/SM: fewer warps need more independent chains), 2
-// otherwise; the signed loop measured slower with 4 (its odd steps chain four
-// FMAs on one accumulator).
+// Occupancy: the plain (small-theta) instantiations fit in 168 registers up
+// to 128 q, so 3 CTAs (12 warps) share an SM and hide the seed latency (6 %
+// faster than 2 CTAs with 4 pairs per step at 201 q); the signed ones keep 2
+// CTAs/SM above 64 q.  Both step 2 pairs at a time.
 template <int QS>
 static cudaError_t wide_launch(DebyeArgs a, int k_base, int n_slabs, cudaStream_t st)
 {
-    constexpr int IL_PLAIN = QS > 64 ? 4 : 2;
     a.k_base = k_base;
     const dim3 grid(a.n_items, n_slabs);
     if (a.small_theta)
-        forward_wide_kernel<QS, IL_PLAIN, false><<<grid, kBlockAtoms, 0, st>>>(a);
+        forward_wide_kernel<QS, 2, false><<<grid, kBlockAtoms, 0, st>>>(a);
     else
         forward_wide_kernel<QS, 2, true><<<grid, kBlockAtoms, 0, st>>>(a);
     count_launch();
     return cudaGetLastError();
 }
 
-static cudaError_t wide_tail(const DebyeArgs &a, int k0, int len, cudaStream_t st)
+// Relative cost of one slab per pair on GB300 (CUDA-event times of single
+// slabs at N = 20,000 on a compact structure, plain instantiations at 3
+// CTAs/SM, in ms per 2e8 pairs): full slabs of 64, 112 and 128 q, and a slab
+// 16, 32, ..., 128 q wide.  The seed of a slab costs about as much as 40
+// steps, so short slabs are dear per q (the 48-q slab measured slower than
+// the 64-q one, which therefore also serves remainders of 33..48 q).
+static constexpr float kCostMain64 = 1.82f, kCostMain112 = 2.75f, kCostMain128 = 3.00f;
+static constexpr float kCostWidth[8] = {0.99f, 1.35f, 2.34f, 1.82f, 2.13f, 2.29f, 2.75f, 3.00f};
+
+// Width (multiple of 16, <= 128) of the cheapest slab that covers len q.
+static int tail_width(int len)
 {
-    switch ((len + 15) / 16) {
+    int best = 0;
+    for (int w = (len + 15) / 16; w <= 8; ++w)
+        if (best == 0 || kCostWidth[w - 1] < kCostWidth[best / 16 - 1])
+            best = 16 * w;
+    return best;
+}
+
+static float tail_cost(int len) { return len > 0 ? kCostWidth[tail_width(len) / 16 - 1] : 0.f; }
+
+static cudaError_t wide_tail(const DebyeArgs &a, int k0, int width, cudaStream_t st)
+{
+    switch (width / 16) {
     case 1:
         return wide_launch<16>(a, k0, 1, st);
     case 2:
@@ -405,17 +426,6 @@ static cudaError_t wide_tail(const DebyeArgs &a, int k0, int len, cudaStream_t s
     }
 }
 
-// Relative cost of one slab per pair on GB300 (CUDA-event times of the
-// wide kernels at N = 20,000 / 50,000 / 100,000 on compact structures, in ms
-// per 2e8 pairs): full slabs of 64 q (2 pairs interleaved, 3 CTAs/SM), of
-// 112 and 128 q (4 pairs interleaved, 2 CTAs/SM), and a single tail slab of
-// 16..128 q.  The seed of a slab costs about as much as 40 steps, so short
-// tails are dear per q.
-static constexpr float kCostMain64 = 1.885f, kCostMain112 = 2.92f, kCostMain128 = 3.16f;
-static constexpr float kCostTail[8] = {1.10f, 1.15f, 1.50f, 1.885f, 2.48f, 2.65f, 2.92f, 3.16f};
-
-static float tail_cost(int len) { return len > 0 ? kCostTail[(len + 15) / 16 - 1] : 0.f; }
-
 // The cheapest of: 64-q slabs and a tail; 64-q slabs with a short remainder
 // (<= 48 q) folded into the last slab; 112-q slabs and a tail.
 WidePlan wide_plan(int n_q, int q_slab)
@@ -425,7 +435,7 @@ WidePlan wide_plan(int n_q, int q_slab)
     auto consider = [&](int main, int full, int rest, float cost) {
         if (cost < best_cost) {
             best_cost = cost;
-            best = WidePlan{main, full, full * main, rest, main >= 112 ? 4 : 2};
+            best = WidePlan{main, full, full * main, rest, rest > 0 ? tail_width(rest) : 0};
         }
     };
     const int f64 = n_q / 64, r64 = n_q - 64 * f64;
@@ -456,7 +466,7 @@ static cudaError_t launch_forward_wide(const DebyeArgs &a, int q_slab, cudaStrea
     }
     if (p.tail_len == 0)
         return cudaSuccess;
-    return wide_tail(a, p.tail_k0, p.tail_len, st);
+    return wide_tail(a, p.tail_k0, p.tail_w, st);
 }
 
 // Uniform grids without water and q_slab 64 / 128 take the wide slabs (64 or
@@ -532,7 +542,7 @@ static cudaError_t launch_delta_wide(const DeltaArgs &a, cudaStream_t st)
     }
     if (p.tail_len == 0)
         return cudaSuccess;
-    switch ((p.tail_len + 15) / 16) {
+    switch (p.tail_w / 16) {
     case 1:
         return delta_wide_launch<16>(a, p.tail_k0, 1, st);
     case 2:
@@ -545,8 +555,10 @@ static cudaError_t launch_delta_wide(const DeltaArgs &a, cudaStream_t st)
         return delta_wide_launch<80>(a, p.tail_k0, 1, st);
     case 6:
         return delta_wide_launch<96>(a, p.tail_k0, 1, st);
-    default:
+    case 7:
         return delta_wide_launch<112>(a, p.tail_k0, 1, st);
+    default: // a 64-q plan never needs a wider remainder slab
+        return cudaErrorInvalidValue;
     }
 }
 

@@ -78,11 +78,11 @@ constexpr int kDeltaGroups = 8; // moved-list groups of the wide delta kernel
 
 // launchers (debye_kernels.cu); all asynchronous on `st`
 // Slab plan of the wide uniform forward: `full` slabs of `main` q from q 0,
-// then one tail slab [tail_k0, tail_k0 + tail_len) (tail_len 0: none); `il`
-// pairs interleaved per thread in the main slabs.  q_slab 64 restricts the
-// plan to 64-q main slabs; 128 also allows 112- and 128-q slabs.
+// then one tail slab covering [tail_k0, tail_k0 + tail_len) with a kernel
+// `tail_w` q wide (tail_len 0: none).  q_slab 64 restricts the plan to 64-q
+// main slabs; 128 also allows 112- and 128-q slabs.
 struct WidePlan {
-    int main, full, tail_k0, tail_len, il;
+    int main, full, tail_k0, tail_len, tail_w;
 };
 WidePlan wide_plan(int n_q, int q_slab);
 
