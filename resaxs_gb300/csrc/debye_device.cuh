@@ -670,31 +670,33 @@ __device__ __forceinline__ void adj_circle_slab2(const float4 *t, int L, float s
     P2 = fmaf(d, e2, P2);
 }
 
-// Four pairs interleaved (all on the magic-circle form).
-__device__ __forceinline__ void adj_circle_slab4(const float4 *t, int L, float (&s)[4],
-                                                 float (&e)[4], const float (&ac)[4],
-                                                 float (&P)[4], float (&Q)[4])
+// IL pairs interleaved (all on the magic-circle form): one table load feeds
+// all of them.
+template <int IL>
+__device__ __forceinline__ void adj_circle_slabN(const float4 *t, int L, float (&s)[IL],
+                                                 float (&e)[IL], const float (&ac)[IL],
+                                                 float (&P)[IL], float (&Q)[IL])
 {
     for (int c = 0; c < L; c += 8) {
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
             const float2 cf = *reinterpret_cast<const float2 *>(t + c + u);
 #pragma unroll
-            for (int v = 0; v < 4; ++v) {
+            for (int v = 0; v < IL; ++v) {
                 P[v] = fmaf(cf.x, e[v], P[v]);
                 Q[v] = fmaf(cf.y, s[v], Q[v]);
             }
 #pragma unroll
-            for (int v = 0; v < 4; ++v)
+            for (int v = 0; v < IL; ++v)
                 e[v] = fmaf(-ac[v], s[v], e[v]);
 #pragma unroll
-            for (int v = 0; v < 4; ++v)
+            for (int v = 0; v < IL; ++v)
                 s[v] = fmaf(ac[v], e[v], s[v]);
         }
     }
     const float d = t[L].x;
 #pragma unroll
-    for (int v = 0; v < 4; ++v)
+    for (int v = 0; v < IL; ++v)
         P[v] = fmaf(d, e[v], P[v]);
 }
 
@@ -793,29 +795,33 @@ __device__ __forceinline__ void adj_pair2_sums(const DebyeArgs &a, const float4 
     B2 = Q2;
 }
 
-__device__ __forceinline__ void adj_pair4_sums(const DebyeArgs &a, const float4 *tab, int n_slabs,
-                                               const AdjPair (&p)[4], float (&A)[4],
-                                               float (&B)[4])
+template <int IL>
+__device__ __forceinline__ void adj_pairN_sums(const DebyeArgs &a, const float4 *tab, int n_slabs,
+                                               const AdjPair (&p)[IL], float (&A)[IL],
+                                               float (&B)[IL])
 {
-    float P[4] = {0.f, 0.f, 0.f, 0.f}, Q[4] = {0.f, 0.f, 0.f, 0.f}, ac[4];
+    float P[IL], Q[IL], ac[IL];
 #pragma unroll
-    for (int v = 0; v < 4; ++v)
+    for (int v = 0; v < IL; ++v) {
+        P[v] = 0.f;
+        Q[v] = 0.f;
         ac[v] = 2.0f * p[v].sh;
+    }
     for (int sl = 0; sl < n_slabs; ++sl) {
         const int kb = sl * kAdjSlab;
         const int L = (min(kAdjSlab, a.n_q - kb) + 7) & ~7;
         const float q0 = a.q[kb];
-        float s[4], e[4];
+        float s[IL], e[IL];
 #pragma unroll
-        for (int v = 0; v < 4; ++v) {
+        for (int v = 0; v < IL; ++v) {
             float c;
             slab_seed(q0, p[v].r, s[v], c);
             e[v] = fmaf(c, p[v].ch, s[v] * p[v].sh);
         }
-        adj_circle_slab4(tab + sl * kAdjStride, L, s, e, ac, P, Q);
+        adj_circle_slabN<IL>(tab + sl * kAdjStride, L, s, e, ac, P, Q);
     }
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
+    for (int v = 0; v < IL; ++v) {
         A[v] = P[v] * (0.5f / p[v].ch);
         B[v] = Q[v];
     }
@@ -893,22 +899,25 @@ __device__ __forceinline__ void adjoint_uniform_item(const DebyeArgs &a, int ite
         __syncthreads();
         const bool diag = (b == it.bi);
         int jj = 0;
-        if (IL == 4) {
-            for (; jj + 3 < bj.len; jj += 4) {
-                AdjPair p[4];
+        if (IL > 2) {
+            for (; jj + IL - 1 < bj.len; jj += IL) {
+                AdjPair p[IL];
+                bool all_circle = true;
 #pragma unroll
-                for (int v = 0; v < 4; ++v)
+                for (int v = 0; v < IL; ++v) {
                     p[v] = adj_pair<SMALL>(pi, s_pos[jj + v], dq);
-                float A[4], B[4];
-                if (p[0].circle && p[1].circle && p[2].circle && p[3].circle) {
-                    adj_pair4_sums(a, tab, n_slabs, p, A, B);
+                    all_circle = all_circle && p[v].circle;
+                }
+                float A[IL], B[IL];
+                if (all_circle) {
+                    adj_pairN_sums<IL>(a, tab, n_slabs, p, A, B);
                 } else {
 #pragma unroll
-                    for (int v = 0; v < 4; ++v)
+                    for (int v = 0; v < IL; ++v)
                         adj_pair_sums(a, tab, n_slabs, p[v], A[v], B[v]);
                 }
 #pragma unroll
-                for (int v = 0; v < 4; ++v)
+                for (int v = 0; v < IL; ++v)
                     adj_scatter(p[v], A[v], B[v], valid_i && (!diag || jj + v > tid), gi0, gi1,
                                 gi2, s_gj, jj + v, lane);
             }
