@@ -40,6 +40,22 @@ def test_batch_forward_vs_oracle(oracle_lib, ensemble):
         assert rel(out[m], oracle_lib.debye_f64(q, body, ff)) < TOL, m
 
 
+def test_batch_spread_member_switches_kernels(oracle_lib, ensemble):
+    """Stretching one member 600 A wide takes the whole pass off the
+    small-theta kernels (signed far-pair steps, reduced seeds, graph captured
+    again); compacting it brings them back.  Every curve must follow."""
+    from resaxs_gb300.batch import DebyeBatch
+    q, ff, members = ensemble
+    spread = [m.copy() for m in members]
+    spread[5][:, :3] *= np.float32(8.0)
+    with DebyeBatch(q, ff, [len(m) for m in members]) as b:
+        for ms in (members, spread, members):
+            out = b.forward(ms)
+            for m, body in enumerate(ms):
+                if len(body) > 0:
+                    assert rel(out[m], oracle_lib.debye_f64(q, body, ff)) < TOL, m
+
+
 def test_batch_new_positions_and_types(oracle_lib, ensemble):
     from resaxs_gb300.batch import DebyeBatch
     q, ff, members = ensemble

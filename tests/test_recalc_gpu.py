@@ -46,6 +46,26 @@ def test_recalc_indices_matches_full_recompute(S, oracle_lib, q_slab, n_q):
             assert rel(out, ref) < TOL
 
 
+def test_recalc_far_pairs(S, oracle_lib):
+    """A free random-walk chain on a coarse grid: many pairs step angles past
+    pi/2 (signed far-pair steps in the wide delta kernel); moves far beyond
+    the current extent must also be followed."""
+    w = W.make_config(1, seed=23, n_override=1500)
+    q = W.q_grid(101, 0.8)
+    ff = W.exp_form_factors(q, W.Z5, np.random.default_rng(4).uniform(0.5, 2.0, 5))
+    rng = np.random.default_rng(5)
+    bodies = w.bodies.copy()
+    with S.Debye(q, ff, w.n) as d:
+        d.calc(bodies)
+        for step in range(3):
+            idx = rng.choice(w.n, size=40, replace=False).astype(np.uint32)
+            moved = bodies[idx].copy()
+            moved[:, :3] += rng.normal(0, 40.0 if step == 1 else 0.5, (40, 3)).astype(np.float32)
+            d.recalc_indices(moved, idx)
+            bodies[idx] = moved
+            assert rel(d.curve_f64(), oracle_lib.debye_f64(q, bodies, ff)) < TOL, step
+
+
 def test_recalc_range_matches_full_recompute(S, oracle_lib):
     """The reference's contiguous-range API (saxs_algorithm.hpp:172)."""
     w = W.make_config(1, seed=22, n_override=900)
