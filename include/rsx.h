@@ -71,6 +71,11 @@ rsx_status rsx_debug_layout(const rsx_body *bodies, int n_bodies, int n_factors,
                             int min_adj_items, int *n_blocks, int *n_items, int *n_adj_items,
                             int *pairs_covered_ok);
 
+/* Host-only view of the slab plan of the wide uniform kernels for n_q q and
+ * q_slab 64 or 128: out[0..4] = main slab width, number of main slabs, first
+ * q of the remainder slab, q it covers, width of its kernel (0: none). */
+rsx_status rsx_debug_wide_plan(int n_q, int q_slab, int *out);
+
 /* Host-only check of the shard split used by rsx_debye_calc_shard: item
  * bounds[0..n_shards] (shard s = items [bounds[s], bounds[s+1])) and, if
  * pairs is not NULL, the body pairs of each shard. */

@@ -1,5 +1,6 @@
 // Debye pair kernels for sm_103a: forward I(q), incremental delta I(q) and
-// the adjoint dL/dx.  Written from scratch for this project.
+// the adjoint dL/dx, with their launchers.  Written from scratch for this
+// project; the per-item device code is in debye_device.cuh.
 //
 // Common structure
 //  * Bodies are stored in type-sorted order and cut into block tiles of at
@@ -7,18 +8,20 @@
 //    of tiles has a single pair of form factors F[q][t_i] * F[q][t_j].
 //  * One CTA of 128 threads owns an I-block (one body per thread) and streams
 //    its J-blocks through shared memory with one float4 load per thread.
-//  * A CTA covers a slab of QS consecutive q values.  On a uniform q grid the
-//    per-pair values sin(q_k r)/r, cos(q_k r)/r for the slab are produced by
-//    rotating the pair (s, c) by the angle dq*r: 4 FP32 ops per q instead of a
-//    sine evaluation.  The seeds sin/cos(q_0 r) and sin/cos(dq r) come from an
-//    explicit Cody-Waite range reduction plus the Taylor series (rsx_math.cuh),
-//    so they carry relative accuracy even for tiny arguments, and the rotation
-//    keeps that relative accuracy (error grows ~ k*eps over the slab).
+//  * A CTA covers a slab of consecutive q values.  On a uniform q grid the
+//    per-pair values sin(q_k r)/r come from Reinsch's two-term recurrence
+//    (3 FP32 ops per pair*q with the accumulation), seeded per pair and slab
+//    from the range-reduced FP32 sin/cos of rsx_math.cuh; the wide kernels
+//    (forward_wide_kernel, delta_wide_kernel) run 64..128 q per seed following
+//    the slab plan of wide_plan().  Non-uniform grids and water use
+//    forward_kernel / delta_kernel (8..32 q per slab, sin/cos per pair*q).
 //    sinc(q r) = (sin(q r)/r) / q: the 1/q factor is applied once per q in FP64
 //    when the curve is assembled.
-//  * Per-thread sums: plain FP32 over one J-block, then folded into a Kahan
-//    (compensated) accumulator per q.  Warp-level: a reduce-scatter with
-//    shuffles (lane k ends with q index k).  Across warps and CTAs: FP64.
+//  * Per-thread sums: FP32 over one J-block, then reduce-scattered over the
+//    warp into FP64 (wide kernels) or folded into a Kahan accumulator per q
+//    (general kernels).  Across warps and CTAs: FP64.
+//  * The adjoint steps sin and cos(q r - theta/2) together (the magic-circle
+//    form) and sums both sides of every pair's gradient; see debye_device.cuh.
 #include "debye_device.cuh"
 
 #include <algorithm>

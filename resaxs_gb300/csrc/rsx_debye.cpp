@@ -869,6 +869,19 @@ rsx_status rsx_debye_calc_shard(rsx_debye *h, const rsx_body *bodies, int shard,
     return ok();
 }
 
+rsx_status rsx_debug_wide_plan(int n_q, int q_slab, int *out)
+{
+    if (n_q <= 0 || !out || (q_slab != 64 && q_slab != 128))
+        return fail(RSX_INVALID_ARG, "need n_q > 0, q_slab 64 or 128 and an output");
+    const WidePlan p = wide_plan(n_q, q_slab);
+    out[0] = p.main;
+    out[1] = p.full;
+    out[2] = p.tail_k0;
+    out[3] = p.tail_len;
+    out[4] = p.tail_w;
+    return ok();
+}
+
 rsx_status rsx_debug_shard_items(const rsx_body *bodies, int n_bodies, int n_factors,
                                  int max_items, int n_shards, int *bounds, double *pairs)
 {

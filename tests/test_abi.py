@@ -102,3 +102,26 @@ def test_layout_covers_every_block_pair_once(librsx, n, types, max_items):
     if n:
         # at most one item per (I-block, remaining type run) once the cap bites
         assert ni.value <= max(max_items, nb.value * types)
+
+
+def test_wide_slab_plan_covers_every_q(librsx):
+    """The slab plan of the wide kernels: main slabs plus one remainder slab
+    cover [0, n_q) exactly, every kernel width exists (16..128 in steps of 16)
+    and a 64-q plan (the incremental kernel's) never needs a remainder slab
+    wider than 112 q."""
+    from resaxs_gb300 import _lib
+    out = np.zeros(5, np.int32)
+    for q_slab in (64, 128):
+        for n_q in range(1, 700):
+            _lib.check(librsx.rsx_debug_wide_plan(n_q, q_slab, out))
+            main, full, k0, tail_len, tail_w = (int(x) for x in out)
+            assert main in ((64,) if q_slab == 64 else (64, 112, 128)), (n_q, out)
+            assert k0 == full * main and k0 + tail_len == n_q, (n_q, out)
+            if tail_len:
+                assert tail_w % 16 == 0 and tail_len <= tail_w <= 128, (n_q, out)
+                if q_slab == 64:
+                    assert tail_w <= 112, (n_q, out)
+            else:
+                assert tail_w == 0
+    assert librsx.rsx_debug_wide_plan(0, 128, out) == _lib.RSX_INVALID_ARG
+    assert librsx.rsx_debug_wide_plan(10, 32, out) == _lib.RSX_INVALID_ARG
