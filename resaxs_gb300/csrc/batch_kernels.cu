@@ -175,7 +175,7 @@ static cudaError_t wide_batch_launch(const DebyeArgs &a, const int *order, int n
                                      cudaStream_t st)
 {
     // instantiations as in the single-structure launcher
-    auto kfn = a.small_theta ? batch_wide_kernel<QS, 2, false> : batch_wide_kernel<QS, 2, true>;
+    auto kfn = a.small_theta >= 2 ? batch_wide_kernel<QS, 2, false> : batch_wide_kernel<QS, 2, true>;
     const int grid = std::min(occupancy_grid(kfn, 0, sms), n_items * n_slabs);
     kfn<<<grid, kBlockAtoms, 0, st>>>(a, order, n_items * n_slabs, n_slabs, k_base, counter);
     count_launch();
@@ -231,7 +231,7 @@ static cudaError_t adj_launch(const DebyeArgs &a, const int *order, int n_items,
 {
     const int n_slabs = (a.n_q + QS - 1) / QS;
     const size_t smem = adjoint_smem_bytes(a.n_q, QS, U, false);
-    auto kfn = (U && a.small_theta) ? batch_adjoint_kernel<QS, U, true> : batch_adjoint_kernel<QS, U, false>;
+    auto kfn = (U && a.small_theta >= 1) ? batch_adjoint_kernel<QS, U, true> : batch_adjoint_kernel<QS, U, false>;
     if (smem > 48 * 1024) {
         cudaError_t e =
             cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -183,13 +183,39 @@ struct WideSlab {
     static constexpr int NR = QP / 32;             // q values per lane after the scatter
 };
 
-// sin/cos(q0 r) (exactly 0 and 1 when q0 = 0, as sincos_prod gives) and
-// sin/cos(theta/2); `small_theta` (uniform over the launch) promises
-// |theta/2| < pi/4, where the reduction is the identity (sincos_small2 gives
-// sincos_rr2's results bit for bit).  Both tests are uniform branches.
-__device__ __forceinline__ void seed_angles(float q0, float dq, float r, bool small_theta,
-                                            float &s0, float &c0, float &sh, float &ch)
+// Seed of the wide path: Reinsch's recurrence in paired steps.  The q values
+// of a slab are taken two at a time: the even ones (k = 2m) and the odd ones
+// (k = 2m + 1) form two sequences with the step 2 theta (theta = dq r), packed
+// in one float2 so that every FP32x2 instruction (__ffma2_rn, __fadd2_rn)
+// advances both.  The FP32 lane work stays at 3 operations per pair*q, but
+// the issue slots are halved: the scalar loop is issue-bound (a measured 77 %
+// of the FMA rate in a register-resident test), the paired one runs at the
+// FMA rate.  Reinsch's form, with lam = -4 sin^2(theta) (the half angle of
+// the step 2 theta):
+//     d_{m+1} = d_m + lam s_m,   s_{m+1} = s_m + d_{m+1},
+// seeded with d_0 = s_0 - s_{-1}, the previous element of the same sequence:
+//     even: sin(x0) - sin(x0 - 2 theta)     = 2 sin(theta) cos(x0 - theta)
+//     odd:  sin(x0 + theta) - sin(x0 - theta) = 2 sin(theta) cos(x0).
+// The form is accurate while cos^2(theta) >= sin^2(theta).  Elsewhere (theta
+// mod pi in (pi/4, 3 pi/4): far-apart bodies on coarse grids) both sequences
+// run instead on t_m = (-1)^m s_m, whose step 2 theta - pi is back in range:
+//     lam = -4 cos^2(theta),
+//     d_0 = 2 cos(theta) sin(x0 - theta) (even),  2 cos(theta) sin(x0) (odd),
+// and odd m are accumulated with the sign sg = -1.  So every pair steps an
+// angle of magnitude <= pi/2 with the same operations, and no warp diverges
+// on far pairs.
+struct WideSeed {
+    float2 s, d; // (even, odd) t_0 / r and d_0 / r
+    float l, sg; // lam, sign of the odd steps (+1 or -1)
+};
+
+// `small_theta` (uniform over the launch) promises |theta| < pi/4 for every
+// pair, where the reduction is the identity (sincos_small2 gives sincos_rr2's
+// results bit for bit) and every sign is +1.
+__device__ __forceinline__ WideSeed wide_seed(float q0, float dq, float r, float sc,
+                                              bool small_theta = false)
 {
+    float s0, c0, st, ct;
     if (q0 == 0.f) {
         s0 = 0.f;
         c0 = 1.f;
@@ -199,120 +225,116 @@ __device__ __forceinline__ void seed_angles(float q0, float dq, float r, bool sm
     const float th = dq * r;
     const float th_lo = fmaf(dq, r, -th);
     if (small_theta)
-        sincos_small2(0.5f * th, 0.5f * th_lo, sh, ch);
+        sincos_small2(th, th_lo, st, ct);
     else
-        sincos_rr2(0.5f * th, 0.5f * th_lo, sh, ch);
-}
-
-// Seed of the wide path: Reinsch's recurrence on a folded angle, branch-free
-// for every theta.  The step angle theta = dq r enters the recurrence only
-// through lam, so any theta is equivalent to its value mod 2 pi; where
-// cos^2(theta/2) < sin^2(theta/2) (theta mod 2 pi in (pi/2, 3 pi/2), where the
-// form loses accuracy as theta -> pi) the recurrence runs instead on
-//     t_k = (-1)^k s_k = sin(x0 + k (theta - pi)),
-// whose angle theta - pi lies in (-pi/2, pi/2):
-//     lam = -4 cos^2(theta/2),  d_0 = t_0 - t_{-1} = 2 cos(theta/2) sin(x0 - theta/2),
-// and the odd steps are accumulated with the sign sg = -1.  So every pair
-// steps an angle of magnitude <= pi/2 with the same three operations, and no
-// warp diverges on far-apart pairs.
-struct WideSeed {
-    float s, d, l, sg; // t_0 / r, d_0 / r, lam, sign of the odd steps (+1 or -1)
-};
-
-__device__ __forceinline__ WideSeed wide_seed(float q0, float dq, float r, float sc,
-                                              bool small_theta = false)
-{
+        sincos_rr2(th, th_lo, st, ct);
     WideSeed p;
-    float s0, c0, sh, ch;
-    seed_angles(q0, dq, r, small_theta, s0, c0, sh, ch);
-    p.s = s0 * sc;
-    if (ch * ch >= sh * sh) {
-        p.l = -4.0f * sh * sh;
-        p.d = 2.0f * sh * fmaf(c0, ch, s0 * sh) * sc;
+    p.s = make_float2(s0 * sc, fmaf(s0, ct, c0 * st) * sc); // sin(x0), sin(x0 + theta)
+    if (ct * ct >= st * st) {
+        p.l = -4.0f * st * st;
+        const float g = 2.0f * st * sc;
+        p.d = make_float2(g * fmaf(c0, ct, s0 * st), g * c0);
         p.sg = 1.0f;
     } else {
-        p.l = -4.0f * ch * ch;
-        p.d = 2.0f * ch * fmaf(s0, ch, -c0 * sh) * sc;
+        p.l = -4.0f * ct * ct;
+        const float g = 2.0f * ct * sc;
+        p.d = make_float2(g * fmaf(s0, ct, -c0 * st), g * s0);
         p.sg = -1.0f;
     }
     return p;
 }
 
-// Two pairs, interleaved for ILP (the hot loop: 3 FP32 lane-ops per pair*q).
-// SIGNED adds the odd steps with the pairs' signs (FMAs); warps whose pairs
-// all have sign +1 (compact structures: all of them) take the plain adds,
-// which the FMA chain would slow by ~9 %.
-template <int QS, int QP, bool SIGNED>
+__device__ __forceinline__ float2 splat2(float x) { return make_float2(x, x); }
+
+// Two pairs, interleaved for ILP (the hot loop: per paired step of both
+// pairs 6 FP32x2 instructions = 12 lane-ops for 4 pair*q).  S[m] holds
+// (q_{2m}, q_{2m+1}).  SIGNED adds the odd steps with the pairs' signs;
+// warps whose pairs all have sign +1 (compact structures: all of them) take
+// the plain adds.
+template <int QS, int QH, bool SIGNED>
 __device__ __forceinline__ void wide_pair2_body(const WideSeed &a, const WideSeed &b,
-                                                float (&S)[QP])
+                                                float2 (&S)[QH])
 {
-    float sa = a.s, da = a.d, sb = b.s, db = b.d;
+    float2 sa = a.s, da = a.d, sb = b.s, db = b.d;
+    const float2 la = splat2(a.l), lb = splat2(b.l);
 #pragma unroll
-    for (int k = 0; k < QS; ++k) {
-        if (SIGNED && (k & 1))
-            S[k] = fmaf(a.sg, sa, fmaf(b.sg, sb, S[k]));
+    for (int m = 0; m < QS / 2; ++m) {
+        if (SIGNED && (m & 1))
+            S[m] = __ffma2_rn(splat2(a.sg), sa, __ffma2_rn(splat2(b.sg), sb, S[m]));
         else
-            S[k] += sa + sb;
-        da = fmaf(a.l, sa, da);
-        db = fmaf(b.l, sb, db);
-        sa += da;
-        sb += db;
+            S[m] = __fadd2_rn(S[m], __fadd2_rn(sa, sb));
+        da = __ffma2_rn(la, sa, da);
+        db = __ffma2_rn(lb, sb, db);
+        sa = __fadd2_rn(sa, da);
+        sb = __fadd2_rn(sb, db);
     }
 }
 
-template <int QS, int QP>
-__device__ __forceinline__ void wide_pair2(const WideSeed &a, const WideSeed &b, float (&S)[QP])
+template <int QS, int QH>
+__device__ __forceinline__ void wide_pair2(const WideSeed &a, const WideSeed &b, float2 (&S)[QH])
 {
     if (__any_sync(0xffffffffu, a.sg < 0.f || b.sg < 0.f))
-        wide_pair2_body<QS, QP, true>(a, b, S);
+        wide_pair2_body<QS, QH, true>(a, b, S);
     else
-        wide_pair2_body<QS, QP, false>(a, b, S);
+        wide_pair2_body<QS, QH, false>(a, b, S);
 }
 
 // Four pairs: more independent chains per warp for when few warps fit on an SM.
-template <int QS, int QP, bool SIGNED>
+template <int QS, int QH, bool SIGNED>
 __device__ __forceinline__ void wide_pair4_body(const WideSeed &a, const WideSeed &b,
                                                 const WideSeed &c, const WideSeed &e,
-                                                float (&S)[QP])
+                                                float2 (&S)[QH])
 {
-    float sa = a.s, da = a.d, sb = b.s, db = b.d, sc = c.s, dc = c.d, se = e.s, de = e.d;
+    float2 sa = a.s, da = a.d, sb = b.s, db = b.d, sc = c.s, dc = c.d, se = e.s, de = e.d;
+    const float2 la = splat2(a.l), lb = splat2(b.l), lc = splat2(c.l), le = splat2(e.l);
 #pragma unroll
-    for (int k = 0; k < QS; ++k) {
-        if (SIGNED && (k & 1))
-            S[k] = fmaf(a.sg, sa, fmaf(b.sg, sb, fmaf(c.sg, sc, fmaf(e.sg, se, S[k]))));
+    for (int m = 0; m < QS / 2; ++m) {
+        if (SIGNED && (m & 1))
+            S[m] = __ffma2_rn(splat2(a.sg), sa,
+                              __ffma2_rn(splat2(b.sg), sb,
+                                         __ffma2_rn(splat2(c.sg), sc,
+                                                    __ffma2_rn(splat2(e.sg), se, S[m]))));
         else
-            S[k] += (sa + sb) + (sc + se);
-        da = fmaf(a.l, sa, da);
-        db = fmaf(b.l, sb, db);
-        dc = fmaf(c.l, sc, dc);
-        de = fmaf(e.l, se, de);
-        sa += da;
-        sb += db;
-        sc += dc;
-        se += de;
+            S[m] = __fadd2_rn(S[m], __fadd2_rn(__fadd2_rn(sa, sb), __fadd2_rn(sc, se)));
+        da = __ffma2_rn(la, sa, da);
+        db = __ffma2_rn(lb, sb, db);
+        dc = __ffma2_rn(lc, sc, dc);
+        de = __ffma2_rn(le, se, de);
+        sa = __fadd2_rn(sa, da);
+        sb = __fadd2_rn(sb, db);
+        sc = __fadd2_rn(sc, dc);
+        se = __fadd2_rn(se, de);
     }
 }
 
-template <int QS, int QP>
+template <int QS, int QH>
 __device__ __forceinline__ void wide_pair4(const WideSeed &a, const WideSeed &b, const WideSeed &c,
-                                           const WideSeed &e, float (&S)[QP])
+                                           const WideSeed &e, float2 (&S)[QH])
 {
     if (__any_sync(0xffffffffu, a.sg < 0.f || b.sg < 0.f || c.sg < 0.f || e.sg < 0.f))
-        wide_pair4_body<QS, QP, true>(a, b, c, e, S);
+        wide_pair4_body<QS, QH, true>(a, b, c, e, S);
     else
-        wide_pair4_body<QS, QP, false>(a, b, c, e, S);
+        wide_pair4_body<QS, QH, false>(a, b, c, e, S);
 }
 
-template <int QS, int QP>
-__device__ __forceinline__ void wide_pair1(const WideSeed &p, float (&S)[QP])
+template <int QS, int QH>
+__device__ __forceinline__ void wide_pair1(const WideSeed &p, float2 (&S)[QH])
 {
-    float s = p.s, d = p.d;
+    float2 s = p.s, d = p.d;
+    const float2 l = splat2(p.l), g = splat2(p.sg);
 #pragma unroll
-    for (int k = 0; k < QS; ++k) {
-        S[k] = (k & 1) ? fmaf(p.sg, s, S[k]) : S[k] + s;
-        d = fmaf(p.l, s, d);
-        s += d;
+    for (int m = 0; m < QS / 2; ++m) {
+        S[m] = (m & 1) ? __ffma2_rn(g, s, S[m]) : __fadd2_rn(S[m], s);
+        d = __ffma2_rn(l, s, d);
+        s = __fadd2_rn(s, d);
     }
+}
+
+// Value of q index k of a paired accumulator array.
+template <int QH>
+__device__ __forceinline__ float pair_at(const float2 (&S)[QH], int k)
+{
+    return (k & 1) ? S[k >> 1].y : S[k >> 1].x;
 }
 
 // Forward pair sums of one work item for q values [k0, k0 + QS) on a uniform
@@ -337,7 +359,7 @@ __device__ __forceinline__ void forward_wide_item(const DebyeArgs &a, int item_i
     const float4 pi = valid_i ? a.pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float q0 = a.q[k0];
     const float dq = a.dq;
-    const bool small_th = !SIGNED || a.small_theta != 0;
+    const bool small_th = !SIGNED || a.small_theta >= 2;
 
     double acc[NR];
 #pragma unroll
@@ -351,10 +373,10 @@ __device__ __forceinline__ void forward_wide_item(const DebyeArgs &a, int item_i
             s_pos[tid] = a.pos[bj.start + tid];
         __syncthreads();
         const bool diag = (b == it.bi);
-        float S[QP];
+        float2 S[QP / 2];
 #pragma unroll
-        for (int k = 0; k < QP; ++k)
-            S[k] = 0.f;
+        for (int m = 0; m < QP / 2; ++m)
+            S[m] = make_float2(0.f, 0.f);
         int jj = 0;
         if (IL == 4) {
             for (; jj + 3 < bj.len; jj += 4) {
@@ -367,9 +389,9 @@ __device__ __forceinline__ void forward_wide_item(const DebyeArgs &a, int item_i
                     p[u] = wide_seed(q0, dq, r, use ? ri : 0.f, small_th);
                 }
                 if constexpr (SIGNED)
-                    wide_pair4<QS, QP>(p[0], p[1], p[2], p[3], S);
+                    wide_pair4<QS, QP / 2>(p[0], p[1], p[2], p[3], S);
                 else
-                    wide_pair4_body<QS, QP, false>(p[0], p[1], p[2], p[3], S);
+                    wide_pair4_body<QS, QP / 2, false>(p[0], p[1], p[2], p[3], S);
             }
         }
         for (; jj + 1 < bj.len; jj += 2) {
@@ -381,22 +403,22 @@ __device__ __forceinline__ void forward_wide_item(const DebyeArgs &a, int item_i
             const WideSeed p1 = wide_seed(q0, dq, r1, u1 ? ri1 : 0.f, small_th);
             const WideSeed p2 = wide_seed(q0, dq, r2, u2 ? ri2 : 0.f, small_th);
             if constexpr (SIGNED)
-                wide_pair2<QS, QP>(p1, p2, S);
+                wide_pair2<QS, QP / 2>(p1, p2, S);
             else
-                wide_pair2_body<QS, QP, false>(p1, p2, S);
+                wide_pair2_body<QS, QP / 2, false>(p1, p2, S);
         }
         if (jj < bj.len) {
             float r, rinv, dx, dy, dz;
             pair_r(pi, s_pos[jj], r, rinv, dx, dy, dz);
             const bool use = valid_i && (!diag || jj > tid);
-            wide_pair1<QS, QP>(wide_seed(q0, dq, r, use ? rinv : 0.f, small_th), S);
+            wide_pair1<QS, QP / 2>(wide_seed(q0, dq, r, use ? rinv : 0.f, small_th), S);
         }
 #pragma unroll
         for (int c = 0; c < NR; ++c) {
             float v[32];
 #pragma unroll
             for (int k = 0; k < 32; ++k)
-                v[k] = S[32 * c + k];
+                v[k] = pair_at(S, 32 * c + k);
             warp_reduce_scatter<32>(v, lane);
             acc[c] += (double)v[0];
         }
@@ -587,15 +609,20 @@ __device__ __forceinline__ void forward_item(const DebyeArgs &a, int item_idx, i
 //     A = sum_{m=0..L} delta_m e_m / (2 cos(theta/2)),
 //     delta_m = alpha_m + alpha_{m-1}   (alpha outside the slab = 0),
 // so a pair costs four FMAs per q: two for the recurrence and one for each
-// sum.  The recurrence is reseeded from sin/cos(q_0 r) every kAdjSlab q.
-// Pairs with theta > pi/2 (cos(theta/2)^2 < 1/2, far-apart bodies on coarse
-// grids) take the rotation form with alpha directly.
+// sum.  Pairs step two at a time, packed in float2 lanes, so each FP32x2
+// instruction (__ffma2_rn) advances both: the same lane work in half the
+// issue slots.  The recurrence is reseeded from sin/cos(q_0 r) every kAdjSlab
+// q.  Pairs with theta > pi/2 (cos(theta/2)^2 < 1/2, far-apart bodies on
+// coarse grids) take the rotation form with alpha directly.
 
 constexpr int kAdjSlab = 256;   // q values between reseeds
 constexpr int kAdjStride = 257; // table entries per slab (delta has L + 1)
 
-// Table entry m of slab sl: (delta_m, beta_m, alpha_m, 0).
-__device__ __forceinline__ void adjoint_uniform_table(const DebyeArgs &a, float4 *tab, int n_slabs,
+// Table entry m of slab sl: tab = (delta_m, delta_m, beta_m, beta_m) (each
+// coefficient twice, the operand of a paired instruction) and tab_a = alpha_m
+// (the rotation form's cosine coefficient).
+__device__ __forceinline__ void adjoint_uniform_table(const DebyeArgs &a, float4 *tab,
+                                                      float *tab_a, int n_slabs,
                                                       const float *lambda, int ti, int tj)
 {
     const int n = n_slabs * kAdjStride;
@@ -623,7 +650,8 @@ __device__ __forceinline__ void adjoint_uniform_table(const DebyeArgs &a, float4
         float b0, bm1;
         const float a0 = alpha(m, &b0);
         const float am1 = alpha(m - 1, &bm1);
-        tab[idx] = make_float4(a0 + am1, b0, a0, 0.f);
+        tab[idx] = make_float4(a0 + am1, a0 + am1, b0, b0);
+        tab_a[idx] = a0;
     }
 }
 
@@ -635,9 +663,9 @@ __device__ __forceinline__ void adj_circle_slab(const float4 *t, int L, float s,
     for (int c = 0; c < L; c += 8) {
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-            const float2 cf = *reinterpret_cast<const float2 *>(t + c + u);
+            const float4 cf = t[c + u];
             P = fmaf(cf.x, e, P);
-            Q = fmaf(cf.y, s, Q);
+            Q = fmaf(cf.z, s, Q);
             e = fmaf(-ac, s, e);
             s = fmaf(ac, e, s);
         }
@@ -645,69 +673,49 @@ __device__ __forceinline__ void adj_circle_slab(const float4 *t, int L, float s,
     P = fmaf(t[L].x, e, P);
 }
 
-// Two pairs interleaved (both on the magic-circle form): one table load feeds
-// both.
-__device__ __forceinline__ void adj_circle_slab2(const float4 *t, int L, float s1, float e1,
-                                                 float a1, float s2, float e2, float a2, float &P1,
-                                                 float &Q1, float &P2, float &Q2)
+// NP float2 lanes of two pairs each (all on the magic-circle form): one table
+// load feeds all of them.
+template <int NP>
+__device__ __forceinline__ void adj_circle_slab_paired(const float4 *t, int L, float2 (&s)[NP],
+                                                       float2 (&e)[NP], const float2 (&ac)[NP],
+                                                       float2 (&P)[NP], float2 (&Q)[NP])
 {
+    float2 nac[NP];
+#pragma unroll
+    for (int v = 0; v < NP; ++v)
+        nac[v] = make_float2(-ac[v].x, -ac[v].y);
     for (int c = 0; c < L; c += 8) {
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-            const float2 cf = *reinterpret_cast<const float2 *>(t + c + u);
-            P1 = fmaf(cf.x, e1, P1);
-            Q1 = fmaf(cf.y, s1, Q1);
-            P2 = fmaf(cf.x, e2, P2);
-            Q2 = fmaf(cf.y, s2, Q2);
-            e1 = fmaf(-a1, s1, e1);
-            e2 = fmaf(-a2, s2, e2);
-            s1 = fmaf(a1, e1, s1);
-            s2 = fmaf(a2, e2, s2);
-        }
-    }
-    const float d = t[L].x;
-    P1 = fmaf(d, e1, P1);
-    P2 = fmaf(d, e2, P2);
-}
-
-// IL pairs interleaved (all on the magic-circle form): one table load feeds
-// all of them.
-template <int IL>
-__device__ __forceinline__ void adj_circle_slabN(const float4 *t, int L, float (&s)[IL],
-                                                 float (&e)[IL], const float (&ac)[IL],
-                                                 float (&P)[IL], float (&Q)[IL])
-{
-    for (int c = 0; c < L; c += 8) {
+            const float4 cf = t[c + u];
+            const float2 dd = make_float2(cf.x, cf.y), bb = make_float2(cf.z, cf.w);
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const float2 cf = *reinterpret_cast<const float2 *>(t + c + u);
-#pragma unroll
-            for (int v = 0; v < IL; ++v) {
-                P[v] = fmaf(cf.x, e[v], P[v]);
-                Q[v] = fmaf(cf.y, s[v], Q[v]);
+            for (int v = 0; v < NP; ++v) {
+                P[v] = __ffma2_rn(dd, e[v], P[v]);
+                Q[v] = __ffma2_rn(bb, s[v], Q[v]);
             }
 #pragma unroll
-            for (int v = 0; v < IL; ++v)
-                e[v] = fmaf(-ac[v], s[v], e[v]);
+            for (int v = 0; v < NP; ++v)
+                e[v] = __ffma2_rn(nac[v], s[v], e[v]);
 #pragma unroll
-            for (int v = 0; v < IL; ++v)
-                s[v] = fmaf(ac[v], e[v], s[v]);
+            for (int v = 0; v < NP; ++v)
+                s[v] = __ffma2_rn(ac[v], e[v], s[v]);
         }
     }
-    const float d = t[L].x;
+    const float4 cf = t[L];
+    const float2 dd = make_float2(cf.x, cf.y);
 #pragma unroll
-    for (int v = 0; v < IL; ++v)
-        P[v] = fmaf(d, e[v], P[v]);
+    for (int v = 0; v < NP; ++v)
+        P[v] = __ffma2_rn(dd, e[v], P[v]);
 }
 
 // Rotation form for one pair over one slab: A += sum alpha cos, B += sum beta sin.
-__device__ __forceinline__ void adj_rotate_slab(const float4 *t, int L, float s, float c, float sd,
-                                                float cd, float &A, float &B)
+__device__ __forceinline__ void adj_rotate_slab(const float4 *t, const float *ta, int L, float s,
+                                                float c, float sd, float cd, float &A, float &B)
 {
     for (int k = 0; k < L; ++k) {
-        const float4 cf = t[k];
-        A = fmaf(cf.z, c, A);
-        B = fmaf(cf.y, s, B);
+        A = fmaf(ta[k], c, A);
+        B = fmaf(t[k].z, s, B);
         const float sn = fmaf(c, sd, s * cd);
         const float cn = fmaf(-s, sd, c * cd);
         s = sn;
@@ -752,8 +760,9 @@ __device__ __forceinline__ void slab_seed(float q0, float r, float &s, float &c)
 }
 
 // Sums A (cosine side) and B (sine side) of one pair over all slabs.
-__device__ __forceinline__ void adj_pair_sums(const DebyeArgs &a, const float4 *tab, int n_slabs,
-                                              const AdjPair &p, float &A, float &B)
+__device__ __forceinline__ void adj_pair_sums(const DebyeArgs &a, const float4 *tab,
+                                              const float *tab_a, int n_slabs, const AdjPair &p,
+                                              float &A, float &B)
 {
     float P = 0.f, Q = 0.f;
     for (int sl = 0; sl < n_slabs; ++sl) {
@@ -766,64 +775,49 @@ __device__ __forceinline__ void adj_pair_sums(const DebyeArgs &a, const float4 *
             adj_circle_slab(t, L, s0, fmaf(c0, p.ch, s0 * p.sh), 2.0f * p.sh, P, Q);
         } else {
             const float sd = 2.0f * p.sh * p.ch, cd = fmaf(-2.0f * p.sh, p.sh, 1.0f);
-            adj_rotate_slab(t, L, s0, c0, sd, cd, P, Q);
+            adj_rotate_slab(t, tab_a + sl * kAdjStride, L, s0, c0, sd, cd, P, Q);
         }
     }
     A = p.circle ? P * (0.5f / p.ch) : P;
     B = Q;
 }
 
-__device__ __forceinline__ void adj_pair2_sums(const DebyeArgs &a, const float4 *tab, int n_slabs,
-                                               const AdjPair &p1, const AdjPair &p2, float &A1,
-                                               float &B1, float &A2, float &B2)
+// Sums of 2 NP pairs, all on the magic-circle form, stepped in NP float2
+// lanes (pairs 2v and 2v + 1 share lane v).
+template <int NP>
+__device__ __forceinline__ void adj_paired_sums(const DebyeArgs &a, const float4 *tab, int n_slabs,
+                                                const AdjPair (&p)[2 * NP], float (&A)[2 * NP],
+                                                float (&B)[2 * NP])
 {
-    float P1 = 0.f, Q1 = 0.f, P2 = 0.f, Q2 = 0.f;
-    for (int sl = 0; sl < n_slabs; ++sl) {
-        const int kb = sl * kAdjSlab;
-        const int L = (min(kAdjSlab, a.n_q - kb) + 7) & ~7;
-        const float4 *t = tab + sl * kAdjStride;
-        const float q0 = a.q[kb];
-        float s1, c1, s2, c2;
-        slab_seed(q0, p1.r, s1, c1);
-        slab_seed(q0, p2.r, s2, c2);
-        adj_circle_slab2(t, L, s1, fmaf(c1, p1.ch, s1 * p1.sh), 2.0f * p1.sh, s2,
-                         fmaf(c2, p2.ch, s2 * p2.sh), 2.0f * p2.sh, P1, Q1, P2, Q2);
-    }
-    A1 = P1 * (0.5f / p1.ch);
-    B1 = Q1;
-    A2 = P2 * (0.5f / p2.ch);
-    B2 = Q2;
-}
-
-template <int IL>
-__device__ __forceinline__ void adj_pairN_sums(const DebyeArgs &a, const float4 *tab, int n_slabs,
-                                               const AdjPair (&p)[IL], float (&A)[IL],
-                                               float (&B)[IL])
-{
-    float P[IL], Q[IL], ac[IL];
+    float2 P[NP], Q[NP], ac[NP];
 #pragma unroll
-    for (int v = 0; v < IL; ++v) {
-        P[v] = 0.f;
-        Q[v] = 0.f;
-        ac[v] = 2.0f * p[v].sh;
+    for (int v = 0; v < NP; ++v) {
+        P[v] = make_float2(0.f, 0.f);
+        Q[v] = make_float2(0.f, 0.f);
+        ac[v] = make_float2(2.0f * p[2 * v].sh, 2.0f * p[2 * v + 1].sh);
     }
     for (int sl = 0; sl < n_slabs; ++sl) {
         const int kb = sl * kAdjSlab;
         const int L = (min(kAdjSlab, a.n_q - kb) + 7) & ~7;
         const float q0 = a.q[kb];
-        float s[IL], e[IL];
+        float2 s[NP], e[NP];
 #pragma unroll
-        for (int v = 0; v < IL; ++v) {
-            float c;
-            slab_seed(q0, p[v].r, s[v], c);
-            e[v] = fmaf(c, p[v].ch, s[v] * p[v].sh);
+        for (int v = 0; v < NP; ++v) {
+            float s0, c0, s1, c1;
+            const AdjPair &p0 = p[2 * v], &p1 = p[2 * v + 1];
+            slab_seed(q0, p0.r, s0, c0);
+            slab_seed(q0, p1.r, s1, c1);
+            s[v] = make_float2(s0, s1);
+            e[v] = make_float2(fmaf(c0, p0.ch, s0 * p0.sh), fmaf(c1, p1.ch, s1 * p1.sh));
         }
-        adj_circle_slabN<IL>(tab + sl * kAdjStride, L, s, e, ac, P, Q);
+        adj_circle_slab_paired<NP>(tab + sl * kAdjStride, L, s, e, ac, P, Q);
     }
 #pragma unroll
-    for (int v = 0; v < IL; ++v) {
-        A[v] = P[v] * (0.5f / p[v].ch);
-        B[v] = Q[v];
+    for (int v = 0; v < NP; ++v) {
+        A[2 * v] = P[v].x * (0.5f / p[2 * v].ch);
+        A[2 * v + 1] = P[v].y * (0.5f / p[2 * v + 1].ch);
+        B[2 * v] = Q[v].x;
+        B[2 * v + 1] = Q[v].y;
     }
 }
 
@@ -857,7 +851,8 @@ __device__ __forceinline__ void adj_scatter(const AdjPair &p, float A, float B, 
 __host__ __device__ inline size_t adjoint_smem_bytes(int n_q, int qs, bool uniform, bool water)
 {
     if (uniform && !water)
-        return (size_t)((n_q + kAdjSlab - 1) / kAdjSlab) * kAdjStride * sizeof(float4);
+        return (size_t)((n_q + kAdjSlab - 1) / kAdjSlab) * kAdjStride *
+               (sizeof(float4) + sizeof(float));
     const int n_slabs = (n_q + qs - 1) / qs;
     return (size_t)n_slabs * qs * (water ? 8 : 4) * sizeof(float);
 }
@@ -880,7 +875,8 @@ __device__ __forceinline__ void adjoint_uniform_item(const DebyeArgs &a, int ite
     const int tj = a.blocks[it.bj_begin].type;
     const int n_slabs = (a.n_q + kAdjSlab - 1) / kAdjSlab;
     float4 *tab = s_dyn;
-    adjoint_uniform_table(a, tab, n_slabs, lambda, bi.type, tj);
+    float *tab_a = reinterpret_cast<float *>(s_dyn + n_slabs * kAdjStride);
+    adjoint_uniform_table(a, tab, tab_a, n_slabs, lambda, bi.type, tj);
 
     const int i = bi.start + tid;
     const bool valid_i = tid < bi.len;
@@ -910,11 +906,11 @@ __device__ __forceinline__ void adjoint_uniform_item(const DebyeArgs &a, int ite
                 }
                 float A[IL], B[IL];
                 if (all_circle) {
-                    adj_pairN_sums<IL>(a, tab, n_slabs, p, A, B);
+                    adj_paired_sums<IL / 2>(a, tab, n_slabs, p, A, B);
                 } else {
 #pragma unroll
                     for (int v = 0; v < IL; ++v)
-                        adj_pair_sums(a, tab, n_slabs, p[v], A[v], B[v]);
+                        adj_pair_sums(a, tab, tab_a, n_slabs, p[v], A[v], B[v]);
                 }
 #pragma unroll
                 for (int v = 0; v < IL; ++v)
@@ -923,23 +919,24 @@ __device__ __forceinline__ void adjoint_uniform_item(const DebyeArgs &a, int ite
             }
         }
         for (; jj + 1 < bj.len; jj += 2) {
-            const AdjPair p1 = adj_pair<SMALL>(pi, s_pos[jj], dq);
-            const AdjPair p2 = adj_pair<SMALL>(pi, s_pos[jj + 1], dq);
-            float A1, B1, A2, B2;
-            if (p1.circle && p2.circle) {
-                adj_pair2_sums(a, tab, n_slabs, p1, p2, A1, B1, A2, B2);
+            const AdjPair p2[2] = {adj_pair<SMALL>(pi, s_pos[jj], dq),
+                                   adj_pair<SMALL>(pi, s_pos[jj + 1], dq)};
+            float A[2], B[2];
+            if (p2[0].circle && p2[1].circle) {
+                adj_paired_sums<1>(a, tab, n_slabs, p2, A, B);
             } else {
-                adj_pair_sums(a, tab, n_slabs, p1, A1, B1);
-                adj_pair_sums(a, tab, n_slabs, p2, A2, B2);
+                adj_pair_sums(a, tab, tab_a, n_slabs, p2[0], A[0], B[0]);
+                adj_pair_sums(a, tab, tab_a, n_slabs, p2[1], A[1], B[1]);
             }
-            adj_scatter(p1, A1, B1, valid_i && (!diag || jj > tid), gi0, gi1, gi2, s_gj, jj, lane);
-            adj_scatter(p2, A2, B2, valid_i && (!diag || jj + 1 > tid), gi0, gi1, gi2, s_gj,
+            adj_scatter(p2[0], A[0], B[0], valid_i && (!diag || jj > tid), gi0, gi1, gi2, s_gj, jj,
+                        lane);
+            adj_scatter(p2[1], A[1], B[1], valid_i && (!diag || jj + 1 > tid), gi0, gi1, gi2, s_gj,
                         jj + 1, lane);
         }
         for (; jj < bj.len; ++jj) {
             const AdjPair p = adj_pair<SMALL>(pi, s_pos[jj], dq);
             float A, B;
-            adj_pair_sums(a, tab, n_slabs, p, A, B);
+            adj_pair_sums(a, tab, tab_a, n_slabs, p, A, B);
             adj_scatter(p, A, B, valid_i && (!diag || jj > tid), gi0, gi1, gi2, s_gj, jj, lane);
         }
         __syncthreads();

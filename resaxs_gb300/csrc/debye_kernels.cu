@@ -264,10 +264,10 @@ __global__ void __launch_bounds__(kBlockAtoms, QS <= 64 ? 3 : 2) delta_wide_kern
             s_fx[k] = (k < QS && k0 + k < a.n_q) ? a.ff[(size_t)(k0 + k) * a.n_types + tile.type]
                                                  : 0.f;
         __syncthreads();
-        float S[QP];
+        float2 S[QP / 2];
 #pragma unroll
-        for (int k = 0; k < QP; ++k)
-            S[k] = 0.f;
+        for (int m = 0; m < QP / 2; ++m)
+            S[m] = make_float2(0.f, 0.f);
         for (int jj = 0; jj < tile.len; ++jj) {
             const bool use = valid && s_idx[jj] != y;
             float rn, rninv, ro, roinv, dx, dy, dz;
@@ -275,14 +275,14 @@ __global__ void __launch_bounds__(kBlockAtoms, QS <= 64 ? 3 : 2) delta_wide_kern
             pair_r(py_old, s_old[jj], ro, roinv, dx, dy, dz);
             const WideSeed pn = wide_seed(q0, dq, rn, use ? mult * rninv : 0.f);
             const WideSeed po = wide_seed(q0, dq, ro, use ? -mult * roinv : 0.f);
-            wide_pair2<QS, QP>(pn, po, S);
+            wide_pair2<QS, QP / 2>(pn, po, S);
         }
 #pragma unroll
         for (int c = 0; c < NR; ++c) {
             float v[32];
 #pragma unroll
             for (int k = 0; k < 32; ++k)
-                v[k] = s_fx[32 * c + k] * S[32 * c + k];
+                v[k] = s_fx[32 * c + k] * pair_at(S, 32 * c + k);
             warp_reduce_scatter<32>(v, lane);
             acc[c] += (double)v[0];
         }
@@ -378,7 +378,7 @@ static cudaError_t wide_launch(DebyeArgs a, int k_base, int n_slabs, cudaStream_
 {
     a.k_base = k_base;
     const dim3 grid(a.n_items, n_slabs);
-    if (a.small_theta)
+    if (a.small_theta >= 2)
         forward_wide_kernel<QS, 2, false><<<grid, kBlockAtoms, 0, st>>>(a);
     else
         forward_wide_kernel<QS, 2, true><<<grid, kBlockAtoms, 0, st>>>(a);
@@ -641,7 +641,7 @@ static cudaError_t adjoint_qs(const DebyeArgs &a, bool uniform, bool water, cuda
         if (e == cudaSuccess)                                                              \
             kfn<<<grid, kBlockAtoms, smem, st>>>(a, n_slabs);                              \
     } while (0)
-    if (uniform && !water && a.small_theta)
+    if (uniform && !water && a.small_theta >= 1)
         RSX_ADJ_SMALL();
     else if (uniform && !water)
         RSX_ADJ(true, false);

@@ -35,7 +35,7 @@ struct rsx_batch {
     std::vector<int> sizes, offsets; // caller layout of the concatenated bodies
     bool uniform = false;
     float dq = 0.f;
-    int small_theta = 0; // flag the captured graphs were built with
+    int small_theta = 0; // theta_level() the captured graphs were built with
     int q_slab = 64;
     bool autotune = false, tuned = false;
 
@@ -405,10 +405,7 @@ rsx_status stage_bodies(rsx_batch *h, const rsx_body *bodies)
             worst = std::max(worst, std::sqrt(d2));
         }
     }
-    const int small = (h->uniform && std::isfinite(worst) &&
-                       std::fabs((double)h->dq) * worst * 1.0001 <= 1.4)
-                          ? 1
-                          : 0;
+    const int small = theta_level(h->uniform, (double)h->dq, worst);
     if (small != h->small_theta) {
         drop_graphs(h);
         h->small_theta = small;

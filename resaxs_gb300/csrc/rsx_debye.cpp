@@ -354,8 +354,8 @@ void grow_extent(rsx_debye *h, const rsx_body *b, unsigned n)
     }
 }
 
-// 1 when every pair has |theta/2| = |dq r / 2| <= 0.7 < pi/4 (the seeds may
-// then skip the range reduction; the result is the same bit for bit).
+// theta_level() of the tracked bounding box (the seeds may skip the range
+// reduction where it allows; the result is the same bit for bit).
 int small_theta(const rsx_debye *h)
 {
     if (!h->uniform || h->n < 2)
@@ -367,7 +367,7 @@ int small_theta(const rsx_debye *h)
             return 0;
         d2 += e * e;
     }
-    return std::fabs((double)h->dq) * std::sqrt(d2) * 1.0001 <= 1.4 ? 1 : 0;
+    return theta_level(true, (double)h->dq, std::sqrt(d2));
 }
 
 DebyeArgs debye_args(rsx_debye *h)

@@ -21,6 +21,21 @@ struct PairItem {
     int bi, bj_begin, bj_end, pad;
 };
 
+// How small the step angle theta = dq r is guaranteed to be for every pair
+// of a uniform grid with step dq over bodies whose bounding-box diagonal is
+// `diag` (an upper bound of every pair distance):
+//   2: |theta| <= 0.7 < pi/4 (the paired-step seeds of the forward skip the
+//      range reduction, and every pair takes the unsigned form);
+//   1: |theta / 2| <= 0.7 (the half-angle seeds of the adjoint skip it);
+//   0: neither (or not a uniform grid).
+inline int theta_level(bool uniform, double dq, double diag)
+{
+    if (!uniform || !(diag >= 0.0) || !(diag < 1e30))
+        return 0;
+    const double t = (dq < 0.0 ? -dq : dq) * diag * 1.0001;
+    return t <= 0.7 ? 2 : (t <= 1.4 ? 1 : 0);
+}
+
 // Arguments of the Debye pair kernels (forward and adjoint).
 struct DebyeArgs {
     const float4 *pos;       // bodies in type-sorted order, .w = type bits
@@ -33,7 +48,7 @@ struct DebyeArgs {
     int n, n_q, n_types, n_items;
     int k_base;              // first q index of the launch (set by the launcher)
     float dq;                // uniform q step (rotation path)
-    int small_theta;         // 1: dq * (largest pair distance) <= 1.4, so |theta/2| < pi/4
+    int small_theta;         // theta_level() of the launch's bodies
     float water_weight;      // w (water path)
     int water_index;         // column of the water factor
     // adjoint
