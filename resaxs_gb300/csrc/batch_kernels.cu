@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(kBlockAtoms, (QS <= 64 || !SIGNED) ? 3 : 2)
 }
 
 template <int QS, bool UNIFORM, bool SMALL = false>
-__global__ void __launch_bounds__(kBlockAtoms)
+__global__ void __launch_bounds__(kBlockAtoms, UNIFORM ? 4 : 1)
     batch_adjoint_kernel(const DebyeArgs a, const int *work_order, int n_units, int n_slabs,
                          int *counter)
 {

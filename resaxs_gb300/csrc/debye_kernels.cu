@@ -321,8 +321,10 @@ __global__ void f64_to_f32_kernel(const double *src, float *dst, int n)
 // a pair is complete before it is scattered.
 // ----------------------------------------------------------------------------
 
+// The uniform form: 4 CTAs per SM (8 pairs per thread step need 128 registers).
 template <int QS, bool UNIFORM, bool WATER, bool SMALL = false>
-__global__ void __launch_bounds__(kBlockAtoms) adjoint_kernel(const DebyeArgs a, int n_slabs)
+__global__ void __launch_bounds__(kBlockAtoms, (UNIFORM && !WATER) ? 4 : 1)
+    adjoint_kernel(const DebyeArgs a, int n_slabs)
 {
     adjoint_item<QS, UNIFORM, WATER, SMALL>(a, blockIdx.x, n_slabs);
 }
