@@ -71,6 +71,12 @@ rsx_status rsx_debug_layout(const rsx_body *bodies, int n_bodies, int n_factors,
                             int min_adj_items, int *n_blocks, int *n_items, int *n_adj_items,
                             int *pairs_covered_ok);
 
+/* Host-only view of the small-angle level the kernels are chosen by, for a
+ * q grid (uniform or not) with step dq over bodies whose bounding-box
+ * diagonal is diag: 2 when |dq| * diag * 1.0001 <= 0.7 (|theta| < pi/4 for
+ * every pair), 1 when it is <= 1.4 (|theta / 2| < pi/4), else 0. */
+int rsx_debug_theta_level(int uniform, double dq, double diag);
+
 /* Host-only view of the slab plan of the wide uniform kernels for n_q q and
  * q_slab 64 or 128: out[0..4] = main slab width, number of main slabs, first
  * q of the remainder slab, q it covers, width of its kernel (0: none). */

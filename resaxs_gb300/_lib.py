@@ -79,6 +79,7 @@ SIGNATURES = [
     ("rsx_debye_set_water", _st, [_vp, ctypes.c_float, _i, _vp]),
     ("rsx_debye_calc", _st, [_vp, _f32p, _f32p]),
     ("rsx_debye_calc_shard", _st, [_vp, _f32p, _i, _i, _f64p]),
+    ("rsx_debug_theta_level", _i, [_i, ctypes.c_double, ctypes.c_double]),
     ("rsx_debug_wide_plan", _st, [_i, _i, np.ctypeslib.ndpointer(np.int32)]),
     ("rsx_debug_shard_items", _st, [_f32p, _i, _i, _i, _i, np.ctypeslib.ndpointer(np.int32),
                                     _vp]),

@@ -869,6 +869,11 @@ rsx_status rsx_debye_calc_shard(rsx_debye *h, const rsx_body *bodies, int shard,
     return ok();
 }
 
+int rsx_debug_theta_level(int uniform, double dq, double diag)
+{
+    return theta_level(uniform != 0, dq, diag);
+}
+
 rsx_status rsx_debug_wide_plan(int n_q, int q_slab, int *out)
 {
     if (n_q <= 0 || !out || (q_slab != 64 && q_slab != 128))

@@ -125,3 +125,19 @@ def test_wide_slab_plan_covers_every_q(librsx):
                 assert tail_w == 0
     assert librsx.rsx_debug_wide_plan(0, 128, out) == _lib.RSX_INVALID_ARG
     assert librsx.rsx_debug_wide_plan(10, 32, out) == _lib.RSX_INVALID_ARG
+
+
+def test_theta_level_thresholds(librsx):
+    """The small-angle level that picks the kernel instantiations: 2 up to
+    |dq| * diagonal * 1.0001 = 0.7, 1 up to 1.4, else 0; never above 0 for a
+    non-uniform grid or a non-finite extent."""
+    lv = librsx.rsx_debug_theta_level
+    dq = 0.0025
+    for diag, want in ((0.0, 2), (100.0, 2), (279.9, 2), (280.1, 1), (400.0, 1), (559.9, 1),
+                       (560.1, 0), (900.0, 0)):
+        assert lv(1, dq, diag) == want, (diag, want)
+        assert lv(1, -dq, diag) == want, (diag, want)
+        assert lv(0, dq, diag) == 0
+    assert lv(1, dq, float("inf")) == 0
+    assert lv(1, dq, float("nan")) == 0
+    assert lv(1, dq, -1.0) == 0

@@ -34,6 +34,30 @@ def test_backward_vs_fp64_gradient(S, oracle_lib, idx, n):
     assert e_norm < 2e-5 and e_max < 1e-4, (e_norm, e_max)
 
 
+@pytest.mark.parametrize("diag", [150.0, 400.0, 700.0, 1500.0])
+def test_backward_on_every_small_theta_level(S, oracle_lib, diag):
+    """dq = 0.6/255: the adjoint's reduction-free half-angle seeds hold up to
+    a box diagonal of 595 A; beyond 668 A the far body's pairs have
+    theta > pi/2 and take the rotation form.  One body of a compact structure
+    is placed so that the diagonal is `diag`; the gradient must match the
+    FP64 analytic gradient in every case."""
+    w = W.make_config(3, seed=35, n_override=500)
+    b = w.bodies.copy()
+    lo = b[1:, :3].min(0)
+    hi = b[1:, :3].max(0)
+    rest = float(np.sum((hi[1:] - lo[1:]) ** 2))
+    b[0, 0] = np.float32(lo[0] + np.sqrt(diag * diag - rest))
+    b[0, 1:3] = lo[1:]
+    rng = np.random.default_rng(int(diag))
+    lam = rng.normal(size=len(w.q)).astype(np.float32)
+    with S.Debye(w.q, w.ff, w.n) as d:
+        d.calc(b)
+        g = d.backward(lam, f64=True)
+    ref = oracle_lib.debye_grad_f64(w.q, lam.astype(np.float64), b, w.ff)
+    e_norm, e_max = grad_err(g, ref)
+    assert e_norm < 2e-5 and e_max < 1e-4, (e_norm, e_max)
+
+
 def test_backward_general_q_and_water(S, oracle_lib):
     w = W.make_config(1, seed=32, n_override=400)
     rng = np.random.default_rng(5)

@@ -73,6 +73,32 @@ def test_seed_paths_both_sides_of_the_small_theta_bound(saxs, oracle_lib):
         assert rel(out64, oracle_lib.debye_f64(w.q, bodies, w.ff)) < TOL
 
 
+@pytest.mark.parametrize("diag,level", [(150.0, 2), (279.0, 2), (281.0, 1), (400.0, 1),
+                                        (559.0, 1), (561.0, 0), (900.0, 0)])
+def test_forward_on_every_small_theta_level(saxs, oracle_lib, diag, level):
+    """The forward picks its instantiation from the bounding box: plain
+    paired steps with reduction-free seeds (|theta| < pi/4 for every pair),
+    or the signed steps with range-reduced seeds.  One body of a compact
+    structure is placed so that the box diagonal lands on each side of both
+    thresholds (dq = 0.0025: 280 and 560 A); every case must match the
+    oracle, including the pairs of the far body."""
+    from resaxs_gb300 import _lib
+    w = W.make_config(2, seed=37, n_override=800)
+    b = w.bodies.copy()
+    lo = b[1:, :3].min(0)
+    hi = b[1:, :3].max(0)
+    # body 0 on the far side of the box's x extent so that the diagonal is `diag`
+    rest = float(np.sum((hi[1:] - lo[1:]) ** 2))
+    b[0, 0] = np.float32(lo[0] + np.sqrt(diag * diag - rest))
+    b[0, 1:3] = lo[1:]
+    ext = b[:, :3].max(0).astype(np.float64) - b[:, :3].min(0).astype(np.float64)
+    dq = float(w.q[1] - w.q[0])
+    assert _lib.lib().rsx_debug_theta_level(1, dq, float(np.sqrt(np.sum(ext ** 2)))) == level
+    _, out64, cfg = gpu_curve(saxs, w.q, w.ff, b)
+    assert cfg["uniform_q"]
+    assert rel(out64, oracle_lib.debye_f64(w.q, b, w.ff)) < TOL
+
+
 def test_forward_general_q_path(saxs, oracle_lib):
     w = W.make_config(2, seed=13, n_override=800)
     rng = np.random.default_rng(3)
