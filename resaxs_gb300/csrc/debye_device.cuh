@@ -345,9 +345,9 @@ __device__ __forceinline__ float pair_at(const float2 (&S)[QH], int k)
 
 // Forward pair sums of one work item for q values [k0, k0 + QS) on a uniform
 // grid without water; writes partial[k][item_idx] as forward_item does.
-// SIGNED = false: the launch promises small theta (every pair has
-// |theta/2| < pi/4, so every sign is +1), and the pair loop keeps only the
-// plain adds.
+// SIGNED = false: the launch promises small theta (small_theta level 2: every
+// pair has |theta| < pi/4, so every sign is +1), and the pair loop keeps only
+// the plain adds.
 template <int QS, int IL, bool SIGNED = true>
 __device__ __forceinline__ void forward_wide_item(const DebyeArgs &a, int item_idx, int k0)
 {

@@ -13,7 +13,9 @@
 //    (3 FP32 ops per pair*q with the accumulation), seeded per pair and slab
 //    from the range-reduced FP32 sin/cos of rsx_math.cuh; the wide kernels
 //    (forward_wide_kernel, delta_wide_kernel) run 64..128 q per seed following
-//    the slab plan of wide_plan().  Non-uniform grids and water use
+//    the slab plan of wide_plan(), with the even and odd q of a slab as two
+//    sequences of step 2 theta packed in float2 lanes, so that each FP32x2
+//    instruction advances both.  Non-uniform grids and water use
 //    forward_kernel / delta_kernel (8..32 q per slab, sin/cos per pair*q).
 //    sinc(q r) = (sin(q r)/r) / q: the 1/q factor is applied once per q in FP64
 //    when the curve is assembled.
@@ -21,7 +23,8 @@
 //    warp into FP64 (wide kernels) or folded into a Kahan accumulator per q
 //    (general kernels).  Across warps and CTAs: FP64.
 //  * The adjoint steps sin and cos(q r - theta/2) together (the magic-circle
-//    form) and sums both sides of every pair's gradient; see debye_device.cuh.
+//    form, two pairs per FP32x2 instruction) and sums both sides of every
+//    pair's gradient; see debye_device.cuh.
 #include "debye_device.cuh"
 
 #include <algorithm>
@@ -371,10 +374,10 @@ static cudaError_t forward_dispatch(const DebyeArgs &a, int qs, int k_base, int 
     }
 }
 
-// Occupancy: the plain (small-theta) instantiations fit in 168 registers up
-// to 128 q, so 3 CTAs (12 warps) share an SM and hide the seed latency (6 %
-// faster than 2 CTAs with 4 pairs per step at 201 q); the signed ones keep 2
-// CTAs/SM above 64 q.  Both step 2 pairs at a time.
+// Occupancy: the plain instantiations (small_theta level 2) fit in 168
+// registers up to 128 q, so 3 CTAs (12 warps) share an SM and hide the seed
+// latency (6 % faster than 2 CTAs with 4 pairs per step at 201 q); the signed
+// ones keep 2 CTAs/SM above 64 q.  Both step 2 pairs at a time.
 template <int QS>
 static cudaError_t wide_launch(DebyeArgs a, int k_base, int n_slabs, cudaStream_t st)
 {
