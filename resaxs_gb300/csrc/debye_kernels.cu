@@ -101,11 +101,29 @@ __global__ void __launch_bounds__(256) assemble_kernel(const AssembleArgs a)
 // incremental: delta of the cross sum when the moved list changes position
 // ----------------------------------------------------------------------------
 
+// Slot in the moved list of this thread's body of static block `by` (-1:
+// static or past the block), found by scanning the moved list into shared
+// memory (k <= n / 3 on this path; the indices are distinct).  No device
+// state outlives the step.
+__device__ __forceinline__ int moved_slot_of(const DeltaArgs &a, const BlockDesc &by, int *s_slot)
+{
+    const int tid = threadIdx.x;
+    s_slot[tid] = -1;
+    __syncthreads();
+    for (int m = tid; m < a.k; m += kBlockAtoms) {
+        const int i = a.moved_idx[m] - by.start;
+        if (i >= 0 && i < by.len)
+            s_slot[i] = m;
+    }
+    __syncthreads();
+    return tid < by.len ? s_slot[tid] : -1;
+}
+
 template <int QS, bool UNIFORM>
 __global__ void __launch_bounds__(kBlockAtoms) delta_kernel(const DeltaArgs a)
 {
     __shared__ float4 s_new[kBlockAtoms], s_old[kBlockAtoms];
-    __shared__ int s_idx[kBlockAtoms];
+    __shared__ int s_idx[kBlockAtoms], s_slot[kBlockAtoms];
     __shared__ float s_q[QS], s_fy[QS], s_fx[QS];
     __shared__ double s_red[kBlockAtoms / 32][QS];
 
@@ -121,7 +139,7 @@ __global__ void __launch_bounds__(kBlockAtoms) delta_kernel(const DeltaArgs a)
     const int y = by.start + tid;
     const bool valid = tid < by.len;
     const float4 py_old = valid ? a.pos_old[y] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const int slot = valid ? a.moved_slot[y] : -1;
+    const int slot = moved_slot_of(a, by, s_slot);
     const float4 py_new = slot >= 0 ? a.moved_new[slot] : py_old;
     // pairs with a static body are met once (weight 1); pairs inside the moved
     // list are met from both ends (weight 1/2 each)
@@ -202,20 +220,13 @@ __global__ void __launch_bounds__(kBlockAtoms) delta_kernel(const DeltaArgs a)
     }
 }
 
+// After a delta step: the moved bodies take their new positions.
 __global__ void apply_moves_kernel(float4 *pos, const float4 *moved_new, const int *moved_idx,
                                    int k)
 {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m < k)
         pos[moved_idx[m]] = moved_new[m];
-}
-
-// slot[idx[m]] = m (set) or -1 (clear) for the moved list
-__global__ void mark_moved_kernel(int *slot, const int *moved_idx, int k, int set)
-{
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m < k)
-        slot[moved_idx[m]] = set ? m : -1;
 }
 
 // Incremental delta on a uniform grid with wide slabs: as delta_kernel, but
@@ -228,7 +239,7 @@ __global__ void __launch_bounds__(kBlockAtoms, QS <= 64 ? 3 : 2) delta_wide_kern
 {
     constexpr int QP = WideSlab<QS>::QP, NR = WideSlab<QS>::NR;
     __shared__ float4 s_new[kBlockAtoms], s_old[kBlockAtoms];
-    __shared__ int s_idx[kBlockAtoms];
+    __shared__ int s_idx[kBlockAtoms], s_slot[kBlockAtoms];
     __shared__ float s_fx[QP];
     __shared__ double s_red[kBlockAtoms / 32][QP];
 
@@ -241,7 +252,7 @@ __global__ void __launch_bounds__(kBlockAtoms, QS <= 64 ? 3 : 2) delta_wide_kern
     const int y = by.start + tid;
     const bool valid = tid < by.len;
     const float4 py_old = valid ? a.pos_old[y] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const int slot = valid ? a.moved_slot[y] : -1;
+    const int slot = moved_slot_of(a, by, s_slot);
     const float4 py_new = slot >= 0 ? a.moved_new[slot] : py_old;
     // pairs with a static body are met once (weight 1); pairs inside the moved
     // list are met from both ends (weight 1/2 each)
@@ -599,15 +610,6 @@ cudaError_t launch_apply_moves(float4 *pos, const float4 *moved_new, const int *
     if (k == 0)
         return cudaSuccess;
     apply_moves_kernel<<<(k + 255) / 256, 256, 0, st>>>(pos, moved_new, moved_idx, k);
-    count_launch();
-    return cudaGetLastError();
-}
-
-cudaError_t launch_mark_moved(int *slot, const int *moved_idx, int k, int set, cudaStream_t st)
-{
-    if (k == 0)
-        return cudaSuccess;
-    mark_moved_kernel<<<(k + 255) / 256, 256, 0, st>>>(slot, moved_idx, k, set);
     count_launch();
     return cudaGetLastError();
 }

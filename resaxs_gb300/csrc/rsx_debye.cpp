@@ -200,7 +200,6 @@ struct rsx_debye {
     // incremental
     unsigned char *d_moved = nullptr; // packed moved_new | moved_idx | tiles
     size_t moved_cap = 0;
-    int *d_slot = nullptr;
     // adjoint
     double *d_grad = nullptr;
     float *d_lambda = nullptr;
@@ -598,7 +597,6 @@ rsx_status delta_update(rsx_debye *h, const rsx_body *moved, const unsigned *idx
     a.pos_old = h->d_pos;
     a.moved_new = reinterpret_cast<const float4 *>(h->d_moved);
     a.moved_idx = reinterpret_cast<const int *>(h->d_moved + off_idx);
-    a.moved_slot = h->d_slot;
     a.blocks = h->d_blocks;
     a.mtiles = reinterpret_cast<const BlockDesc *>(h->d_moved + off_tiles);
     a.ff = h->d_ff;
@@ -613,7 +611,6 @@ rsx_status delta_update(rsx_debye *h, const rsx_body *moved, const unsigned *idx
     a.max_groups = kDeltaGroups;
     a.dq = h->dq;
     int *d_idx = reinterpret_cast<int *>(h->d_moved + off_idx);
-    RSX_LAUNCH(launch_mark_moved(h->d_slot, d_idx, (int)k, 1, h->st), "mark moved");
     if (h->timing)
         RSX_TRY_CUDA(cudaEventRecord(h->ev_k0, h->st), "event");
     RSX_LAUNCH(launch_delta(a, slab_for(h), h->uniform, h->st), "delta kernel");
@@ -623,7 +620,6 @@ rsx_status delta_update(rsx_debye *h, const rsx_body *moved, const unsigned *idx
                                h->st),
                "assemble delta");
     RSX_LAUNCH(launch_apply_moves(h->d_pos, a.moved_new, d_idx, (int)k, h->st), "apply moves");
-    RSX_LAUNCH(launch_mark_moved(h->d_slot, d_idx, (int)k, 0, h->st), "unmark moved");
     return RSX_OK;
 }
 
@@ -672,8 +668,8 @@ rsx_status release(rsx_debye *h)
     void *dev[] = {h->d_pos,        h->d_pos_saved, h->d_rsasa,      h->d_ff,
                    h->d_q,          h->d_blocks,    h->d_items,      h->d_adj_items,
                    h->d_partial,    h->d_iq64,      h->d_iq64_saved, h->d_iq32,
-                   h->d_type_count, h->d_rsasa_sum, h->d_moved,      h->d_slot,
-                   h->d_grad,       h->d_lambda};
+                   h->d_type_count, h->d_rsasa_sum, h->d_moved,      h->d_grad,
+                   h->d_lambda};
     for (void *p : dev)
         dev_free(p);
     void *pinned[] = {h->h_pos, h->h_iq, h->h_iq64, h->h_grad, h->h_moved, h->h_rsasa};
@@ -768,7 +764,6 @@ rsx_status rsx_debye_create(const float *q, int n_q, const float *t_factors, int
     RSX_ALLOC(h->d_iq32, sizeof(float) * n_q, "curve f32");
     RSX_ALLOC(h->d_type_count, sizeof(int) * n_factors, "type counts");
     RSX_ALLOC(h->d_rsasa_sum, sizeof(double) * n_factors, "rsasa sums");
-    RSX_ALLOC(h->d_slot, sizeof(int) * n, "moved slots");
     RSX_ALLOC(h->d_grad, sizeof(double) * 3 * n, "gradient");
     RSX_ALLOC(h->d_lambda, sizeof(float) * n_q, "lambda");
     RSX_PIN(h->h_pos, sizeof(float4) * n, "pinned bodies");
@@ -779,8 +774,6 @@ rsx_status rsx_debye_create(const float *q, int n_q, const float *t_factors, int
 #undef RSX_ALLOC
 #undef RSX_PIN
     e = cudaMemcpyAsync(h->d_q, h->q.data(), sizeof(float) * n_q, cudaMemcpyHostToDevice, h->st);
-    if (e == cudaSuccess)
-        e = cudaMemsetAsync(h->d_slot, 0xff, sizeof(int) * n, h->st); // -1 everywhere
     if (e == cudaSuccess)
         e = cudaMemsetAsync(h->d_iq64, 0, sizeof(double) * n_q, h->st);
     if (e == cudaSuccess)

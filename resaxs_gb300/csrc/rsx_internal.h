@@ -79,7 +79,6 @@ struct DeltaArgs {
     const float4 *pos_old;   // [n] sorted positions before the move
     const float4 *moved_new; // [k] new positions of the moved bodies, grouped by type
     const int *moved_idx;    // [k] sorted index of each moved body
-    const int *moved_slot;   // [n] slot in the moved list, -1 for static bodies
     const BlockDesc *blocks; // [n_blocks] static-side blocks
     const BlockDesc *mtiles; // [n_mtiles] moved-list tiles (start/len into the list, type)
     const float *ff, *q;
@@ -110,7 +109,6 @@ int delta_parts(const DeltaArgs &a, int q_slab, bool uniform);
 int delta_groups(const DeltaArgs &a);
 cudaError_t launch_apply_moves(float4 *pos, const float4 *moved_new, const int *moved_idx,
                                int k, cudaStream_t st);
-cudaError_t launch_mark_moved(int *slot, const int *moved_idx, int k, int set, cudaStream_t st);
 cudaError_t launch_f64_to_f32(const double *src, float *dst, int n, cudaStream_t st);
 cudaError_t launch_adjoint(const DebyeArgs &a, int q_slab, bool uniform, bool water,
                            cudaStream_t st);
