@@ -563,10 +563,25 @@ rsx_status delta_update(rsx_debye *h, const rsx_body *moved, const unsigned *idx
         for (unsigned m = 0; m < k; ++m)
             order[fill[type_of(moved[m])]++] = (int)m;
     }
+    // Each type's run is cut into near-equal tiles of at most max(8, k / G)
+    // bodies (G = kDeltaGroups moved-list groups of the wide kernel), longest
+    // first, so that the groups get similar shares of a small moved list.
     std::vector<BlockDesc> tiles;
-    for (int t = 0; t < h->n_types; ++t)
-        for (int s = cnt[t]; s < cnt[t + 1]; s += kBlockAtoms)
-            tiles.push_back(BlockDesc{s, std::min(kBlockAtoms, cnt[t + 1] - s), t, 0});
+    const int cap = std::min(kBlockAtoms,
+                             std::max(8, (int)((k + kDeltaGroups - 1) / kDeltaGroups)));
+    for (int t = 0; t < h->n_types; ++t) {
+        const int c = cnt[t + 1] - cnt[t];
+        if (c == 0)
+            continue;
+        const int nt = (c + cap - 1) / cap, base = c / nt, extra = c % nt;
+        for (int j = 0, s = cnt[t]; j < nt; ++j) {
+            const int len = base + (j < extra ? 1 : 0);
+            tiles.push_back(BlockDesc{s, len, t, 0});
+            s += len;
+        }
+    }
+    std::stable_sort(tiles.begin(), tiles.end(),
+                     [](const BlockDesc &x, const BlockDesc &y) { return x.len > y.len; });
     const size_t off_idx = sizeof(float4) * k;
     const size_t off_tiles = (off_idx + sizeof(int) * k + 15) & ~size_t(15);
     const size_t bytes = off_tiles + sizeof(BlockDesc) * tiles.size();
