@@ -371,12 +371,35 @@ rsx_status capture(rsx_batch *h, bool with_adjoint, cudaGraphExec_t *out)
 
 rsx_status stage_bodies(rsx_batch *h, const rsx_body *bodies)
 {
-    for (int i = 0; i < h->n_total; ++i)
-        if (btype(bodies[i]) >= (unsigned)h->n_types)
-            return fail(RSX_INVALID_ARG, "body " + std::to_string(i) + " has a factor index >= n_factors");
+    // One sequential pass: factor indices, whether the type layout is the one
+    // the graphs were built for, and each member's bounding box (min and max
+    // of floats are exact; the diagonal is formed in double).
     bool same = h->have_layout;
-    for (int i = 0; i < h->n_total && same; ++i)
-        same = btype(bodies[i]) == h->types[i];
+    double worst = 0.0;
+    for (int m = 0; m < h->n_members; ++m) {
+        float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+        const int end = h->offsets[m] + h->sizes[m];
+        for (int i = h->offsets[m]; i < end; ++i) {
+            const rsx_body &b = bodies[i];
+            const unsigned t = btype(b);
+            if (t >= (unsigned)h->n_types)
+                return fail(RSX_INVALID_ARG,
+                            "body " + std::to_string(i) + " has a factor index >= n_factors");
+            same = same && t == h->types[i];
+            lo[0] = std::min(lo[0], b.x);
+            hi[0] = std::max(hi[0], b.x);
+            lo[1] = std::min(lo[1], b.y);
+            hi[1] = std::max(hi[1], b.y);
+            lo[2] = std::min(lo[2], b.z);
+            hi[2] = std::max(hi[2], b.z);
+        }
+        if (h->sizes[m] > 1) {
+            double d2 = 0.0;
+            for (int d = 0; d < 3; ++d)
+                d2 += ((double)hi[d] - lo[d]) * ((double)hi[d] - lo[d]);
+            worst = std::max(worst, std::sqrt(d2));
+        }
+    }
     if (!same)
         RSX_TRY(build_batch_layout(h, bodies));
     RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "batch staging");
@@ -384,27 +407,10 @@ rsx_status stage_bodies(rsx_batch *h, const rsx_body *bodies)
         const rsx_body &b = bodies[h->perm[s]];
         h->h_pos[s] = make_float4(b.x, b.y, b.z, b.w);
     }
-    // 1 when every member's pairs have |theta/2| = |dq r / 2| <= 0.7 < pi/4:
-    // the seeds may skip the range reduction (same results bit for bit).  The
-    // flag is a kernel argument of the captured graphs, so they are captured
-    // again when it changes.
-    double worst = 0.0;
-    for (int m = 0; m < h->n_members; ++m) {
-        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-        for (int i = h->offsets[m]; i < h->offsets[m] + h->sizes[m]; ++i) {
-            const double x[3] = {bodies[i].x, bodies[i].y, bodies[i].z};
-            for (int d = 0; d < 3; ++d) {
-                lo[d] = std::min(lo[d], x[d]);
-                hi[d] = std::max(hi[d], x[d]);
-            }
-        }
-        if (h->sizes[m] > 1) {
-            double d2 = 0.0;
-            for (int d = 0; d < 3; ++d)
-                d2 += (hi[d] - lo[d]) * (hi[d] - lo[d]);
-            worst = std::max(worst, std::sqrt(d2));
-        }
-    }
+    // theta_level() of the widest member selects the kernel instantiations
+    // (the reduction-free seeds give the same results bit for bit).  It is a
+    // kernel argument of the captured graphs, so they are captured again when
+    // it changes.
     const int small = theta_level(h->uniform, (double)h->dq, worst);
     if (small != h->small_theta) {
         drop_graphs(h);
