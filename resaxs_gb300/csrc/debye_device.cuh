@@ -449,6 +449,188 @@ __device__ __forceinline__ void forward_wide_item(const DebyeArgs &a, int item_i
     }
 }
 
+// ----------------------------------------------------------------------------
+// forward, uniform q grid with the implicit water term: wide slabs
+// ----------------------------------------------------------------------------
+//
+// With water every body's factor is f~_b(q) = f_t(q) + w rsasa_b f_w(q), so a
+// pair term is f~_i f~_j sin(q r)/r.  Per J-block a thread accumulates
+// U(q) = sum_j f~_j(q) sin(q r_ij)/r_ij: the coefficient of pair j at q 2m and
+// 2m + 1 is one FP32x2 FMA from a per-item table row (f_tj and w f_w at both
+// q) and the pair's rsasa, and the sum one more, so a pair*q costs 4 FP32
+// lane-ops with the recurrence.  f~_i(q) multiplies U once per J-block,
+// before the warp reduce-scatter (it differs from lane to lane).
+
+// Two pairs with their rsasa values ra, rb; fq[m] = (f_tj(q_2m), f_tj(q_2m+1),
+// w f_w(q_2m), w f_w(q_2m+1)).  SIGNED multiplies the odd steps' coefficients
+// by the pairs' signs.
+template <int QS, int QH, bool SIGNED>
+__device__ __forceinline__ void wide_water_pair2_body(const WideSeed &a, const WideSeed &b,
+                                                      float ra, float rb, const float4 *fq,
+                                                      float2 (&S)[QH])
+{
+    float2 sa = a.s, da = a.d, sb = b.s, db = b.d;
+    const float2 la = splat2(a.l), lb = splat2(b.l), rsa = splat2(ra), rsb = splat2(rb);
+#pragma unroll
+    for (int m = 0; m < QS / 2; ++m) {
+        const float4 f = fq[m];
+        const float2 fj = make_float2(f.x, f.y), fw = make_float2(f.z, f.w);
+        float2 ca = __ffma2_rn(fw, rsa, fj), cb = __ffma2_rn(fw, rsb, fj);
+        if (SIGNED && (m & 1)) {
+            ca = __fmul2_rn(splat2(a.sg), ca);
+            cb = __fmul2_rn(splat2(b.sg), cb);
+        }
+        S[m] = __ffma2_rn(ca, sa, __ffma2_rn(cb, sb, S[m]));
+        da = __ffma2_rn(la, sa, da);
+        db = __ffma2_rn(lb, sb, db);
+        sa = __fadd2_rn(sa, da);
+        sb = __fadd2_rn(sb, db);
+    }
+}
+
+template <int QS, int QH>
+__device__ __forceinline__ void wide_water_pair2(const WideSeed &a, const WideSeed &b, float ra,
+                                                 float rb, const float4 *fq, float2 (&S)[QH])
+{
+    if (__any_sync(0xffffffffu, a.sg < 0.f || b.sg < 0.f))
+        wide_water_pair2_body<QS, QH, true>(a, b, ra, rb, fq, S);
+    else
+        wide_water_pair2_body<QS, QH, false>(a, b, ra, rb, fq, S);
+}
+
+template <int QS, int QH>
+__device__ __forceinline__ void wide_water_pair1(const WideSeed &p, float rp, const float4 *fq,
+                                                 float2 (&S)[QH])
+{
+    float2 s = p.s, d = p.d;
+    const float2 l = splat2(p.l), rs = splat2(rp);
+#pragma unroll
+    for (int m = 0; m < QS / 2; ++m) {
+        const float4 f = fq[m];
+        float2 c = __ffma2_rn(make_float2(f.z, f.w), rs, make_float2(f.x, f.y));
+        if (m & 1)
+            c = __fmul2_rn(splat2(p.sg), c);
+        S[m] = __ffma2_rn(c, s, S[m]);
+        d = __ffma2_rn(l, s, d);
+        s = __fadd2_rn(s, d);
+    }
+}
+
+// Forward pair sums with water of one work item for q values [k0, k0 + QS) on
+// a uniform grid; writes partial[k][item_idx] = sum over the item's pairs of
+// f~_i f~_j sin(q_k r)/r (the factors included, as forward_item<QS, U, true>
+// does).  SIGNED as in forward_wide_item.
+template <int QS, bool SIGNED = true>
+__device__ __forceinline__ void forward_wide_water_item(const DebyeArgs &a, int item_idx, int k0)
+{
+    constexpr int QP = WideSlab<QS>::QP, NR = WideSlab<QS>::NR;
+    __shared__ float4 s_pos[kBlockAtoms];
+    __shared__ float s_rs[kBlockAtoms];
+    __shared__ float4 s_fq[QP / 2];
+    __shared__ float s_fi[QP], s_fw[QP];
+    __shared__ double s_red[kBlockAtoms / 32][QP];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    __syncthreads(); // a previous item of this CTA may still read shared memory
+    const PairItem it = a.items[item_idx];
+    const BlockDesc bi = a.blocks[it.bi];
+    const int tj = a.blocks[it.bj_begin].type;
+    for (int k = tid; k < QP; k += kBlockAtoms) {
+        const int kk = k0 + k;
+        const bool in = k < QS && kk < a.n_q;
+        const float *row = a.ff + (size_t)(in ? kk : 0) * a.n_types;
+        s_fi[k] = in ? row[bi.type] : 0.f;
+        s_fw[k] = in ? a.water_weight * row[a.water_index] : 0.f;
+        const float fj = in ? row[tj] : 0.f;
+        // the table row of step m = k / 2 holds both q of the step
+        float *fq = reinterpret_cast<float *>(&s_fq[k >> 1]);
+        fq[k & 1] = fj;
+        fq[2 + (k & 1)] = s_fw[k];
+    }
+    const int i = bi.start + tid;
+    const bool valid_i = tid < bi.len;
+    const float4 pi = valid_i ? a.pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float rs_i = valid_i ? a.rsasa[i] : 0.f;
+    const float q0 = a.q[k0];
+    const float dq = a.dq;
+    const bool small_th = !SIGNED || a.small_theta >= 2;
+
+    double acc[NR];
+#pragma unroll
+    for (int c = 0; c < NR; ++c)
+        acc[c] = 0.0;
+
+    for (int b = it.bj_begin; b < it.bj_end; ++b) {
+        const BlockDesc bj = a.blocks[b];
+        __syncthreads();
+        if (tid < bj.len) {
+            s_pos[tid] = a.pos[bj.start + tid];
+            s_rs[tid] = a.rsasa[bj.start + tid];
+        }
+        __syncthreads();
+        const bool diag = (b == it.bi);
+        float2 S[QP / 2];
+#pragma unroll
+        for (int m = 0; m < QP / 2; ++m)
+            S[m] = make_float2(0.f, 0.f);
+        int jj = 0;
+        for (; jj + 1 < bj.len; jj += 2) {
+            // the table rows are the same for every pair: an offset the
+            // compiler cannot see through keeps it from hoisting all of them
+            // into registers (one shared load per step is the intent)
+            int fo = 0;
+            asm volatile("" : "+r"(fo));
+            float r1, ri1, r2, ri2, dx, dy, dz;
+            pair_r(pi, s_pos[jj], r1, ri1, dx, dy, dz);
+            pair_r(pi, s_pos[jj + 1], r2, ri2, dx, dy, dz);
+            const bool u1 = valid_i && (!diag || jj > tid);
+            const bool u2 = valid_i && (!diag || jj + 1 > tid);
+            const WideSeed p1 = wide_seed(q0, dq, r1, u1 ? ri1 : 0.f, small_th);
+            const WideSeed p2 = wide_seed(q0, dq, r2, u2 ? ri2 : 0.f, small_th);
+            if constexpr (SIGNED)
+                wide_water_pair2<QS, QP / 2>(p1, p2, s_rs[jj], s_rs[jj + 1], s_fq + fo, S);
+            else
+                wide_water_pair2_body<QS, QP / 2, false>(p1, p2, s_rs[jj], s_rs[jj + 1],
+                                                         s_fq + fo, S);
+        }
+        if (jj < bj.len) {
+            int fo = 0;
+            asm volatile("" : "+r"(fo));
+            float r, rinv, dx, dy, dz;
+            pair_r(pi, s_pos[jj], r, rinv, dx, dy, dz);
+            const bool use = valid_i && (!diag || jj > tid);
+            wide_water_pair1<QS, QP / 2>(wide_seed(q0, dq, r, use ? rinv : 0.f, small_th),
+                                         s_rs[jj], s_fq + fo, S);
+        }
+#pragma unroll
+        for (int c = 0; c < NR; ++c) {
+            float v[32];
+#pragma unroll
+            for (int k = 0; k < 32; ++k) {
+                const int kq = 32 * c + k;
+                v[k] = fmaf(rs_i, s_fw[kq], s_fi[kq]) * pair_at(S, kq);
+            }
+            warp_reduce_scatter<32>(v, lane);
+            acc[c] += (double)v[0];
+        }
+    }
+
+#pragma unroll
+    for (int c = 0; c < NR; ++c)
+        s_red[warp][32 * c + lane] = acc[c];
+    __syncthreads();
+    for (int k = tid; k < QS; k += kBlockAtoms) {
+        const int kk = k0 + k;
+        if (kk >= a.n_q)
+            continue;
+        double s = 0.0;
+#pragma unroll
+        for (int w = 0; w < kBlockAtoms / 32; ++w)
+            s += s_red[w][k];
+        a.partial[(size_t)kk * a.n_items + item_idx] = s;
+    }
+}
+
 // Forward pair sums of one work item for q values [k0, k0 + QS): writes
 // partial[k][item_idx] = sum over the item's pairs of f_i f_j sin(q_k r)/r.
 // Called once per CTA by the grid kernel and repeatedly by the persistent

@@ -50,6 +50,14 @@ __global__ void __launch_bounds__(kBlockAtoms, (QS <= 64 || !SIGNED) ? 3 : 2)
     forward_wide_item<QS, IL, SIGNED>(a, blockIdx.x, a.k_base + blockIdx.y * QS);
 }
 
+// the same with the implicit water term (one more FP32x2 FMA per step)
+template <int QS, bool SIGNED>
+__global__ void __launch_bounds__(kBlockAtoms, (QS <= 64 || !SIGNED) ? 3 : 2)
+    forward_wide_water_kernel(const DebyeArgs a)
+{
+    forward_wide_water_item<QS, SIGNED>(a, blockIdx.x, a.k_base + blockIdx.y * QS);
+}
+
 // ----------------------------------------------------------------------------
 // assemble I(q) = self(q) + 2 * cross(q) / q  (q = 0: (sum f)^2)
 // ----------------------------------------------------------------------------
@@ -390,11 +398,15 @@ static cudaError_t forward_dispatch(const DebyeArgs &a, int qs, int k_base, int 
 // latency (6 % faster than 2 CTAs with 4 pairs per step at 201 q); the signed
 // ones keep 2 CTAs/SM above 64 q.  Both step 2 pairs at a time.
 template <int QS>
-static cudaError_t wide_launch(DebyeArgs a, int k_base, int n_slabs, cudaStream_t st)
+static cudaError_t wide_launch(DebyeArgs a, int k_base, int n_slabs, bool water, cudaStream_t st)
 {
     a.k_base = k_base;
     const dim3 grid(a.n_items, n_slabs);
-    if (a.small_theta >= 2)
+    if (water && a.small_theta >= 2)
+        forward_wide_water_kernel<QS, false><<<grid, kBlockAtoms, 0, st>>>(a);
+    else if (water)
+        forward_wide_water_kernel<QS, true><<<grid, kBlockAtoms, 0, st>>>(a);
+    else if (a.small_theta >= 2)
         forward_wide_kernel<QS, 2, false><<<grid, kBlockAtoms, 0, st>>>(a);
     else
         forward_wide_kernel<QS, 2, true><<<grid, kBlockAtoms, 0, st>>>(a);
@@ -423,25 +435,25 @@ static int tail_width(int len)
 
 static float tail_cost(int len) { return len > 0 ? kCostWidth[tail_width(len) / 16 - 1] : 0.f; }
 
-static cudaError_t wide_tail(const DebyeArgs &a, int k0, int width, cudaStream_t st)
+static cudaError_t wide_tail(const DebyeArgs &a, int k0, int width, bool water, cudaStream_t st)
 {
     switch (width / 16) {
     case 1:
-        return wide_launch<16>(a, k0, 1, st);
+        return wide_launch<16>(a, k0, 1, water, st);
     case 2:
-        return wide_launch<32>(a, k0, 1, st);
+        return wide_launch<32>(a, k0, 1, water, st);
     case 3:
-        return wide_launch<48>(a, k0, 1, st);
+        return wide_launch<48>(a, k0, 1, water, st);
     case 4:
-        return wide_launch<64>(a, k0, 1, st);
+        return wide_launch<64>(a, k0, 1, water, st);
     case 5:
-        return wide_launch<80>(a, k0, 1, st);
+        return wide_launch<80>(a, k0, 1, water, st);
     case 6:
-        return wide_launch<96>(a, k0, 1, st);
+        return wide_launch<96>(a, k0, 1, water, st);
     case 7:
-        return wide_launch<112>(a, k0, 1, st);
+        return wide_launch<112>(a, k0, 1, water, st);
     default:
-        return wide_launch<128>(a, k0, 1, st);
+        return wide_launch<128>(a, k0, 1, water, st);
     }
 }
 
@@ -470,35 +482,35 @@ WidePlan wide_plan(int n_q, int q_slab)
     return best;
 }
 
-// Uniform grid without water: full slabs of the plan's main width, then the
-// tail slab (a second launch on the same stream).
-static cudaError_t launch_forward_wide(const DebyeArgs &a, int q_slab, cudaStream_t st)
+// Uniform grid: full slabs of the plan's main width, then the tail slab (a
+// second launch on the same stream).
+static cudaError_t launch_forward_wide(const DebyeArgs &a, int q_slab, bool water, cudaStream_t st)
 {
     const WidePlan p = wide_plan(a.n_q, q_slab);
     if (p.full > 0) {
         cudaError_t e;
-        e = p.main == 64    ? wide_launch<64>(a, 0, p.full, st)
-            : p.main == 112 ? wide_launch<112>(a, 0, p.full, st)
-                            : wide_launch<128>(a, 0, p.full, st);
+        e = p.main == 64    ? wide_launch<64>(a, 0, p.full, water, st)
+            : p.main == 112 ? wide_launch<112>(a, 0, p.full, water, st)
+                            : wide_launch<128>(a, 0, p.full, water, st);
         if (e != cudaSuccess)
             return e;
     }
     if (p.tail_len == 0)
         return cudaSuccess;
-    return wide_tail(a, p.tail_k0, p.tail_w, st);
+    return wide_tail(a, p.tail_k0, p.tail_w, water, st);
 }
 
-// Uniform grids without water and q_slab 64 / 128 take the wide slabs (64 or
-// 112 q per seed); otherwise full slabs of q_slab values, then the remainder
-// in the smallest slab of 8 / 16 / 32 that covers it (a second launch on the
-// same stream).
+// Uniform grids and q_slab 64 / 128 take the wide slabs (64 to 128 q per
+// seed, with or without water); otherwise full slabs of q_slab values, then
+// the remainder in the smallest slab of 8 / 16 / 32 that covers it (a second
+// launch on the same stream).
 cudaError_t launch_forward(const DebyeArgs &a, int q_slab, bool uniform, bool water,
                            cudaStream_t st)
 {
     if (a.n_items == 0)
         return cudaSuccess;
-    if (uniform && !water && q_slab >= 64)
-        return launch_forward_wide(a, q_slab, st);
+    if (uniform && q_slab >= 64)
+        return launch_forward_wide(a, q_slab, water, st);
     const int full = a.n_q / q_slab;
     const int rest = a.n_q - full * q_slab;
     if (full > 0) {

@@ -259,14 +259,23 @@ void water_sums(rsx_debye *h)
 
 bool has_water(const rsx_debye *h) { return h->water_weight != 0.f; }
 
+// q slab of the general kernels (the adjoint, the delta and the non-wide
+// forward): water keeps two accumulator sets in registers there.
 int slab_for(const rsx_debye *h)
 {
     int qs = h->q_slab;
     if (has_water(h) && qs > 16)
-        qs = 16; // water keeps two accumulator sets in registers
+        qs = 16;
     if (!h->uniform && qs > 32)
         qs = 32; // the direct-sine path has no wide variant
     return qs;
+}
+
+// q slab of the forward: on uniform grids the wide slabs (q_slab 64 / 128)
+// also carry the water term.
+int forward_slab(const rsx_debye *h)
+{
+    return (h->uniform && h->q_slab >= 64) ? h->q_slab : slab_for(h);
 }
 
 // Re-derives the device layout when the body types changed.
@@ -418,7 +427,8 @@ rsx_status forward_device(rsx_debye *h)
     const DebyeArgs a = debye_args(h);
     if (h->timing)
         RSX_TRY_CUDA(cudaEventRecord(h->ev_k0, h->st), "event");
-    RSX_LAUNCH(launch_forward(a, slab_for(h), h->uniform, has_water(h), h->st), "forward kernel");
+    RSX_LAUNCH(launch_forward(a, forward_slab(h), h->uniform, has_water(h), h->st),
+               "forward kernel");
     if (h->timing)
         RSX_TRY_CUDA(cudaEventRecord(h->ev_k1, h->st), "event");
     RSX_LAUNCH(launch_assemble(assemble_args(h, a.n_items, 0), h->st), "assemble kernel");
@@ -465,7 +475,7 @@ rsx_status tune_slab(rsx_debye *h)
         return RSX_OK;
     }
     std::vector<int> cands = {16, 32};
-    if (h->uniform && !has_water(h)) {
+    if (h->uniform) {
         cands.push_back(64);
         cands.push_back(128);
     }
@@ -861,7 +871,7 @@ rsx_status rsx_debye_calc_shard(rsx_debye *h, const rsx_body *bodies, int shard,
     a.items = h->d_items + range.first;
     a.n_items = range.second - range.first;
     if (a.n_items > 0)
-        RSX_LAUNCH(launch_forward(a, slab_for(h), h->uniform, has_water(h), h->st),
+        RSX_LAUNCH(launch_forward(a, forward_slab(h), h->uniform, has_water(h), h->st),
                    "forward kernel");
     if (shard == 0) {
         RSX_LAUNCH(launch_assemble(assemble_args(h, a.n_items, 0), h->st), "assemble kernel");
@@ -1146,7 +1156,7 @@ rsx_status rsx_debye_config(rsx_debye *h, int *q_slab, int *n_items, int *unifor
     if (!h)
         return fail(RSX_ALG_NOT_INITIALIZED, "null rsx_debye handle");
     if (q_slab)
-        *q_slab = slab_for(h);
+        *q_slab = forward_slab(h);
     if (n_items)
         *n_items = (int)h->L.items.size();
     if (uniform_q)

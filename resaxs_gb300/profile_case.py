@@ -5,6 +5,10 @@
     python -m resaxs_gb300.profile_case adjoint --config 3 [--n N]
     python -m resaxs_gb300.profile_case sasa    --config 2 [--dots 960]
 
+`--general` forces the general (non-recurrence) q path; `--water W` turns
+the implicit water term on with weight W, seeded rsasa in [0, 1] and the
+last factor column as the water factor.
+
 Uses the seeded synthetic workloads of resaxs_gb300.workloads; prints one
 line with the wall time per repetition.  Exits non-zero on any librsx error.
 """
@@ -26,6 +30,8 @@ def main(argv=None):
     p.add_argument("--k", type=int, default=50)
     p.add_argument("--dots", type=int, default=960)
     p.add_argument("--q-slab", type=int, default=0)
+    p.add_argument("--general", action="store_true")
+    p.add_argument("--water", type=float, default=0.0)
     a = p.parse_args(argv)
     from . import workloads as W
     from .saxs import Debye
@@ -54,7 +60,10 @@ def main(argv=None):
         return 0
 
     w = W.make_config(a.config, seed=0, n_override=a.n)
-    with Debye(w.q, w.ff, w.n, q_slab=a.q_slab) as d:
+    with Debye(w.q, w.ff, w.n, q_slab=a.q_slab, force_general_q=a.general) as d:
+        if a.water != 0.0:
+            rs = np.random.default_rng(2).uniform(0, 1, w.n).astype(np.float32)
+            d.set_water(a.water, w.ff.shape[1] - 1, rs)
         d.calc(w.bodies)
         rng = np.random.default_rng(1)
         t0 = time.perf_counter()

@@ -146,6 +146,27 @@ def test_water_term(saxs, oracle_lib):
     assert rel(out64, ref) < TOL
 
 
+@pytest.mark.parametrize("q_slab,n_q,ww", [(0, 201, 0.8), (64, 201, -1.5), (128, 101, 3.0),
+                                           (128, 47, 0.8), (64, 130, 2.0)])
+def test_water_term_wide_slabs(saxs, oracle_lib, q_slab, n_q, ww):
+    """The implicit water term on uniform grids runs in the wide slabs (the
+    per-(j, q) coefficient f_t + w rsasa f_w folded into the paired steps):
+    compact structure (unsigned steps), several slab plans and tail widths,
+    negative and large water weights; FP64 oracle."""
+    w = W.make_config(2, seed=16, n_override=900)
+    rng = np.random.default_rng(n_q)
+    q = W.q_grid(n_q, 0.5)
+    ff = W.exp_form_factors(q, W.Z5, rng.uniform(0.5, 2.0, 5))
+    rs = rng.uniform(0, 1, w.n).astype(np.float32)
+    with saxs.Debye(q, ff, w.n, q_slab=q_slab) as d:
+        d.set_water(ww, 4, rs)
+        d.calc(w.bodies)
+        out64 = d.curve_f64()
+        assert d.config()["uniform_q"]
+    ref = oracle_lib.debye_f64(q, w.bodies, ff, rsasa=rs, water_weight=ww, water_index=4)
+    assert rel(out64, ref) < TOL
+
+
 def test_small_item_cap_forces_chunking(saxs, oracle_lib):
     w = W.make_config(2, seed=15, n_override=1500)
     _, _, cfg1 = gpu_curve(saxs, w.q, w.ff, w.bodies)
