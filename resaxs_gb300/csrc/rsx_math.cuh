@@ -36,21 +36,6 @@ constexpr float kC3 = -1.0f / 720.0f;
 constexpr float kC4 = 1.0f / 40320.0f;
 constexpr float kC5 = -1.0f / 3628800.0f;
 
-// sin and cos of |r| <= pi/4 by their Taylor series.
-__device__ __forceinline__ void sincos_poly(float r, float &s, float &c)
-{
-    const float r2 = r * r;
-    float ps = fmaf(r2, kS4, kS3);
-    ps = fmaf(r2, ps, kS2);
-    ps = fmaf(r2, ps, kS1);
-    s = fmaf(r * r2, ps, r);
-    float pc = fmaf(r2, kC5, kC4);
-    pc = fmaf(r2, pc, kC3);
-    pc = fmaf(r2, pc, kC2);
-    pc = fmaf(r2, pc, kC1);
-    c = fmaf(r2, pc, 1.0f);
-}
-
 // sin and cos of the unevaluated sum x_hi + x_lo (|x_lo| <= ulp(x_hi)),
 // with the reduction split so that no FP32 rounding sees a constant offset.
 // r = x - n*pi/2 is carried as r_hi = x_hi - n*P1 (exact: both terms are
@@ -116,8 +101,6 @@ __device__ __forceinline__ void sincos_small2(float x, float x_lo, float &s, flo
     s = x + fmaf(r3, ps, x_lo * cp);
     c = 1.0f + fmaf(r2, pc, -x_lo * sp);
 }
-
-__device__ __forceinline__ void sincos_rr(float x, float &s, float &c) { sincos_rr2(x, 0.0f, s, c); }
 
 // sin and cos of the product a*b, its rounding error folded in exactly.
 __device__ __forceinline__ void sincos_prod(float a, float b, float &s, float &c)
