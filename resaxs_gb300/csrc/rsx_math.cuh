@@ -5,7 +5,7 @@
 //    x * 2/pi, r = (x - n*P1) - n*P2 where P1 + P2 (+ P3) is pi/2 split into
 //    FP32 numbers (P1 = fl(pi/2), P2 = fl(pi/2 - P1), P3 = fl(pi/2 - P1 - P2),
 //    computed from a 60-digit value of pi); with FMA the first step is exact,
-//    and the second is carried as a separate low part (see sincos_rr);
+//    and the second is carried as a separate low part (see sincos_rr2);
 //  * the Taylor series of sin and cos about 0 on |r| <= pi/4 (the
 //    "small-argument series"): sin to r^9 (truncation < 2e-10 relative),
 //    cos to r^10 (truncation < 2e-11);
