@@ -1,0 +1,86 @@
+// Adjoint kernel launches (dL/dx from dL/dI(q) in one pair pass), split from
+// debye_kernels.cu so that the two translation units compile in parallel.
+// The per-item device code is in debye_device.cuh.
+#include "debye_device.cuh"
+
+namespace rsx {
+
+// ----------------------------------------------------------------------------
+// adjoint: grad_i = sum_j G_ij (x_i - x_j),
+//   G_ij = 2/r^2 sum_q lambda_q f_i f_j (cos(q r) - sinc(q r))
+// Each pair is visited once (upper triangle); the J side of every pair is
+// summed over the warp with shuffles, accumulated in shared memory and
+// flushed to the FP64 gradient once per J-block.  The thread runs the whole
+// q range for each pair (slab by slab, all in registers), so the gradient of
+// a pair is complete before it is scattered.
+// ----------------------------------------------------------------------------
+
+// The uniform form: 4 CTAs per SM (8 pairs per thread step need 128 registers).
+template <int QS, bool UNIFORM, bool WATER, bool SMALL = false>
+__global__ void __launch_bounds__(kBlockAtoms, (UNIFORM && !WATER) ? 4 : 1)
+    adjoint_kernel(const DebyeArgs a, int n_slabs)
+{
+    adjoint_item<QS, UNIFORM, WATER, SMALL>(a, blockIdx.x, n_slabs);
+}
+
+template <int QS>
+static cudaError_t adjoint_qs(const DebyeArgs &a, bool uniform, bool water, cudaStream_t st)
+{
+    const int n_slabs = (a.n_q + QS - 1) / QS;
+    const size_t smem = adjoint_smem_bytes(a.n_q, QS, uniform, water);
+    const dim3 grid(a.n_items);
+    cudaError_t e = cudaSuccess;
+#define RSX_ADJ_SMALL()                                                                    \
+    do {                                                                                   \
+        auto kfn = adjoint_kernel<QS, true, false, true>;                                  \
+        if (smem > 48 * 1024)                                                              \
+            e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,     \
+                                     (int)smem);                                           \
+        if (e == cudaSuccess)                                                              \
+            kfn<<<grid, kBlockAtoms, smem, st>>>(a, n_slabs);                              \
+    } while (0)
+#define RSX_ADJ(U, W)                                                                      \
+    do {                                                                                   \
+        auto kfn = adjoint_kernel<QS, U, W>;                                               \
+        if (smem > 48 * 1024)                                                              \
+            e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,     \
+                                     (int)smem);                                           \
+        if (e == cudaSuccess)                                                              \
+            kfn<<<grid, kBlockAtoms, smem, st>>>(a, n_slabs);                              \
+    } while (0)
+    if (uniform && !water && a.small_theta >= 1)
+        RSX_ADJ_SMALL();
+    else if (uniform && !water)
+        RSX_ADJ(true, false);
+    else if (uniform && water)
+        RSX_ADJ(true, true);
+    else if (!uniform && !water)
+        RSX_ADJ(false, false);
+    else
+        RSX_ADJ(false, true);
+#undef RSX_ADJ
+#undef RSX_ADJ_SMALL
+    if (e != cudaSuccess)
+        return e;
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint(const DebyeArgs &a, int q_slab, bool uniform, bool water,
+                           cudaStream_t st)
+{
+    if (a.n_items == 0)
+        return cudaSuccess;
+    switch (q_slab > 32 ? 32 : q_slab) { // the adjoint walks all q per pair in 32-q slabs
+    case 8:
+        return adjoint_qs<8>(a, uniform, water, st);
+    case 16:
+        return adjoint_qs<16>(a, uniform, water, st);
+    case 32:
+        return adjoint_qs<32>(a, uniform, water, st);
+    default:
+        return cudaErrorInvalidValue;
+    }
+}
+
+} // namespace rsx

@@ -90,7 +90,7 @@ struct DeltaArgs {
 
 constexpr int kDeltaGroups = 8; // moved-list groups of the wide delta kernel
 
-// launchers (debye_kernels.cu); all asynchronous on `st`
+// launchers (debye_kernels.cu, adjoint_kernels.cu); all asynchronous on `st`
 // Slab plan of the wide uniform forward: `full` slabs of `main` q from q 0,
 // then one tail slab covering [tail_k0, tail_k0 + tail_len) with a kernel
 // `tail_w` q wide (tail_len 0: none).  q_slab 64 restricts the plan to 64-q
