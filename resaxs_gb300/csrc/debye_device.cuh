@@ -1,7 +1,7 @@
 // Device-side building blocks of the Debye pair kernels, shared by the
-// per-structure launches (debye_kernels.cu, adjoint_kernels.cu) and the persistent batch kernels
-// (batch_kernels.cu).  Written from scratch for this project; see
-// debye_kernels.cu for the overall scheme.
+// per-structure launches (debye_kernels.cu, adjoint_kernels.cu) and the
+// persistent batch kernels (batch_kernels.cu).  Written from scratch for this
+// project; see debye_kernels.cu for the overall scheme.
 #pragma once
 #include "rsx_internal.h"
 #include "rsx_math.cuh"
