@@ -465,10 +465,20 @@ WidePlan wide_plan(int n_q, int q_slab)
 }
 
 // Uniform grid: full slabs of the plan's main width, then the tail slab (a
-// second launch on the same stream).
-static cudaError_t launch_forward_wide(const DebyeArgs &a, int q_slab, bool water, cudaStream_t st)
+// second launch: on `aux` when given, forked after the work queued on `st`
+// and joined back into it, else on `st`).
+static cudaError_t launch_forward_wide(const DebyeArgs &a, int q_slab, bool water, cudaStream_t st,
+                                       const AuxStream *aux)
 {
     const WidePlan p = wide_plan(a.n_q, q_slab);
+    const bool split = aux && p.full > 0 && p.tail_len > 0;
+    if (split) {
+        cudaError_t e = cudaEventRecord(aux->fork, st);
+        if (e == cudaSuccess)
+            e = cudaStreamWaitEvent(aux->stream, aux->fork, 0);
+        if (e != cudaSuccess)
+            return e;
+    }
     if (p.full > 0) {
         cudaError_t e;
         e = p.main == 64    ? wide_launch<64>(a, 0, p.full, water, st)
@@ -479,7 +489,14 @@ static cudaError_t launch_forward_wide(const DebyeArgs &a, int q_slab, bool wate
     }
     if (p.tail_len == 0)
         return cudaSuccess;
-    return wide_tail(a, p.tail_k0, p.tail_w, water, st);
+    if (!split)
+        return wide_tail(a, p.tail_k0, p.tail_w, water, st);
+    cudaError_t e = wide_tail(a, p.tail_k0, p.tail_w, water, aux->stream);
+    // the join is recorded and awaited even after a failed launch, so that
+    // `st` never runs ahead of work queued on the aux stream
+    const cudaError_t ej = cudaEventRecord(aux->join, aux->stream);
+    const cudaError_t ew = ej == cudaSuccess ? cudaStreamWaitEvent(st, aux->join, 0) : ej;
+    return e != cudaSuccess ? e : ew;
 }
 
 // Uniform grids and q_slab 64 / 128 take the wide slabs (64 to 128 q per
@@ -487,12 +504,12 @@ static cudaError_t launch_forward_wide(const DebyeArgs &a, int q_slab, bool wate
 // the remainder in the smallest slab of 8 / 16 / 32 that covers it (a second
 // launch on the same stream).
 cudaError_t launch_forward(const DebyeArgs &a, int q_slab, bool uniform, bool water,
-                           cudaStream_t st)
+                           cudaStream_t st, const AuxStream *aux)
 {
     if (a.n_items == 0)
         return cudaSuccess;
     if (uniform && q_slab >= 64)
-        return launch_forward_wide(a, q_slab, water, st);
+        return launch_forward_wide(a, q_slab, water, st, aux);
     const int full = a.n_q / q_slab;
     const int rest = a.n_q - full * q_slab;
     if (full > 0) {

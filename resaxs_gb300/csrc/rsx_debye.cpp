@@ -153,6 +153,7 @@ struct rsx_debye {
     int device = -1;
     cudaStream_t st = nullptr;
     cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr, ev_c0 = nullptr, ev_c1 = nullptr;
+    AuxStream aux{nullptr, nullptr, nullptr}; // tail slab of the wide forward
     bool timing = false;
     int n = 0, n_q = 0, n_types = 0;
     std::vector<float> q, ff;
@@ -427,7 +428,7 @@ rsx_status forward_device(rsx_debye *h)
     const DebyeArgs a = debye_args(h);
     if (h->timing)
         RSX_TRY_CUDA(cudaEventRecord(h->ev_k0, h->st), "event");
-    RSX_LAUNCH(launch_forward(a, forward_slab(h), h->uniform, has_water(h), h->st),
+    RSX_LAUNCH(launch_forward(a, forward_slab(h), h->uniform, has_water(h), h->st, &h->aux),
                "forward kernel");
     if (h->timing)
         RSX_TRY_CUDA(cudaEventRecord(h->ev_k1, h->st), "event");
@@ -690,6 +691,8 @@ rsx_status release(rsx_debye *h)
     DeviceGuard g(h->device);
     if (h->st)
         cudaStreamSynchronize(h->st);
+    if (h->aux.stream)
+        cudaStreamSynchronize(h->aux.stream);
     void *dev[] = {h->d_pos,        h->d_pos_saved, h->d_rsasa,      h->d_ff,
                    h->d_q,          h->d_blocks,    h->d_items,      h->d_adj_items,
                    h->d_partial,    h->d_iq64,      h->d_iq64_saved, h->d_iq32,
@@ -700,10 +703,12 @@ rsx_status release(rsx_debye *h)
     void *pinned[] = {h->h_pos, h->h_iq, h->h_iq64, h->h_grad, h->h_moved, h->h_rsasa};
     for (void *p : pinned)
         host_free_pinned(p);
-    cudaEvent_t evs[] = {h->ev_k0, h->ev_k1, h->ev_c0, h->ev_c1};
+    cudaEvent_t evs[] = {h->ev_k0, h->ev_k1, h->ev_c0, h->ev_c1, h->aux.fork, h->aux.join};
     for (auto e : evs)
         if (e)
             cudaEventDestroy(e);
+    if (h->aux.stream)
+        cudaStreamDestroy(h->aux.stream);
     if (h->st)
         cudaStreamDestroy(h->st);
     delete h;
@@ -768,6 +773,14 @@ rsx_status rsx_debye_create(const float *q, int n_q, const float *t_factors, int
         return bail(cuda_status(e, "cudaStreamCreate"));
     for (cudaEvent_t *ev : {&h->ev_k0, &h->ev_k1, &h->ev_c0, &h->ev_c1}) {
         e = cudaEventCreate(ev);
+        if (e != cudaSuccess)
+            return bail(cuda_status(e, "cudaEventCreate"));
+    }
+    e = cudaStreamCreateWithFlags(&h->aux.stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess)
+        return bail(cuda_status(e, "cudaStreamCreate"));
+    for (cudaEvent_t *ev : {&h->aux.fork, &h->aux.join}) {
+        e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
         if (e != cudaSuccess)
             return bail(cuda_status(e, "cudaEventCreate"));
     }

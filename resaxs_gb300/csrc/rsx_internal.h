@@ -100,8 +100,15 @@ struct WidePlan {
 };
 WidePlan wide_plan(int n_q, int q_slab);
 
+// A second stream for the tail slab of a wide forward, so that it runs
+// beside the main slabs and fills their last wave; `fork` and `join` are
+// events (timing disabled) owned with the stream.
+struct AuxStream {
+    cudaStream_t stream;
+    cudaEvent_t fork, join;
+};
 cudaError_t launch_forward(const DebyeArgs &a, int q_slab, bool uniform, bool water,
-                           cudaStream_t st);
+                           cudaStream_t st, const AuxStream *aux = nullptr);
 cudaError_t launch_assemble(const AssembleArgs &a, cudaStream_t st);
 cudaError_t launch_delta(const DeltaArgs &a, int q_slab, bool uniform, cudaStream_t st);
 // partial sums per q that launch_delta writes (the assembly's n_parts)
