@@ -83,4 +83,43 @@ cudaError_t launch_adjoint(const DebyeArgs &a, int q_slab, bool uniform, bool wa
     }
 }
 
+// ----------------------------------------------------------------------------
+// adjoint through tabulated pair functions (debye_device.cuh): the table of
+// every present type pair (t_i <= t_j), then one pair pass
+// ----------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(128)
+    adjoint_table_kernel(const DebyeArgs a, float4 *tab, unsigned type_mask)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ti = blockIdx.y, tj = blockIdx.z;
+    if (b >= a.adj_nodes || tj < ti || !((type_mask >> ti) & 1u) || !((type_mask >> tj) & 1u))
+        return;
+    tab[(size_t)(ti * a.n_types + tj) * a.adj_nodes + b] = adjoint_table_node(a, ti, tj, b, a.adj_h);
+}
+
+template <int IL>
+__global__ void __launch_bounds__(kBlockAtoms) adjoint_pairs_table_kernel(const DebyeArgs a)
+{
+    adjoint_table_item<IL>(a, blockIdx.x);
+}
+
+cudaError_t launch_adjoint_table(const DebyeArgs &a, float4 *tab, unsigned type_mask,
+                                 cudaStream_t st)
+{
+    if (a.n_items == 0)
+        return cudaSuccess;
+    if (a.n_types > 32 || a.adj_nodes < 2)
+        return cudaErrorInvalidValue;
+    const dim3 g((a.adj_nodes + 127) / 128, a.n_types, a.n_types);
+    adjoint_table_kernel<<<g, 128, 0, st>>>(a, tab, type_mask);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return e;
+    adjoint_pairs_table_kernel<4><<<a.n_items, kBlockAtoms, 0, st>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
 } // namespace rsx

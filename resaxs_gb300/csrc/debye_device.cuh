@@ -1040,6 +1040,136 @@ __device__ __forceinline__ void adj_scatter(const AdjPair &p, float A, float B, 
     }
 }
 
+// ----------------------------------------------------------------------------
+// adjoint through tabulated pair functions (any q grid, no water)
+// ----------------------------------------------------------------------------
+//
+// For one item's type pair (t_i, t_j) the gradient of a pair needs only
+//   A(r) = sum_k alpha_k cos(q_k r),   B(r) = sum_k beta_k sin(q_k r)
+// (alpha_k = lambda_k f_ti(q_k) f_tj(q_k), beta_k = alpha_k / q_k; q = 0 adds
+// nothing to either, since d sinc(q r)/dr vanishes there),
+// smooth functions of r alone whose derivatives are bounded by powers of
+// q_max.  They are tabulated with their first derivatives on a uniform r grid
+// of step h covering every pair distance (adjoint_table_kernel: sums over q in
+// FP64), and each pair reads them by cubic Hermite interpolation.  Its error
+// is at most h^4 max|f| / 384 with |f| <= q_max^4 sum|alpha|, so below
+// (q_max h)^4 / 384 of sum|alpha| (1.6e-8 at q_max h = 0.05, the step the host
+// picks) -- smaller than the FP32 recurrence's.  A pair then costs two table
+// loads and ~25 FP32 operations instead of 4 per q.
+
+// Node b of the table at r_b = b h (exact in double): A, h dA/dr, B, h dB/dr.
+// sin/cos(q r_b) in FP32 with the rounding of q r_b folded in as the low part
+// (r_b itself is carried as hi + lo), sums in FP64.
+__device__ __forceinline__ float4 adjoint_table_node(const DebyeArgs &a, int ti, int tj, int b,
+                                                     float h)
+{
+    const double rb = (double)b * (double)h;
+    const float r_hi = (float)rb, r_lo = (float)(rb - (double)r_hi);
+    double A = 0.0, dA = 0.0, B = 0.0, dB = 0.0;
+    for (int k = 0; k < a.n_q; ++k) {
+        const float qk = a.q[k];
+        if (qk == 0.f)
+            continue; // d sinc(q r) / dr = 0 at q = 0: no term on either side
+        const float al = a.lambda[k] * a.ff[(size_t)k * a.n_types + ti] *
+                         a.ff[(size_t)k * a.n_types + tj];
+        const float x = qk * r_hi;
+        const float x_lo = fmaf(qk, r_hi, -x) + qk * r_lo;
+        float s, c;
+        sincos_rr2(x, x_lo, s, c);
+        const double be = (double)(al / qk);
+        A += (double)al * c;
+        dA -= (double)al * qk * s;
+        B += be * s;
+        dB += be * qk * c;
+    }
+    return make_float4((float)A, (float)(h * dA), (float)B, (float)(h * dB));
+}
+
+// A(r) and B(r) of one pair from the table of its item's type pair.
+__device__ __forceinline__ void adjoint_table_eval(const float4 *tab, int n_nodes, float h,
+                                                   float inv_h, float r, float &A, float &B)
+{
+    // node index: clamped into the table (a NaN distance reads node 0)
+    const float u = fminf(fmaxf(r * inv_h, 0.f), (float)(n_nodes - 2));
+    const int b = (int)u;
+    const float t = fmaf(-(float)b, h, r) * inv_h; // (r - b h) / h with r - b h rounded once
+    const float4 p0 = __ldg(tab + b), p1 = __ldg(tab + b + 1);
+    const float t2 = t * t, t3 = t2 * t;
+    const float h01 = fmaf(-2.0f, t3, 3.0f * t2); // Hermite basis
+    const float h00 = 1.0f - h01;
+    const float h10 = t3 - 2.0f * t2 + t;
+    const float h11 = t3 - t2;
+    A = fmaf(h00, p0.x, fmaf(h10, p0.y, fmaf(h01, p1.x, h11 * p1.y)));
+    B = fmaf(h00, p0.z, fmaf(h10, p0.w, fmaf(h01, p1.z, h11 * p1.w)));
+}
+
+// Adjoint of one work item through the tables: every pair of the item reads
+// A and B of its type pair's table, then scatters as the other forms do.  IL
+// pairs per step keep IL table loads in flight.
+template <int IL>
+__device__ __forceinline__ void adjoint_table_item(const DebyeArgs &a, int item_idx)
+{
+    __shared__ float4 s_pos[kBlockAtoms];
+    __shared__ float s_gj[kBlockAtoms][3];
+
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    __syncthreads(); // a previous item of this CTA may still read shared memory
+    const PairItem it = a.items[item_idx];
+    const BlockDesc bi = a.blocks[it.bi];
+    const int tj = a.blocks[it.bj_begin].type;
+    const float4 *tab = a.adj_tab + (size_t)(bi.type * a.n_types + tj) * a.adj_nodes;
+    const int n_nodes = a.adj_nodes;
+    const float h = a.adj_h, inv_h = a.adj_inv_h;
+
+    const int i = bi.start + tid;
+    const bool valid_i = tid < bi.len;
+    const float4 pi = valid_i ? a.pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float gi0 = 0.f, gi1 = 0.f, gi2 = 0.f;
+
+    for (int b = it.bj_begin; b < it.bj_end; ++b) {
+        const BlockDesc bj = a.blocks[b];
+        __syncthreads();
+        if (tid < bj.len)
+            s_pos[tid] = a.pos[bj.start + tid];
+        s_gj[tid][0] = 0.f;
+        s_gj[tid][1] = 0.f;
+        s_gj[tid][2] = 0.f;
+        __syncthreads();
+        const bool diag = (b == it.bi);
+        for (int jj = 0; jj < bj.len; jj += IL) {
+            AdjPair p[IL] = {};
+            float A[IL], B[IL];
+#pragma unroll
+            for (int v = 0; v < IL; ++v) {
+                // past the block's end: a repeated body, masked out below
+                const int j = min(jj + v, bj.len - 1);
+                pair_r(pi, s_pos[j], p[v].r, p[v].rinv, p[v].dx, p[v].dy, p[v].dz);
+                adjoint_table_eval(tab, n_nodes, h, inv_h, p[v].r, A[v], B[v]);
+            }
+#pragma unroll
+            for (int v = 0; v < IL; ++v) {
+                if (jj + v < bj.len) // uniform over the warp
+                    adj_scatter(p[v], A[v], B[v], valid_i && (!diag || jj + v > tid), gi0, gi1,
+                                gi2, s_gj, jj + v, lane);
+            }
+        }
+        __syncthreads();
+        if (tid < bj.len) {
+            double *g = a.grad + 3 * (size_t)(bj.start + tid);
+            atomicAdd(g + 0, (double)s_gj[tid][0]);
+            atomicAdd(g + 1, (double)s_gj[tid][1]);
+            atomicAdd(g + 2, (double)s_gj[tid][2]);
+        }
+    }
+    if (valid_i) {
+        double *g = a.grad + 3 * (size_t)i;
+        atomicAdd(g + 0, (double)gi0);
+        atomicAdd(g + 1, (double)gi1);
+        atomicAdd(g + 2, (double)gi2);
+    }
+}
+
 // Dynamic shared memory of the adjoint kernels for n_q values.
 __host__ __device__ inline size_t adjoint_smem_bytes(int n_q, int qs, bool uniform, bool water)
 {

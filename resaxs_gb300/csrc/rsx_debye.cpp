@@ -204,6 +204,8 @@ struct rsx_debye {
     // adjoint
     double *d_grad = nullptr;
     float *d_lambda = nullptr;
+    float4 *d_adj_tab = nullptr; // tabulated pair functions (no water)
+    size_t adj_tab_cap = 0;      // float4
 
     // pinned staging
     float4 *h_pos = nullptr;
@@ -697,7 +699,7 @@ rsx_status release(rsx_debye *h)
                    h->d_q,          h->d_blocks,    h->d_items,      h->d_adj_items,
                    h->d_partial,    h->d_iq64,      h->d_iq64_saved, h->d_iq32,
                    h->d_type_count, h->d_rsasa_sum, h->d_moved,      h->d_grad,
-                   h->d_lambda};
+                   h->d_lambda,     h->d_adj_tab};
     for (void *p : dev)
         dev_free(p);
     void *pinned[] = {h->h_pos, h->h_iq, h->h_iq64, h->h_grad, h->h_moved, h->h_rsasa};
@@ -1078,6 +1080,33 @@ rsx_status rsx_debye_timing(rsx_debye *h, float *ms_pair_kernel, float *ms_call)
     return ok();
 }
 
+// Geometry of the adjoint's pair-function tables: nodes at r = b h covering
+// the tracked bounding-box diagonal, with q_max h <= 0.05 (interpolation error
+// below 1.6e-8 of sum|alpha|).  False when the tables would not fit the cap
+// (the recurrence adjoint is used then).
+static bool adjoint_table_geometry(const rsx_debye *h, int *nodes, float *step)
+{
+    double d2 = 0.0;
+    for (int d = 0; d < 3; ++d) {
+        const double e = (double)h->hi[d] - (double)h->lo[d];
+        if (!std::isfinite(e))
+            return false;
+        d2 += e > 0.0 ? e * e : 0.0;
+    }
+    double q_max = 0.0;
+    for (float q : h->q)
+        q_max = std::max(q_max, std::fabs((double)q));
+    const double r_max = std::sqrt(d2) * 1.0001 + 1e-3;
+    const double want = std::ceil(r_max * q_max / 0.05) + 2.0;
+    const double n = std::max(16.0, want);
+    const double bytes = n * h->n_types * h->n_types * sizeof(float4);
+    if (!(n < 1e7) || bytes > 512.0 * 1024 * 1024)
+        return false;
+    *nodes = (int)n;
+    *step = (float)(r_max / (n - 2.0));
+    return *step > 0.f;
+}
+
 static rsx_status backward_impl(rsx_debye *h, const float *dl_diq)
 {
     if (!h->computing)
@@ -1093,9 +1122,28 @@ static rsx_status backward_impl(rsx_debye *h, const float *dl_diq)
     a.n_items = (int)h->L.adj_items.size();
     a.lambda = h->d_lambda;
     a.grad = h->d_grad;
+    int nodes = 0;
+    float step = 0.f;
+    const bool tables = !has_water(h) && h->n_types <= 32 && adjoint_table_geometry(h, &nodes, &step);
+    if (tables) {
+        RSX_TRY(ensure(&h->d_adj_tab, h->adj_tab_cap, (size_t)nodes * h->n_types * h->n_types,
+                       "adjoint tables"));
+        a.adj_tab = h->d_adj_tab;
+        a.adj_nodes = nodes;
+        a.adj_h = step;
+        a.adj_inv_h = 1.0f / step;
+    }
+    unsigned type_mask = 0;
+    for (int t = 0; t < h->n_types && t < 32; ++t)
+        if (h->L.type_count[t] > 0)
+            type_mask |= 1u << t;
     if (h->timing)
         RSX_TRY_CUDA(cudaEventRecord(h->ev_k0, h->st), "event");
-    RSX_LAUNCH(launch_adjoint(a, slab_for(h), h->uniform, has_water(h), h->st), "adjoint kernel");
+    if (tables)
+        RSX_LAUNCH(launch_adjoint_table(a, h->d_adj_tab, type_mask, h->st), "adjoint kernels");
+    else
+        RSX_LAUNCH(launch_adjoint(a, slab_for(h), h->uniform, has_water(h), h->st),
+                   "adjoint kernel");
     if (h->timing)
         RSX_TRY_CUDA(cudaEventRecord(h->ev_k1, h->st), "event");
     RSX_TRY_CUDA(cudaMemcpyAsync(h->h_grad, h->d_grad, sizeof(double) * 3 * h->n,

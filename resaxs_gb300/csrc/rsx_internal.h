@@ -54,6 +54,11 @@ struct DebyeArgs {
     // adjoint
     const float *lambda;     // [n_q] dL/dI(q)
     double *grad;            // [n][3] sorted-order FP64 gradient accumulators
+    // adjoint through tabulated pair functions: [n_types * n_types][adj_nodes]
+    // nodes (A, h A', B, h B') at r = b * adj_h, b = 0 .. adj_nodes - 1
+    const float4 *adj_tab;
+    int adj_nodes;
+    float adj_h, adj_inv_h;
 };
 
 // Per-q constants needed to assemble I(q) from the cross sums.
@@ -110,6 +115,10 @@ struct AuxStream {
 cudaError_t launch_forward(const DebyeArgs &a, int q_slab, bool uniform, bool water,
                            cudaStream_t st, const AuxStream *aux = nullptr);
 cudaError_t launch_assemble(const AssembleArgs &a, cudaStream_t st);
+// adjoint through tabulated pair functions: builds the tables of the present
+// type pairs into `tab` ([n_types^2][adj_nodes] float4), then the pair pass
+cudaError_t launch_adjoint_table(const DebyeArgs &a, float4 *tab, unsigned type_mask,
+                                 cudaStream_t st);
 cudaError_t launch_delta(const DeltaArgs &a, int q_slab, bool uniform, cudaStream_t st);
 // partial sums per q that launch_delta writes (the assembly's n_parts)
 int delta_parts(const DeltaArgs &a, int q_slab, bool uniform);
