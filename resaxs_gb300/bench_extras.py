@@ -110,6 +110,10 @@ def adjoint(device: int):
             "fwd_plus_adjoint_over_fwd": (f + a) / f,
             "forward_gpairq_per_s": pq / (f * 1e-3) / 1e9,
             "adjoint_gpairq_per_s": pq / (a * 1e-3) / 1e9,
+            "adjoint_method": "pair functions A(r), B(r) tabulated per type pair (FP64 sums over q) "
+                              "and read by cubic Hermite interpolation: the per-pair cost does "
+                              "not grow with Q, so adjoint pair*q/s is an effective rate; the "
+                              "time includes the table build",
             "api_fwd_plus_adjoint_ms": statistics.median(tot) * 1e3,
             "grad_finite": bool(np.all(np.isfinite(g)))}
 
