@@ -243,6 +243,39 @@ static cudaError_t adj_launch(const DebyeArgs &a, const int *order, int n_items,
     return cudaGetLastError();
 }
 
+// Persistent pair pass of the adjoint through tabulated pair functions: each
+// unit is one adjoint item; its member's tables are selected by PairItem::pad.
+__global__ void __launch_bounds__(kBlockAtoms)
+    batch_adjoint_table_kernel(const DebyeArgs a, const int *work_order, int n_units, int *counter)
+{
+    __shared__ int s_w;
+    for (;;) {
+        if (threadIdx.x == 0)
+            s_w = atomicAdd(counter, 1);
+        __syncthreads();
+        const int w = s_w;
+        __syncthreads();
+        if (w >= n_units)
+            break;
+        adjoint_table_item<4>(a, work_order[w]);
+    }
+}
+
+cudaError_t launch_batch_adjoint_table(const DebyeArgs &a, const int *work_order,
+                                       int n_work_items, int *counter, int grid, cudaStream_t st)
+{
+    if (n_work_items == 0)
+        return cudaSuccess;
+    batch_adjoint_table_kernel<<<grid, kBlockAtoms, 0, st>>>(a, work_order, n_work_items, counter);
+    count_launch();
+    return cudaGetLastError();
+}
+
+int batch_adjoint_table_grid(int sms)
+{
+    return occupancy_grid(batch_adjoint_table_kernel, 0, sms);
+}
+
 cudaError_t launch_batch_adjoint(const DebyeArgs &a, const int *work_order, int n_work_items,
                                  int q_slab, bool uniform, int *counter, int grid,
                                  cudaStream_t st)

@@ -1060,8 +1060,8 @@ __device__ __forceinline__ void adj_scatter(const AdjPair &p, float A, float B, 
 // Node b of the table at r_b = b h (exact in double): A, h dA/dr, B, h dB/dr.
 // sin/cos(q r_b) in FP32 with the rounding of q r_b folded in as the low part
 // (r_b itself is carried as hi + lo), sums in FP64.
-__device__ __forceinline__ float4 adjoint_table_node(const DebyeArgs &a, int ti, int tj, int b,
-                                                     float h)
+__device__ __forceinline__ float4 adjoint_table_node(const DebyeArgs &a, const float *lambda,
+                                                     int ti, int tj, int b, float h)
 {
     const double rb = (double)b * (double)h;
     const float r_hi = (float)rb, r_lo = (float)(rb - (double)r_hi);
@@ -1070,7 +1070,7 @@ __device__ __forceinline__ float4 adjoint_table_node(const DebyeArgs &a, int ti,
         const float qk = a.q[k];
         if (qk == 0.f)
             continue; // d sinc(q r) / dr = 0 at q = 0: no term on either side
-        const float al = a.lambda[k] * a.ff[(size_t)k * a.n_types + ti] *
+        const float al = lambda[k] * a.ff[(size_t)k * a.n_types + ti] *
                          a.ff[(size_t)k * a.n_types + tj];
         const float x = qk * r_hi;
         const float x_lo = fmaf(qk, r_hi, -x) + qk * r_lo;
@@ -1118,9 +1118,13 @@ __device__ __forceinline__ void adjoint_table_item(const DebyeArgs &a, int item_
     const PairItem it = a.items[item_idx];
     const BlockDesc bi = a.blocks[it.bi];
     const int tj = a.blocks[it.bj_begin].type;
-    const float4 *tab = a.adj_tab + (size_t)(bi.type * a.n_types + tj) * a.adj_nodes;
     const int n_nodes = a.adj_nodes;
-    const float h = a.adj_h, inv_h = a.adj_inv_h;
+    // the item's member (PairItem::pad; 0 for a single structure) owns its tables
+    const float4 *tab =
+        a.adj_tab +
+        ((size_t)it.pad * a.n_types * a.n_types + (size_t)(bi.type * a.n_types + tj)) * n_nodes;
+    const float h = a.adj_geom ? a.adj_geom[0] : a.adj_h;
+    const float inv_h = a.adj_geom ? a.adj_geom[1] : a.adj_inv_h;
 
     const int i = bi.start + tid;
     const bool valid_i = tid < bi.len;

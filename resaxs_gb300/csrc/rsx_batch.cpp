@@ -70,8 +70,16 @@ struct rsx_batch {
     double *h_chi2 = nullptr, *h_grad = nullptr;
     bool have_targets = false;
 
+    // adjoint through tabulated pair functions: the node count is a capacity
+    // fixed in the captured graphs (0: the recurrence adjoint); the step of a
+    // pass travels through h_adj_geom -> d_adj_geom ([h, 1/h]) at replay
+    float4 *d_adj_tab = nullptr;
+    int adj_nodes = 0;
+    float *h_adj_geom = nullptr, *d_adj_geom = nullptr;
+    double q_max = 0.0;
+
     cudaGraphExec_t g_fwd = nullptr, g_fwd_adj = nullptr;
-    int fwd_grid = 0, adj_grid = 0;
+    int fwd_grid = 0, adj_grid = 0, adj_table_grid = 0;
     float last_ms = 0.f;
 };
 
@@ -109,11 +117,12 @@ rsx_status batch_release(rsx_batch *h)
         cudaStreamSynchronize(h->st);
     drop_graphs(h);
     free_layout_buffers(h);
-    void *dev[] = {h->d_pos,    h->d_ff,     h->d_q,      h->d_iq64,  h->d_iq32, h->d_target,
-                   h->d_sigma, h->d_lambda, h->d_chi2,   h->d_grad,  h->d_counter};
+    void *dev[] = {h->d_pos,    h->d_ff,     h->d_q,      h->d_iq64,    h->d_iq32,
+                   h->d_target, h->d_sigma, h->d_lambda, h->d_chi2,    h->d_grad,
+                   h->d_counter, h->d_adj_tab, h->d_adj_geom};
     for (void *x : dev)
         dev_free(x);
-    void *pin[] = {h->h_pos, h->h_iq, h->h_chi2, h->h_grad};
+    void *pin[] = {h->h_pos, h->h_iq, h->h_chi2, h->h_grad, h->h_adj_geom};
     for (void *x : pin)
         host_free_pinned(x);
     if (h->e0)
@@ -326,10 +335,26 @@ rsx_status enqueue_pass(rsx_batch *h, bool with_adjoint, int q_slab)
         l.chi2 = h->d_chi2;
         RSX_TRY_CUDA(launch_batch_loss(l, h->st), "batch loss");
         RSX_TRY_CUDA(cudaMemsetAsync(h->d_grad, 0, sizeof(double) * 3 * nbody, h->st), "grad");
-        const DebyeArgs g = batch_args(h, true);
-        RSX_TRY_CUDA(launch_batch_adjoint(g, h->d_adj_order, (int)h->adj_items.size(), q_slab,
-                                          h->uniform, h->d_counter + 2, h->adj_grid, h->st),
-                     "batch adjoint");
+        DebyeArgs g = batch_args(h, true);
+        if (h->adj_nodes > 0) {
+            g.adj_tab = h->d_adj_tab;
+            g.adj_nodes = h->adj_nodes;
+            g.adj_geom = h->d_adj_geom;
+            RSX_TRY_CUDA(cudaMemcpyAsync(h->d_adj_geom, h->h_adj_geom, sizeof(float) * 2,
+                                         cudaMemcpyHostToDevice, h->st),
+                         "adjoint table step");
+            const unsigned mask = h->n_types >= 32 ? 0xffffffffu : (1u << h->n_types) - 1u;
+            RSX_TRY_CUDA(launch_adjoint_tables(g, h->d_adj_tab, mask, h->n_members, h->st),
+                         "adjoint tables");
+            RSX_TRY_CUDA(launch_batch_adjoint_table(g, h->d_adj_order, (int)h->adj_items.size(),
+                                                    h->d_counter + 2, h->adj_table_grid, h->st),
+                         "batch adjoint");
+        } else {
+            RSX_TRY_CUDA(launch_batch_adjoint(g, h->d_adj_order, (int)h->adj_items.size(),
+                                              q_slab, h->uniform, h->d_counter + 2, h->adj_grid,
+                                              h->st),
+                         "batch adjoint");
+        }
         RSX_TRY_CUDA(cudaMemcpyAsync(h->h_chi2, h->d_chi2, sizeof(double) * h->n_members,
                                      cudaMemcpyDeviceToHost, h->st),
                      "read chi2");
@@ -350,6 +375,7 @@ rsx_status capture(rsx_batch *h, bool with_adjoint, cudaGraphExec_t *out)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
     h->fwd_grid *= sms;
     h->adj_grid = batch_adjoint_grid(h->q_slab, h->uniform, h->n_q, sms);
+    h->adj_table_grid = batch_adjoint_table_grid(sms);
     RSX_TRY_CUDA(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal),
                  "begin capture");
     rsx_status s = enqueue_pass(h, with_adjoint, h->q_slab);
@@ -406,6 +432,32 @@ rsx_status stage_bodies(rsx_batch *h, const rsx_body *bodies)
     for (int s = 0; s < h->n_total; ++s) {
         const rsx_body &b = bodies[h->perm[s]];
         h->h_pos[s] = make_float4(b.x, b.y, b.z, b.w);
+    }
+    // Adjoint tables: nodes for the widest member with q_max h <= 0.05.  The
+    // capacity grows (with headroom) only when a pass needs more nodes; the
+    // graphs are captured again then.  Past 1 GB the recurrence adjoint runs.
+    {
+        const double r_max = worst * 1.0001 + 1e-3;
+        const double need = std::max(16.0, std::ceil(r_max * h->q_max / 0.05) + 2.0);
+        if (need > h->adj_nodes) {
+            const double nodes = std::ceil(need * 1.25);
+            const double bytes = nodes * h->n_types * h->n_types * (double)h->n_members *
+                                 sizeof(float4);
+            dev_free(h->d_adj_tab);
+            h->d_adj_tab = nullptr;
+            const int before = h->adj_nodes;
+            h->adj_nodes = 0;
+            if (bytes <= 1024.0 * 1024 * 1024 && h->n_types <= 32 && h->n_members <= 65535 &&
+                dev_alloc((void **)&h->d_adj_tab, (size_t)bytes, "adjoint tables") == RSX_OK)
+                h->adj_nodes = (int)nodes;
+            if (h->adj_nodes != before)
+                drop_graphs(h);
+        }
+        if (h->adj_nodes > 0) {
+            const double step = r_max / (h->adj_nodes - 2);
+            h->h_adj_geom[0] = (float)step;
+            h->h_adj_geom[1] = (float)(1.0 / (float)step);
+        }
     }
     // theta_level() of the widest member selects the kernel instantiations
     // (the reduction-free seeds give the same results bit for bit).  It is a
@@ -500,6 +552,8 @@ rsx_status rsx_batch_create(const float *q, int n_q, const float *t_factors, int
     h->n_members = n_members;
     h->n_total = (int)total;
     h->q.assign(q, q + n_q);
+    for (int k = 0; k < n_q; ++k)
+        h->q_max = std::max(h->q_max, std::fabs((double)q[k]));
     h->ff.assign(t_factors, t_factors + (size_t)n_q * n_factors);
     h->sizes.assign(member_sizes, member_sizes + n_members);
     h->offsets.resize(n_members);
@@ -549,6 +603,8 @@ rsx_status rsx_batch_create(const float *q, int n_q, const float *t_factors, int
     RSX_A(h->d_chi2, sizeof(double) * M, "chi2");
     RSX_A(h->d_grad, sizeof(double) * 3 * nb, "gradient");
     RSX_A(h->d_counter, sizeof(int) * 4, "work counters");
+    RSX_A(h->d_adj_geom, sizeof(float) * 2, "adjoint table step");
+    RSX_P(h->h_adj_geom, sizeof(float) * 2, "pinned adjoint table step");
     RSX_P(h->h_pos, sizeof(float4) * nb, "pinned bodies");
     RSX_P(h->h_iq, sizeof(float) * M * n_q, "pinned curves");
     RSX_P(h->h_chi2, sizeof(double) * M, "pinned chi2");

@@ -39,10 +39,15 @@ cudaError_t launch_batch_forward_wide(const DebyeArgs &a, const int *work_order,
 cudaError_t launch_batch_adjoint(const DebyeArgs &a, const int *work_order, int n_work_items,
                                  int q_slab, bool uniform, int *counter, int grid,
                                  cudaStream_t st);
+// The pair pass of the adjoint through tabulated pair functions (the tables
+// are built by launch_adjoint_tables), persistent over counter.
+cudaError_t launch_batch_adjoint_table(const DebyeArgs &a, const int *work_order,
+                                       int n_work_items, int *counter, int grid, cudaStream_t st);
 cudaError_t launch_batch_assemble(const BatchAssembleArgs &a, cudaStream_t st);
 cudaError_t launch_batch_loss(const BatchLossArgs &a, cudaStream_t st);
 // CTAs of the persistent kernels that fit on the device at once
 int batch_forward_grid(int q_slab, bool uniform, int sms);
 int batch_adjoint_grid(int q_slab, bool uniform, int n_q, int sms);
+int batch_adjoint_table_grid(int sms);
 
 } // namespace rsx

@@ -54,11 +54,14 @@ struct DebyeArgs {
     // adjoint
     const float *lambda;     // [n_q] dL/dI(q)
     double *grad;            // [n][3] sorted-order FP64 gradient accumulators
-    // adjoint through tabulated pair functions: [n_types * n_types][adj_nodes]
-    // nodes (A, h A', B, h B') at r = b * adj_h, b = 0 .. adj_nodes - 1
+    // adjoint through tabulated pair functions: [member][n_types * n_types]
+    // [adj_nodes] nodes (A, h A', B, h B') at r = b * h, b = 0 .. adj_nodes - 1;
+    // h and 1/h are adj_h / adj_inv_h, or adj_geom[0] / [1] when adj_geom is set
+    // (a device copy, for captured graphs whose step changes between replays)
     const float4 *adj_tab;
     int adj_nodes;
     float adj_h, adj_inv_h;
+    const float *adj_geom;
 };
 
 // Per-q constants needed to assemble I(q) from the cross sums.
@@ -119,6 +122,9 @@ cudaError_t launch_assemble(const AssembleArgs &a, cudaStream_t st);
 // type pairs into `tab` ([n_types^2][adj_nodes] float4), then the pair pass
 cudaError_t launch_adjoint_table(const DebyeArgs &a, float4 *tab, unsigned type_mask,
                                  cudaStream_t st);
+// the tables alone, for `n_members` members (batched passes)
+cudaError_t launch_adjoint_tables(const DebyeArgs &a, float4 *tab, unsigned type_mask,
+                                  int n_members, cudaStream_t st);
 cudaError_t launch_delta(const DeltaArgs &a, int q_slab, bool uniform, cudaStream_t st);
 // partial sums per q that launch_delta writes (the assembly's n_parts)
 int delta_parts(const DeltaArgs &a, int q_slab, bool uniform);
