@@ -88,18 +88,22 @@ cudaError_t launch_adjoint(const DebyeArgs &a, int q_slab, bool uniform, bool wa
 // every present type pair (t_i <= t_j), then one pair pass
 // ----------------------------------------------------------------------------
 
-// grid (nodes / 128, n_types * n_types, members): member m's tables from its
-// dL/dI row lambda + m * n_q
+// One warp per node; grid (nodes / 4, n_types * n_types, members): member
+// m's tables from its dL/dI row lambda + m * n_q.  Whole warps return
+// together (the node sum shuffles over the warp).
 __global__ void __launch_bounds__(128)
     adjoint_table_kernel(const DebyeArgs a, float4 *tab, unsigned type_mask)
 {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int b = blockIdx.x * 4 + (threadIdx.x >> 5);
     const int ti = blockIdx.y / a.n_types, tj = blockIdx.y % a.n_types, m = blockIdx.z;
     if (b >= a.adj_nodes || tj < ti || !((type_mask >> ti) & 1u) || !((type_mask >> tj) & 1u))
         return;
     const float h = a.adj_geom ? a.adj_geom[0] : a.adj_h;
     const size_t tp = (size_t)m * a.n_types * a.n_types + (size_t)(ti * a.n_types + tj);
-    tab[tp * a.adj_nodes + b] = adjoint_table_node(a, a.lambda + (size_t)m * a.n_q, ti, tj, b, h);
+    const float4 v = adjoint_table_node(a, a.lambda + (size_t)m * a.n_q, ti, tj, b, h, lane);
+    if (lane == 0)
+        tab[tp * a.adj_nodes + b] = v;
 }
 
 template <int IL>
@@ -113,7 +117,7 @@ cudaError_t launch_adjoint_tables(const DebyeArgs &a, float4 *tab, unsigned type
 {
     if (a.n_types > 32 || a.adj_nodes < 2 || n_members < 1 || n_members > 65535)
         return cudaErrorInvalidValue;
-    const dim3 g((a.adj_nodes + 127) / 128, a.n_types * a.n_types, n_members);
+    const dim3 g((a.adj_nodes + 3) / 4, a.n_types * a.n_types, n_members);
     adjoint_table_kernel<<<g, 128, 0, st>>>(a, tab, type_mask);
     count_launch();
     return cudaGetLastError();
@@ -126,7 +130,7 @@ cudaError_t launch_adjoint_table(const DebyeArgs &a, float4 *tab, unsigned type_
         return cudaSuccess;
     if (a.n_types > 32 || a.adj_nodes < 2)
         return cudaErrorInvalidValue;
-    const dim3 g((a.adj_nodes + 127) / 128, a.n_types * a.n_types, 1);
+    const dim3 g((a.adj_nodes + 3) / 4, a.n_types * a.n_types, 1);
     adjoint_table_kernel<<<g, 128, 0, st>>>(a, tab, type_mask);
     count_launch();
     cudaError_t e = cudaGetLastError();

@@ -1057,16 +1057,17 @@ __device__ __forceinline__ void adj_scatter(const AdjPair &p, float A, float B, 
 // picks) -- smaller than the FP32 recurrence's.  A pair then costs two table
 // loads and ~25 FP32 operations instead of 4 per q.
 
-// Node b of the table at r_b = b h (exact in double): A, h dA/dr, B, h dB/dr.
-// sin/cos(q r_b) in FP32 with the rounding of q r_b folded in as the low part
-// (r_b itself is carried as hi + lo), sums in FP64.
+// Node b of the table at r_b = b h (exact in double): A, h dA/dr, B, h dB/dr,
+// by one warp (lane l sums q l, l + 32, ...; FP64 partials combined by
+// shuffles; the result is valid in every lane).  sin/cos(q r_b) in FP32 with
+// the rounding of q r_b folded in as the low part (r_b is carried as hi + lo).
 __device__ __forceinline__ float4 adjoint_table_node(const DebyeArgs &a, const float *lambda,
-                                                     int ti, int tj, int b, float h)
+                                                     int ti, int tj, int b, float h, int lane)
 {
     const double rb = (double)b * (double)h;
     const float r_hi = (float)rb, r_lo = (float)(rb - (double)r_hi);
     double A = 0.0, dA = 0.0, B = 0.0, dB = 0.0;
-    for (int k = 0; k < a.n_q; ++k) {
+    for (int k = lane; k < a.n_q; k += 32) {
         const float qk = a.q[k];
         if (qk == 0.f)
             continue; // d sinc(q r) / dr = 0 at q = 0: no term on either side
@@ -1081,6 +1082,13 @@ __device__ __forceinline__ float4 adjoint_table_node(const DebyeArgs &a, const f
         dA -= (double)al * qk * s;
         B += be * s;
         dB += be * qk * c;
+    }
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) {
+        A += __shfl_xor_sync(0xffffffffu, A, m);
+        dA += __shfl_xor_sync(0xffffffffu, dA, m);
+        B += __shfl_xor_sync(0xffffffffu, B, m);
+        dB += __shfl_xor_sync(0xffffffffu, dB, m);
     }
     return make_float4((float)A, (float)(h * dA), (float)B, (float)(h * dB));
 }
@@ -1109,6 +1117,7 @@ __device__ __forceinline__ void adjoint_table_eval(const float4 *tab, int n_node
 template <int IL>
 __device__ __forceinline__ void adjoint_table_item(const DebyeArgs &a, int item_idx)
 {
+    static_assert(3 * IL <= 16, "the J side of a step is reduce-scattered as 16 values");
     __shared__ float4 s_pos[kBlockAtoms];
     __shared__ float s_gj[kBlockAtoms][3];
 
@@ -1151,12 +1160,30 @@ __device__ __forceinline__ void adjoint_table_item(const DebyeArgs &a, int item_
                 pair_r(pi, s_pos[j], p[v].r, p[v].rinv, p[v].dx, p[v].dy, p[v].dz);
                 adjoint_table_eval(tab, n_nodes, h, inv_h, p[v].r, A[v], B[v]);
             }
+            // G d of the step's pairs (zero past the block's end); the I side
+            // stays in registers, the J side (IL x 3 values) is reduce-scattered
+            // over the warp in one pass and added to shared memory by the lanes
+            // that hold the sums
+            float w[16];
 #pragma unroll
             for (int v = 0; v < IL; ++v) {
-                if (jj + v < bj.len) // uniform over the warp
-                    adj_scatter(p[v], A[v], B[v], valid_i && (!diag || jj + v > tid), gi0, gi1,
-                                gi2, s_gj, jj + v, lane);
+                const bool use = jj + v < bj.len && valid_i && (!diag || jj + v > tid);
+                float G = 2.0f * p[v].rinv * p[v].rinv * fmaf(-B[v], p[v].rinv, A[v]);
+                G = use ? G : 0.f;
+                w[3 * v + 0] = G * p[v].dx;
+                w[3 * v + 1] = G * p[v].dy;
+                w[3 * v + 2] = G * p[v].dz;
+                gi0 -= w[3 * v + 0];
+                gi1 -= w[3 * v + 1];
+                gi2 -= w[3 * v + 2];
             }
+#pragma unroll
+            for (int k = 3 * IL; k < 16; ++k)
+                w[k] = 0.f;
+            warp_reduce_scatter<16>(w, lane);
+            const int k = lane & 15, v = k / 3;
+            if (lane < 16 && k < 3 * IL && jj + v < bj.len)
+                atomicAdd(&s_gj[jj + v][k - 3 * v], w[0]);
         }
         __syncthreads();
         if (tid < bj.len) {
