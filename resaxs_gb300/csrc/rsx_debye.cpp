@@ -206,6 +206,9 @@ struct rsx_debye {
     float *d_lambda = nullptr;
     float4 *d_adj_tab = nullptr; // tabulated pair functions (no water)
     size_t adj_tab_cap = 0;      // float4
+    // gridded pair-distance histograms of the non-uniform forward
+    double *d_grid = nullptr;
+    size_t grid_cap = 0; // doubles
 
     // pinned staging
     float4 *h_pos = nullptr;
@@ -425,16 +428,59 @@ AssembleArgs assemble_args(rsx_debye *h, int n_parts, int accumulate)
 }
 
 // Forward over the device-resident bodies (no host transfers).
+// Node grid of the gridded forward / tabulated adjoint: nodes r = b h covering
+// the tracked bounding-box diagonal with q_max h <= 0.05.  False for an empty
+// or non-finite extent.
+bool pair_grid(const rsx_debye *h, double *nodes, double *step)
+{
+    double d2 = 0.0;
+    for (int d = 0; d < 3; ++d) {
+        const double e = (double)h->hi[d] - (double)h->lo[d];
+        if (!std::isfinite(e))
+            return false;
+        d2 += e > 0.0 ? e * e : 0.0;
+    }
+    double q_max = 0.0;
+    for (float q : h->q)
+        q_max = std::max(q_max, std::fabs((double)q));
+    const double r_max = std::sqrt(d2) * 1.0001 + 1e-3;
+    *nodes = std::max(16.0, std::ceil(r_max * q_max / 0.05) + 2.0);
+    *step = r_max / (*nodes - 2.0);
+    return *step > 0.0 && std::isfinite(*step);
+}
+
+unsigned present_types(const rsx_debye *h)
+{
+    unsigned mask = 0;
+    for (int t = 0; t < h->n_types && t < 32; ++t)
+        if (h->L.type_count[t] > 0)
+            mask |= 1u << t;
+    return mask;
+}
+
 rsx_status forward_device(rsx_debye *h)
 {
-    const DebyeArgs a = debye_args(h);
+    DebyeArgs a = debye_args(h);
+    // non-uniform grids without water: the gridded pair-distance distribution
+    double nodes = 0.0, step = 0.0;
+    const bool gridded = !h->uniform && !has_water(h) && h->n_types <= 32 &&
+                         pair_grid(h, &nodes, &step) && nodes <= forward_grid_max_nodes();
+    if (gridded)
+        RSX_TRY(ensure(&h->d_grid, h->grid_cap,
+                       (size_t)nodes * 2 * h->n_types * h->n_types, "forward histograms"));
     if (h->timing)
         RSX_TRY_CUDA(cudaEventRecord(h->ev_k0, h->st), "event");
-    RSX_LAUNCH(launch_forward(a, forward_slab(h), h->uniform, has_water(h), h->st, &h->aux),
-               "forward kernel");
+    if (gridded)
+        RSX_LAUNCH(launch_forward_grid(a, h->d_grid, (int)nodes, (float)step, present_types(h),
+                                       h->st),
+                   "forward kernels");
+    else
+        RSX_LAUNCH(launch_forward(a, forward_slab(h), h->uniform, has_water(h), h->st, &h->aux),
+                   "forward kernel");
     if (h->timing)
         RSX_TRY_CUDA(cudaEventRecord(h->ev_k1, h->st), "event");
-    RSX_LAUNCH(launch_assemble(assemble_args(h, a.n_items, 0), h->st), "assemble kernel");
+    RSX_LAUNCH(launch_assemble(assemble_args(h, gridded ? 1 : a.n_items, 0), h->st),
+               "assemble kernel");
     return RSX_OK;
 }
 
@@ -699,7 +745,7 @@ rsx_status release(rsx_debye *h)
                    h->d_q,          h->d_blocks,    h->d_items,      h->d_adj_items,
                    h->d_partial,    h->d_iq64,      h->d_iq64_saved, h->d_iq32,
                    h->d_type_count, h->d_rsasa_sum, h->d_moved,      h->d_grad,
-                   h->d_lambda,     h->d_adj_tab};
+                   h->d_lambda,     h->d_adj_tab,   h->d_grid};
     for (void *p : dev)
         dev_free(p);
     void *pinned[] = {h->h_pos, h->h_iq, h->h_iq64, h->h_grad, h->h_moved, h->h_rsasa};
@@ -1080,30 +1126,18 @@ rsx_status rsx_debye_timing(rsx_debye *h, float *ms_pair_kernel, float *ms_call)
     return ok();
 }
 
-// Geometry of the adjoint's pair-function tables: nodes at r = b h covering
-// the tracked bounding-box diagonal, with q_max h <= 0.05 (interpolation error
-// below 1.6e-8 of sum|alpha|).  False when the tables would not fit the cap
-// (the recurrence adjoint is used then).
+// Geometry of the adjoint's pair-function tables (pair_grid's nodes).  False
+// when the tables would not fit the cap (the recurrence adjoint is used then).
 static bool adjoint_table_geometry(const rsx_debye *h, int *nodes, float *step)
 {
-    double d2 = 0.0;
-    for (int d = 0; d < 3; ++d) {
-        const double e = (double)h->hi[d] - (double)h->lo[d];
-        if (!std::isfinite(e))
-            return false;
-        d2 += e > 0.0 ? e * e : 0.0;
-    }
-    double q_max = 0.0;
-    for (float q : h->q)
-        q_max = std::max(q_max, std::fabs((double)q));
-    const double r_max = std::sqrt(d2) * 1.0001 + 1e-3;
-    const double want = std::ceil(r_max * q_max / 0.05) + 2.0;
-    const double n = std::max(16.0, want);
+    double n = 0.0, st = 0.0;
+    if (!pair_grid(h, &n, &st))
+        return false;
     const double bytes = n * h->n_types * h->n_types * sizeof(float4);
     if (!(n < 1e7) || bytes > 512.0 * 1024 * 1024)
         return false;
     *nodes = (int)n;
-    *step = (float)(r_max / (n - 2.0));
+    *step = (float)st;
     return *step > 0.f;
 }
 
@@ -1133,10 +1167,7 @@ static rsx_status backward_impl(rsx_debye *h, const float *dl_diq)
         a.adj_h = step;
         a.adj_inv_h = 1.0f / step;
     }
-    unsigned type_mask = 0;
-    for (int t = 0; t < h->n_types && t < 32; ++t)
-        if (h->L.type_count[t] > 0)
-            type_mask |= 1u << t;
+    const unsigned type_mask = present_types(h);
     if (h->timing)
         RSX_TRY_CUDA(cudaEventRecord(h->ev_k0, h->st), "event");
     if (tables)
