@@ -1,6 +1,6 @@
-// Forward on q grids without the uniform-step recurrence (non-uniform grids,
-// no water) through the gridded pair-distance distribution.  Written from
-// scratch for this project.
+// Forward on q grids without the uniform-step recurrence (non-uniform grids)
+// through the gridded pair-distance distribution.  Written from scratch for
+// this project.
 //
 // For one type pair the cross sum needs sum_p g_q(r_p), g_q(r) = sin(q r)/r,
 // for every q.  Each pair deposits its cubic Hermite weights onto the two
@@ -20,6 +20,11 @@
 // item has at most 128 x n bodies' pairs).  A weight is quantised to 2^-32
 // (2.3e-10).  The items' sums are then added into FP64 global histograms
 // (relative rounding ~1e-16 per add).
+//
+// With the implicit water term a body's factor is f~ = f_t + w rsasa f_w, so
+// f~_i f~_j = f_ti f_tj + w f_w (rsasa_i f_tj + rsasa_j f_ti) + w^2 f_w^2
+// rsasa_i rsasa_j: the pairs deposit four histograms, weighted by 1, rsasa_i,
+// rsasa_j and rsasa_i rsasa_j, and the per-q factors apply at evaluation.
 #include "debye_device.cuh"
 
 namespace rsx {
@@ -31,16 +36,24 @@ __device__ __forceinline__ unsigned long long grid_fixed(float w)
     return (unsigned long long)__double2ll_rn((double)w * kGridUnit);
 }
 
+// Histograms per type pair: 1 without water, 4 with (weights 1, rsasa_i,
+// rsasa_j, rsasa_i rsasa_j), each [2][nodes] (W then D).
+template <bool WATER>
+constexpr int kGridHists = WATER ? 4 : 1;
+
 // One CTA per forward work item (one type pair): the item's pairs deposit into
-// shared-memory histograms [2][nodes] (W then D), which are then added to the
-// type pair's FP64 global histograms.
+// shared-memory histograms, which are then added to the type pair's FP64
+// global histograms [n_types^2][hists][2][nodes].
+template <bool WATER>
 __global__ void __launch_bounds__(kBlockAtoms)
     forward_grid_deposit_kernel(const DebyeArgs a, double *hist, int nodes, float h, float inv_h)
 {
-    extern __shared__ unsigned long long s_hist[]; // [2 * nodes]
+    constexpr int NH = kGridHists<WATER>;
+    extern __shared__ unsigned long long s_hist[]; // [NH][2][nodes]
     __shared__ float4 s_pos[kBlockAtoms];
+    __shared__ float s_rs[WATER ? kBlockAtoms : 1];
     const int tid = threadIdx.x;
-    for (int k = tid; k < 2 * nodes; k += kBlockAtoms)
+    for (int k = tid; k < NH * 2 * nodes; k += kBlockAtoms)
         s_hist[k] = 0ull;
     const PairItem it = a.items[blockIdx.x];
     const BlockDesc bi = a.blocks[it.bi];
@@ -48,12 +61,16 @@ __global__ void __launch_bounds__(kBlockAtoms)
     const int i = bi.start + tid;
     const bool valid_i = tid < bi.len;
     const float4 pi = valid_i ? a.pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float rs_i = (WATER && valid_i) ? a.rsasa[i] : 0.f;
 
     for (int b = it.bj_begin; b < it.bj_end; ++b) {
         const BlockDesc bj = a.blocks[b];
         __syncthreads(); // also orders the histogram clearing before the first adds
-        if (tid < bj.len)
+        if (tid < bj.len) {
             s_pos[tid] = a.pos[bj.start + tid];
+            if (WATER)
+                s_rs[tid] = a.rsasa[bj.start + tid];
+        }
         __syncthreads();
         const bool diag = (b == it.bi);
         if (!valid_i)
@@ -70,15 +87,27 @@ __global__ void __launch_bounds__(kBlockAtoms)
             const float h00 = 1.0f - h01;
             const float h10 = t3 - 2.0f * t2 + t;
             const float h11 = t3 - t2;
-            atomicAdd(&s_hist[n], grid_fixed(h00));
-            atomicAdd(&s_hist[n + 1], grid_fixed(h01));
-            atomicAdd(&s_hist[nodes + n], grid_fixed(h10));
-            atomicAdd(&s_hist[nodes + n + 1], grid_fixed(h11));
+            float m[NH];
+            m[0] = 1.0f;
+            if (WATER) {
+                const float rs_j = s_rs[jj];
+                m[1] = rs_i;
+                m[2] = rs_j;
+                m[3] = rs_i * rs_j;
+            }
+#pragma unroll
+            for (int c = 0; c < NH; ++c) {
+                unsigned long long *hc = s_hist + c * 2 * nodes;
+                atomicAdd(&hc[n], grid_fixed(m[c] * h00));
+                atomicAdd(&hc[n + 1], grid_fixed(m[c] * h01));
+                atomicAdd(&hc[nodes + n], grid_fixed(m[c] * h10));
+                atomicAdd(&hc[nodes + n + 1], grid_fixed(m[c] * h11));
+            }
         }
     }
     __syncthreads();
-    double *dst = hist + (size_t)(bi.type * a.n_types + tj) * 2 * nodes;
-    for (int k = tid; k < 2 * nodes; k += kBlockAtoms) {
+    double *dst = hist + (size_t)(bi.type * a.n_types + tj) * NH * 2 * nodes;
+    for (int k = tid; k < NH * 2 * nodes; k += kBlockAtoms) {
         const long long v = (long long)s_hist[k];
         if (v != 0)
             atomicAdd(dst + k, (double)v / kGridUnit);
@@ -86,14 +115,17 @@ __global__ void __launch_bounds__(kBlockAtoms)
 }
 
 // One CTA per q: partial[k][0] = sum over the present type pairs of
-// f_ti(q) f_tj(q) sum_b (W_b g(r_b) + D_b h g'(r_b)), in FP64, with
+// sum_c F_c(q) sum_b (W_cb g(r_b) + D_cb h g'(r_b)), in FP64, with F_0 =
+// f_ti f_tj (and with water F_1 = w f_w f_tj, F_2 = w f_w f_ti, F_3 = (w f_w)^2),
 // g(r) = sin(q r)/r, g'(r) = (q r cos(q r) - sin(q r)) / r^2 and, at r = 0,
 // g = q, g' = 0.  sin/cos(q r_b) in FP32 with the rounding of q r_b folded in
 // (r_b = b h is exact in double and carried as hi + lo).
+template <bool WATER>
 __global__ void __launch_bounds__(256)
     forward_grid_eval_kernel(const DebyeArgs a, const double *hist, int nodes, float h,
                              unsigned type_mask)
 {
+    constexpr int NH = kGridHists<WATER>;
     __shared__ double s_w[8];
     const int k = blockIdx.x;
     const float qk = a.q[k];
@@ -104,9 +136,12 @@ __global__ void __launch_bounds__(256)
         const int ti = tp / T, tj = tp - ti * T;
         if (tj < ti || !((type_mask >> ti) & 1u) || !((type_mask >> tj) & 1u))
             continue;
-        const double *row = hist + (size_t)tp * 2 * nodes;
-        const double W = row[b], D = row[nodes + b];
-        if (W == 0.0 && D == 0.0)
+        const double *row = hist + (size_t)tp * NH * 2 * nodes;
+        bool any = false;
+#pragma unroll
+        for (int c = 0; c < NH; ++c)
+            any = any || row[c * 2 * nodes + b] != 0.0 || row[c * 2 * nodes + nodes + b] != 0.0;
+        if (!any)
             continue;
         double g, dg;
         if (b == 0) {
@@ -125,8 +160,18 @@ __global__ void __launch_bounds__(256)
             g = (double)s * rinv;
             dg = ((double)qk * (double)c - g) * rinv;
         }
-        const double f = (double)a.ff[(size_t)k * T + ti] * (double)a.ff[(size_t)k * T + tj];
-        acc += f * (W * g + D * (double)h * dg);
+        const double fi = a.ff[(size_t)k * T + ti], fj = a.ff[(size_t)k * T + tj];
+        double F[NH];
+        F[0] = fi * fj;
+        if (WATER) {
+            const double fw = (double)a.water_weight * (double)a.ff[(size_t)k * T + a.water_index];
+            F[1] = fw * fj;
+            F[2] = fw * fi;
+            F[3] = fw * fw;
+        }
+#pragma unroll
+        for (int c = 0; c < NH; ++c)
+            acc += F[c] * (row[c * 2 * nodes + b] * g + row[c * 2 * nodes + nodes + b] * (double)h * dg);
     }
 #pragma unroll
     for (int m = 16; m >= 1; m >>= 1)
@@ -142,40 +187,55 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-int forward_grid_max_nodes()
+int forward_grid_hists(bool water) { return water ? kGridHists<true> : kGridHists<false>; }
+
+int forward_grid_max_nodes(bool water)
 {
-    // two 8-byte histograms per node in the deposit kernel's dynamic shared
-    // memory, below the 227 KB a CTA may opt into (the static part is 2 KB)
-    return (200 * 1024) / 16;
+    // 2 x hists 8-byte counters per node in the deposit kernel's dynamic
+    // shared memory, below the 227 KB a CTA may opt into (static part < 3 KB)
+    return (200 * 1024) / (16 * forward_grid_hists(water));
 }
 
-cudaError_t launch_forward_grid(const DebyeArgs &a, double *hist, int nodes, float h,
-                                unsigned type_mask, cudaStream_t st)
+template <bool WATER>
+static cudaError_t grid_launch(const DebyeArgs &a, double *hist, int nodes, float h,
+                               unsigned type_mask, cudaStream_t st)
 {
-    if (nodes < 2 || nodes > forward_grid_max_nodes() || a.n_types > 32)
-        return cudaErrorInvalidValue;
-    cudaError_t e =
-        cudaMemsetAsync(hist, 0, sizeof(double) * 2 * (size_t)nodes * a.n_types * a.n_types, st);
-    if (e != cudaSuccess)
-        return e;
+    cudaError_t e = cudaSuccess;
     if (a.n_items > 0) {
-        const size_t smem = sizeof(unsigned long long) * 2 * (size_t)nodes;
+        const size_t smem = sizeof(unsigned long long) * kGridHists<WATER> * 2 * (size_t)nodes;
         if (smem > 48 * 1024) {
-            e = cudaFuncSetAttribute(forward_grid_deposit_kernel,
+            e = cudaFuncSetAttribute(forward_grid_deposit_kernel<WATER>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess)
                 return e;
         }
-        forward_grid_deposit_kernel<<<a.n_items, kBlockAtoms, smem, st>>>(a, hist, nodes, h,
-                                                                          1.0f / h);
+        forward_grid_deposit_kernel<WATER><<<a.n_items, kBlockAtoms, smem, st>>>(a, hist, nodes, h,
+                                                                                 1.0f / h);
         count_launch();
         e = cudaGetLastError();
         if (e != cudaSuccess)
             return e;
     }
-    forward_grid_eval_kernel<<<a.n_q, 256, 0, st>>>(a, hist, nodes, h, type_mask);
+    forward_grid_eval_kernel<WATER><<<a.n_q, 256, 0, st>>>(a, hist, nodes, h, type_mask);
     count_launch();
     return cudaGetLastError();
+}
+
+cudaError_t launch_forward_grid(const DebyeArgs &a, double *hist, int nodes, float h,
+                                unsigned type_mask, bool water, cudaStream_t st)
+{
+    if (nodes < 2 || nodes > forward_grid_max_nodes(water) || a.n_types > 32 ||
+        (water && !a.rsasa))
+        return cudaErrorInvalidValue;
+    const cudaError_t e =
+        cudaMemsetAsync(hist, 0,
+                        sizeof(double) * forward_grid_hists(water) * 2 * (size_t)nodes *
+                            a.n_types * a.n_types,
+                        st);
+    if (e != cudaSuccess)
+        return e;
+    return water ? grid_launch<true>(a, hist, nodes, h, type_mask, st)
+                 : grid_launch<false>(a, hist, nodes, h, type_mask, st);
 }
 
 } // namespace rsx

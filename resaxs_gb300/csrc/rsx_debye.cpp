@@ -461,18 +461,20 @@ unsigned present_types(const rsx_debye *h)
 rsx_status forward_device(rsx_debye *h)
 {
     DebyeArgs a = debye_args(h);
-    // non-uniform grids without water: the gridded pair-distance distribution
+    // non-uniform grids: the gridded pair-distance distribution
+    const bool water = has_water(h);
     double nodes = 0.0, step = 0.0;
-    const bool gridded = !h->uniform && !has_water(h) && h->n_types <= 32 &&
-                         pair_grid(h, &nodes, &step) && nodes <= forward_grid_max_nodes();
+    const bool gridded = !h->uniform && h->n_types <= 32 && pair_grid(h, &nodes, &step) &&
+                         nodes <= forward_grid_max_nodes(water);
     if (gridded)
         RSX_TRY(ensure(&h->d_grid, h->grid_cap,
-                       (size_t)nodes * 2 * h->n_types * h->n_types, "forward histograms"));
+                       (size_t)nodes * forward_grid_hists(water) * 2 * h->n_types * h->n_types,
+                       "forward histograms"));
     if (h->timing)
         RSX_TRY_CUDA(cudaEventRecord(h->ev_k0, h->st), "event");
     if (gridded)
         RSX_LAUNCH(launch_forward_grid(a, h->d_grid, (int)nodes, (float)step, present_types(h),
-                                       h->st),
+                                       water, h->st),
                    "forward kernels");
     else
         RSX_LAUNCH(launch_forward(a, forward_slab(h), h->uniform, has_water(h), h->st, &h->aux),

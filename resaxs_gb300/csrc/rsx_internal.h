@@ -123,11 +123,12 @@ cudaError_t launch_assemble(const AssembleArgs &a, cudaStream_t st);
 cudaError_t launch_adjoint_table(const DebyeArgs &a, float4 *tab, unsigned type_mask,
                                  cudaStream_t st);
 // forward through the gridded pair-distance distribution (grid_kernels.cu):
-// non-uniform q grids without water; writes partial[k][0] (one part per q)
-// from FP64 histograms `hist` ([n_types^2][2][nodes]) on nodes r = b h
-int forward_grid_max_nodes();
+// non-uniform q grids; writes partial[k][0] (one part per q) from FP64
+// histograms `hist` ([n_types^2][hists][2][nodes]) on nodes r = b h
+int forward_grid_hists(bool water);
+int forward_grid_max_nodes(bool water);
 cudaError_t launch_forward_grid(const DebyeArgs &a, double *hist, int nodes, float h,
-                                unsigned type_mask, cudaStream_t st);
+                                unsigned type_mask, bool water, cudaStream_t st);
 // the tables alone, for `n_members` members (batched passes)
 cudaError_t launch_adjoint_tables(const DebyeArgs &a, float4 *tab, unsigned type_mask,
                                   int n_members, cudaStream_t st);

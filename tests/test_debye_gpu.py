@@ -167,6 +167,28 @@ def test_water_term_wide_slabs(saxs, oracle_lib, q_slab, n_q, ww):
     assert rel(out64, ref) < TOL
 
 
+@pytest.mark.parametrize("ww,n", [(0.0, 1500), (0.7, 1500), (-1.5, 900), (3.0, 600)])
+def test_nonuniform_grid_gridded_forward(saxs, oracle_lib, ww, n):
+    """Non-uniform q grids run through the gridded pair-distance
+    distribution (Hermite deposits on an r grid with q_max h <= 0.05, the
+    sums over q evaluated on the nodes), with and without water; FP64 oracle
+    at the grid's own q values."""
+    w = W.make_config(2, seed=17, n_override=n)
+    rng = np.random.default_rng(n)
+    q = np.sort(rng.uniform(0, 0.6, 77)).astype(np.float32)
+    q[0] = 0.0
+    ff = W.exp_form_factors(q, W.Z5, rng.uniform(0.5, 2.0, 5))
+    rs = rng.uniform(0, 1, w.n).astype(np.float32)
+    with saxs.Debye(q, ff, w.n) as d:
+        if ww != 0.0:
+            d.set_water(ww, 4, rs)
+        d.calc(w.bodies)
+        out64 = d.curve_f64()
+        assert not d.config()["uniform_q"]
+    kw = dict(rsasa=rs, water_weight=ww, water_index=4) if ww != 0.0 else {}
+    assert rel(out64, oracle_lib.debye_f64(q, w.bodies, ff, **kw)) < TOL
+
+
 def test_small_item_cap_forces_chunking(saxs, oracle_lib):
     w = W.make_config(2, seed=15, n_override=1500)
     _, _, cfg1 = gpu_curve(saxs, w.q, w.ff, w.bodies)
