@@ -114,6 +114,41 @@ def test_batch_chi2_gradients(oracle_lib):
         off += len(m)
 
 
+def test_batch_adjoint_tables_follow_the_extent(oracle_lib):
+    """The batched adjoint reads per-member pair-function tables whose node
+    count is fixed in the captured graph and whose step each pass sends to
+    the device.  Stretching one member 8x needs more nodes (new capacity, new
+    graph); compacting it again replays that graph with a smaller step.  The
+    chi^2 gradients (targets: displaced copies, sigma = 1 % of the target, so
+    that dL/dI is insensitive to the curves' rounding) must match the FP64
+    gradient on every pass."""
+    from resaxs_gb300.batch import DebyeBatch
+    q, ff, members = W.batch_members(n_members=3, seed=9, n_lo=150, n_hi=300)
+    stretched = [m.copy() for m in members]
+    stretched[1][:, :3] *= np.float32(8.0)
+    rng = np.random.default_rng(3)
+    with DebyeBatch(q, ff, [len(m) for m in members]) as b:
+        for ms in (members, stretched, members):
+            tgt, sig = [], []
+            for m in ms:
+                tb = m.copy()
+                tb[:, :3] += rng.normal(0, 1.0, (len(m), 3)).astype(np.float32)
+                it = oracle_lib.debye_f64(q, tb, ff).astype(np.float32)
+                tgt.append(it)
+                sig.append((0.01 * it).astype(np.float32))
+            b.set_targets(np.stack(tgt), np.stack(sig))
+            _, _, grad = b.forward_chi2_backward(ms)
+            off = 0
+            for i, m in enumerate(ms):
+                iq = oracle_lib.debye_f64(q, m, ff)
+                s = sig[i].astype(np.float64)
+                lam = 2 * (iq - tgt[i]) / s ** 2
+                g_ref = oracle_lib.debye_grad_f64(q, lam, m, ff)
+                g = grad[off:off + len(m)].astype(np.float64)
+                assert np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref) < 1e-4, i
+                off += len(m)
+
+
 def test_batch_errors():
     from resaxs_gb300 import _lib
     from resaxs_gb300.batch import DebyeBatch
