@@ -143,6 +143,10 @@ typedef struct rsx_debye_options {
     int force_general_q; /* 1: never use the uniform-grid recurrence */
     int timing;          /* 1: record CUDA events around the pair kernel */
     int autotune;        /* 1: time the q-slab candidates on first use and cache the winner */
+    int no_pair_tables;  /* 1: evaluate every pair*q term instead of the tabulated pair
+                            functions (adjoint) and the gridded pair-distance distribution
+                            (forward on non-uniform grids): the recurrence adjoint and the
+                            direct-sine forward, at their pair*q cost */
 } rsx_debye_options;
 
 /* Forgets every autotuned tile choice of this process (the file named by

@@ -48,7 +48,7 @@ class ResaxsError(RuntimeError):
 class DebyeOptions(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("q_slab", ctypes.c_int), ("max_items", ctypes.c_int),
                 ("force_general_q", ctypes.c_int), ("timing", ctypes.c_int),
-                ("autotune", ctypes.c_int)]
+                ("autotune", ctypes.c_int), ("no_pair_tables", ctypes.c_int)]
 
 
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")

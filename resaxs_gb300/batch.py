@@ -14,7 +14,7 @@ __all__ = ["DebyeBatch"]
 
 class DebyeBatch:
     def __init__(self, q, factors, member_sizes, *, device: int = -1, q_slab: int = 0,
-                 autotune: bool = False, force_general_q: bool = False):
+                 autotune: bool = False, force_general_q: bool = False, pair_tables: bool = True):
         self.q = np.ascontiguousarray(q, np.float32)
         factors = np.ascontiguousarray(factors, np.float32)
         self.sizes = np.ascontiguousarray(member_sizes, np.int32)
@@ -28,6 +28,7 @@ class DebyeBatch:
         opts.q_slab = q_slab
         opts.autotune = int(autotune)
         opts.force_general_q = int(force_general_q)
+        opts.no_pair_tables = int(not pair_tables)
         h = ctypes.c_void_p()
         check(lib().rsx_batch_create(self.q, self.n_q, factors.reshape(-1), factors.shape[1],
                                      self.sizes, self.n_members, ctypes.byref(opts),

@@ -557,6 +557,7 @@ int main(int argc, char **argv)
             rsx_debye_default_options(&o);
             o.device = device;
             o.force_general_q = 1;
+            o.no_pair_tables = 1; // per pair*q, not the gridded distribution
             std::vector<float> tab(q.size() * 16), host(q.size());
             check(rsx_ff_atomic_table(q.data(), (int)q.size(), 0.0f, 1.0f, tab.data()));
             rsx_debye *h = nullptr;

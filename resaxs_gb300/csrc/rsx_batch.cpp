@@ -73,6 +73,7 @@ struct rsx_batch {
     // adjoint through tabulated pair functions: the node count is a capacity
     // fixed in the captured graphs (0: the recurrence adjoint); the step of a
     // pass travels through h_adj_geom -> d_adj_geom ([h, 1/h]) at replay
+    bool pair_tables = true; // 0: the recurrence adjoint
     float4 *d_adj_tab = nullptr;
     int adj_nodes = 0;
     float *h_adj_geom = nullptr, *d_adj_geom = nullptr;
@@ -439,7 +440,7 @@ rsx_status stage_bodies(rsx_batch *h, const rsx_body *bodies)
     {
         const double r_max = worst * 1.0001 + 1e-3;
         const double need = std::max(16.0, std::ceil(r_max * h->q_max / 0.05) + 2.0);
-        if (need > h->adj_nodes) {
+        if (h->pair_tables && need > h->adj_nodes) {
             const double nodes = std::ceil(need * 1.25);
             const double bytes = nodes * h->n_types * h->n_types * (double)h->n_members *
                                  sizeof(float4);
@@ -573,6 +574,7 @@ rsx_status rsx_batch_create(const float *q, int n_q, const float *t_factors, int
     if (!h->uniform && h->q_slab > 32)
         h->q_slab = 32;
     h->autotune = o.autotune != 0 && o.q_slab == 0;
+    h->pair_tables = o.no_pair_tables == 0;
     auto bail = [&](rsx_status s) {
         batch_release(h);
         return s;

@@ -163,6 +163,7 @@ struct rsx_debye {
     int q_slab = 32;
     int max_items = 16384;
     bool autotune = false, tuned = false;
+    bool pair_tables = true; // tabulated adjoint, gridded non-uniform forward
 
     // implicit water (caller order)
     float water_weight = 0.f;
@@ -464,8 +465,8 @@ rsx_status forward_device(rsx_debye *h)
     // non-uniform grids: the gridded pair-distance distribution
     const bool water = has_water(h);
     double nodes = 0.0, step = 0.0;
-    const bool gridded = !h->uniform && h->n_types <= 32 && pair_grid(h, &nodes, &step) &&
-                         nodes <= forward_grid_max_nodes(water);
+    const bool gridded = h->pair_tables && !h->uniform && h->n_types <= 32 &&
+                         pair_grid(h, &nodes, &step) && nodes <= forward_grid_max_nodes(water);
     if (gridded)
         RSX_TRY(ensure(&h->d_grid, h->grid_cap,
                        (size_t)nodes * forward_grid_hists(water) * 2 * h->n_types * h->n_types,
@@ -813,6 +814,7 @@ rsx_status rsx_debye_create(const float *q, int n_q, const float *t_factors, int
     h->autotune = o.autotune != 0 && o.q_slab == 0;
     h->max_items = o.max_items > 0 ? o.max_items : 16384;
     h->timing = o.timing != 0;
+    h->pair_tables = o.no_pair_tables == 0;
     h->rsasa.assign(n_bodies, 0.f);
     auto bail = [&](rsx_status s) {
         release(h);
@@ -1160,7 +1162,8 @@ static rsx_status backward_impl(rsx_debye *h, const float *dl_diq)
     a.grad = h->d_grad;
     int nodes = 0;
     float step = 0.f;
-    const bool tables = !has_water(h) && h->n_types <= 32 && adjoint_table_geometry(h, &nodes, &step);
+    const bool tables = h->pair_tables && !has_water(h) && h->n_types <= 32 &&
+                        adjoint_table_geometry(h, &nodes, &step);
     if (tables) {
         RSX_TRY(ensure(&h->d_adj_tab, h->adj_tab_cap, (size_t)nodes * h->n_types * h->n_types,
                        "adjoint tables"));

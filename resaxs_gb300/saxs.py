@@ -42,7 +42,7 @@ class Debye:
 
     def __init__(self, q, factors, n_bodies: int, *, device: int = -1, q_slab: int = 0,
                  max_items: int = 0, force_general_q: bool = False, timing: bool = False,
-                 autotune: bool = False):
+                 autotune: bool = False, pair_tables: bool = True):
         self.q = _f32(q)
         factors = _f32(factors)
         if factors.ndim != 2 or factors.shape[0] != len(self.q):
@@ -58,6 +58,7 @@ class Debye:
         opts.force_general_q = int(force_general_q)
         opts.timing = int(timing)
         opts.autotune = int(autotune)
+        opts.no_pair_tables = int(not pair_tables)
         h = ctypes.c_void_p()
         check(lib().rsx_debye_create(self.q, self.n_q, factors.reshape(-1), self.n_factors,
                                      self.n, ctypes.byref(opts), ctypes.byref(h)))

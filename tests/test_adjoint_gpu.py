@@ -21,12 +21,15 @@ def grad_err(g, ref):
     return np.linalg.norm(g - ref) / np.linalg.norm(ref), np.max(np.abs(g - ref)) / np.max(np.abs(ref))
 
 
+@pytest.mark.parametrize("tables", [True, False])
 @pytest.mark.parametrize("idx,n", [(1, 600), (3, 500), (4, 300)])
-def test_backward_vs_fp64_gradient(S, oracle_lib, idx, n):
+def test_backward_vs_fp64_gradient(S, oracle_lib, idx, n, tables):
+    """Both adjoints: the tabulated pair functions (default) and the
+    recurrence evaluated per pair*q (pair_tables=False)."""
     w = W.make_config(idx, seed=31, n_override=n)
     rng = np.random.default_rng(idx)
     lam = rng.normal(size=len(w.q)).astype(np.float32)
-    with S.Debye(w.q, w.ff, w.n) as d:
+    with S.Debye(w.q, w.ff, w.n, pair_tables=tables) as d:
         d.calc(w.bodies)
         g = d.backward(lam, f64=True)
     ref = oracle_lib.debye_grad_f64(w.q, lam.astype(np.float64), w.bodies, w.ff)
@@ -34,8 +37,9 @@ def test_backward_vs_fp64_gradient(S, oracle_lib, idx, n):
     assert e_norm < 2e-5 and e_max < 1e-4, (e_norm, e_max)
 
 
+@pytest.mark.parametrize("tables", [True, False])
 @pytest.mark.parametrize("diag", [150.0, 400.0, 700.0, 1500.0])
-def test_backward_on_every_small_theta_level(S, oracle_lib, diag):
+def test_backward_on_every_small_theta_level(S, oracle_lib, diag, tables):
     """dq = 0.6/255: the adjoint's reduction-free half-angle seeds hold up to
     a box diagonal of 595 A; beyond 668 A the far body's pairs have
     theta > pi/2 and take the rotation form.  One body of a compact structure
@@ -50,7 +54,7 @@ def test_backward_on_every_small_theta_level(S, oracle_lib, diag):
     b[0, 1:3] = lo[1:]
     rng = np.random.default_rng(int(diag))
     lam = rng.normal(size=len(w.q)).astype(np.float32)
-    with S.Debye(w.q, w.ff, w.n) as d:
+    with S.Debye(w.q, w.ff, w.n, pair_tables=tables) as d:
         d.calc(b)
         g = d.backward(lam, f64=True)
     ref = oracle_lib.debye_grad_f64(w.q, lam.astype(np.float64), b, w.ff)

@@ -87,7 +87,8 @@ def test_batch_matches_single_structure_handles(ensemble):
             assert rel(out[m], d.calc(members[m])) < 2e-6
 
 
-def test_batch_chi2_gradients(oracle_lib):
+@pytest.mark.parametrize("tables", [True, False])
+def test_batch_chi2_gradients(oracle_lib, tables):
     from resaxs_gb300.batch import DebyeBatch
     q, ff, members = W.batch_members(n_members=4, seed=8, n_lo=100, n_hi=400)
     rng = np.random.default_rng(2)
@@ -98,7 +99,7 @@ def test_batch_chi2_gradients(oracle_lib):
         it = oracle_lib.debye_f64(q, tb, ff).astype(np.float32)
         targets.append(it)
         sigmas.append((0.01 * it).astype(np.float32))
-    with DebyeBatch(q, ff, [len(m) for m in members]) as b:
+    with DebyeBatch(q, ff, [len(m) for m in members], pair_tables=tables) as b:
         b.set_targets(np.stack(targets), np.stack(sigmas))
         out, chi2, grad = b.forward_chi2_backward(members)
     off = 0

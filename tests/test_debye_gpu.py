@@ -167,8 +167,9 @@ def test_water_term_wide_slabs(saxs, oracle_lib, q_slab, n_q, ww):
     assert rel(out64, ref) < TOL
 
 
+@pytest.mark.parametrize("tables", [True, False])
 @pytest.mark.parametrize("ww,n", [(0.0, 1500), (0.7, 1500), (-1.5, 900), (3.0, 600)])
-def test_nonuniform_grid_gridded_forward(saxs, oracle_lib, ww, n):
+def test_nonuniform_grid_gridded_forward(saxs, oracle_lib, ww, n, tables):
     """Non-uniform q grids run through the gridded pair-distance
     distribution (Hermite deposits on an r grid with q_max h <= 0.05, the
     sums over q evaluated on the nodes), with and without water; FP64 oracle
@@ -179,7 +180,7 @@ def test_nonuniform_grid_gridded_forward(saxs, oracle_lib, ww, n):
     q[0] = 0.0
     ff = W.exp_form_factors(q, W.Z5, rng.uniform(0.5, 2.0, 5))
     rs = rng.uniform(0, 1, w.n).astype(np.float32)
-    with saxs.Debye(q, ff, w.n) as d:
+    with saxs.Debye(q, ff, w.n, pair_tables=tables) as d:
         if ww != 0.0:
             d.set_water(ww, 4, rs)
         d.calc(w.bodies)
