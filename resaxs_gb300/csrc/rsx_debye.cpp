@@ -157,6 +157,7 @@ struct rsx_debye {
     bool timing = false;
     int n = 0, n_q = 0, n_types = 0;
     std::vector<float> q, ff;
+    bool ff_on_device = false; // d_ff holds ff
     bool uniform = false;
     float dq = 0.f;
     float lo[3] = {0.f, 0.f, 0.f}, hi[3] = {0.f, 0.f, 0.f}; // extent of the device bodies
@@ -286,13 +287,10 @@ int forward_slab(const rsx_debye *h)
 }
 
 // Re-derives the device layout when the body types changed.
-rsx_status update_layout(rsx_debye *h, const rsx_body *bodies)
+// `same`: the bodies' types match the current layout (scan_bodies).
+rsx_status update_layout(rsx_debye *h, const rsx_body *bodies, bool same)
 {
-    bool same = h->have_layout;
-    if (same)
-        for (int i = 0; i < h->n && same; ++i)
-            same = type_of(bodies[i]) == h->L.types[i];
-    if (same)
+    if (same && h->have_layout)
         return RSX_OK;
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
@@ -341,21 +339,35 @@ rsx_status upload_water(rsx_debye *h)
     return RSX_OK;
 }
 
-// Bounding box of the bodies on the device: reset by a full upload, grown by
-// moves (never shrunk until the next full upload, so it stays an upper bound).
-void reset_extent(rsx_debye *h, const rsx_body *b, int n)
+// One pass over a full set of caller bodies: factor indices (an error names
+// the first bad one), whether the types match the device layout, and the
+// bounding box.  The box is the extent of the device bodies: reset by a full
+// upload, grown by moves (never shrunk until the next full upload, so it stays
+// an upper bound).
+rsx_status scan_bodies(rsx_debye *h, const rsx_body *b, bool *same_types)
 {
+    bool same = h->have_layout && (int)h->L.types.size() == h->n;
+    float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+    for (int i = 0; i < h->n; ++i) {
+        const unsigned t = type_of(b[i]);
+        if (t >= (unsigned)h->n_types)
+            return fail(RSX_INVALID_ARG, "body " + std::to_string(i) + " has factor index " +
+                                             std::to_string(t) + " >= n_factors " +
+                                             std::to_string(h->n_types));
+        same = same && t == h->L.types[i];
+        lo[0] = std::min(lo[0], b[i].x);
+        hi[0] = std::max(hi[0], b[i].x);
+        lo[1] = std::min(lo[1], b[i].y);
+        hi[1] = std::max(hi[1], b[i].y);
+        lo[2] = std::min(lo[2], b[i].z);
+        hi[2] = std::max(hi[2], b[i].z);
+    }
     for (int d = 0; d < 3; ++d) {
-        h->lo[d] = 3.4e38f;
-        h->hi[d] = -3.4e38f;
+        h->lo[d] = lo[d];
+        h->hi[d] = hi[d];
     }
-    for (int i = 0; i < n; ++i) {
-        const float x[3] = {b[i].x, b[i].y, b[i].z};
-        for (int d = 0; d < 3; ++d) {
-            h->lo[d] = std::min(h->lo[d], x[d]);
-            h->hi[d] = std::max(h->hi[d], x[d]);
-        }
-    }
+    *same_types = same;
+    return RSX_OK;
 }
 
 void grow_extent(rsx_debye *h, const rsx_body *b, unsigned n)
@@ -572,8 +584,9 @@ rsx_status tune_slab(rsx_debye *h)
 // Full calculation from caller-order bodies.
 rsx_status upload_all(rsx_debye *h, const rsx_body *bodies)
 {
-    RSX_TRY(update_layout(h, bodies));
-    reset_extent(h, bodies, h->n);
+    bool same = false;
+    RSX_TRY(scan_bodies(h, bodies, &same));
+    RSX_TRY(update_layout(h, bodies, same));
     for (int s = 0; s < h->n; ++s) {
         const rsx_body &b = bodies[h->L.perm[s]];
         h->h_pos[s] = make_float4(b.x, b.y, b.z, b.w);
@@ -581,9 +594,12 @@ rsx_status upload_all(rsx_debye *h, const rsx_body *bodies)
     RSX_TRY_CUDA(cudaMemcpyAsync(h->d_pos, h->h_pos, sizeof(float4) * h->n,
                                  cudaMemcpyHostToDevice, h->st),
                  "upload bodies");
-    RSX_TRY_CUDA(cudaMemcpyAsync(h->d_ff, h->ff.data(), sizeof(float) * h->ff.size(),
-                                 cudaMemcpyHostToDevice, h->st),
-                 "upload factors");
+    if (!h->ff_on_device) {
+        RSX_TRY_CUDA(cudaMemcpyAsync(h->d_ff, h->ff.data(), sizeof(float) * h->ff.size(),
+                                     cudaMemcpyHostToDevice, h->st),
+                     "upload factors");
+        h->ff_on_device = true;
+    }
     RSX_TRY(upload_water(h));
     return RSX_OK;
 }
@@ -887,6 +903,7 @@ rsx_status rsx_debye_set_factors(rsx_debye *h, const float *t_factors, int n_fac
     if (!t_factors || n_factors != h->n_types)
         return fail(RSX_INVALID_ARG, "factor table must have the handle's n_factors columns");
     h->ff.assign(t_factors, t_factors + (size_t)h->n_q * n_factors);
+    h->ff_on_device = false;
     h->params_dirty = true;
     return ok();
 }
@@ -912,8 +929,7 @@ rsx_status rsx_debye_calc(rsx_debye *h, const rsx_body *bodies, float *out_iq)
     RSX_TRY(begin_call(h));
     if (!bodies && h->n > 0)
         return fail(RSX_INVALID_ARG, "bodies is null");
-    RSX_TRY(check_bodies(h, bodies, h->n));
-    RSX_TRY(full_calc(h, bodies));
+    RSX_TRY(full_calc(h, bodies)); // validates the bodies before any device work
     RSX_TRY(read_curve(h, out_iq));
     return ok();
 }
@@ -926,8 +942,7 @@ rsx_status rsx_debye_calc_shard(rsx_debye *h, const rsx_body *bodies, int shard,
         return fail(RSX_INVALID_ARG, "bodies is null");
     if (!out_iq || n_shards < 1 || shard < 0 || shard >= n_shards)
         return fail(RSX_INVALID_ARG, "need out_iq and 0 <= shard < n_shards");
-    RSX_TRY(check_bodies(h, bodies, h->n));
-    RSX_TRY(upload_all(h, bodies));
+    RSX_TRY(upload_all(h, bodies)); // validates the bodies before any device work
     // the device positions no longer hold a computed state: an incremental
     // call needs a full calc first
     h->computing = false;
@@ -1056,6 +1071,7 @@ rsx_status rsx_debye_revert(rsx_debye *h)
     if (!h->have_saved)
         return ok(); // saxs_alg_cl_gpu_pt_wf.cpp:607-608
     h->ff = h->saved_ff;
+    h->ff_on_device = false;
     h->rsasa = h->saved_rsasa;
     h->water_weight = h->saved_ww;
     h->water_index = h->saved_wi;
@@ -1073,6 +1089,7 @@ rsx_status rsx_debye_revert(rsx_debye *h)
         RSX_TRY_CUDA(cudaMemcpyAsync(h->d_ff, h->ff.data(), sizeof(float) * h->ff.size(),
                                      cudaMemcpyHostToDevice, h->st),
                      "restore factors");
+        h->ff_on_device = true;
         h->cur = h->saved_bodies;
         grow_extent(h, h->cur.data(), (unsigned)h->cur.size());
         RSX_TRY(upload_water(h));
