@@ -27,6 +27,8 @@
 // rsasa_j and rsasa_i rsasa_j, and the per-q factors apply at evaluation.
 #include "debye_device.cuh"
 
+#include <algorithm>
+
 namespace rsx {
 
 constexpr double kGridUnit = 4294967296.0; // 2^32
@@ -114,77 +116,103 @@ __global__ void __launch_bounds__(kBlockAtoms)
     }
 }
 
-// One CTA per q: partial[k][0] = sum over the present type pairs of
-// sum_c F_c(q) sum_b (W_cb g(r_b) + D_cb h g'(r_b)), in FP64, with F_0 =
-// f_ti f_tj (and with water F_1 = w f_w f_tj, F_2 = w f_w f_ti, F_3 = (w f_w)^2),
-// g(r) = sin(q r)/r, g'(r) = (q r cos(q r) - sin(q r)) / r^2 and, at r = 0,
-// g = q, g' = 0.  sin/cos(q r_b) in FP32 with the rounding of q r_b folded in
-// (r_b = b h is exact in double and carried as hi + lo).
-template <bool WATER>
+// g(q_k, r_b) = sin(q r_b)/r_b and h g'(q_k, r_b) = h (q r cos(q r) - sin(q r))
+// / r^2 for every q and node, in FP64 ([2][n_q][nodes]); at r = 0, g = q and
+// g' = 0.  sin/cos(q r_b) in FP32 with the rounding of q r_b folded in (r_b =
+// b h is exact in double and carried as hi + lo); 1/r_b from the FP32
+// reciprocal with one Newton step in FP64.
 __global__ void __launch_bounds__(256)
-    forward_grid_eval_kernel(const DebyeArgs a, const double *hist, int nodes, float h,
-                             unsigned type_mask)
+    forward_grid_gtab_kernel(const DebyeArgs a, double *gtab, int nodes, float h)
 {
-    constexpr int NH = kGridHists<WATER>;
-    __shared__ double s_w[8];
-    const int k = blockIdx.x;
-    const float qk = a.q[k];
-    const int T = a.n_types;
-    double acc = 0.0;
-    for (int idx = threadIdx.x; idx < T * T * nodes; idx += blockDim.x) {
-        const int tp = idx / nodes, b = idx - tp * nodes;
-        const int ti = tp / T, tj = tp - ti * T;
-        if (tj < ti || !((type_mask >> ti) & 1u) || !((type_mask >> tj) & 1u))
-            continue;
-        const double *row = hist + (size_t)tp * NH * 2 * nodes;
-        bool any = false;
-#pragma unroll
-        for (int c = 0; c < NH; ++c)
-            any = any || row[c * 2 * nodes + b] != 0.0 || row[c * 2 * nodes + nodes + b] != 0.0;
-        if (!any)
-            continue;
-        double g, dg;
-        if (b == 0) {
-            g = qk;
-            dg = 0.0;
-        } else {
+    const size_t n = (size_t)a.n_q * nodes;
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const int k = (int)(idx / nodes), b = (int)(idx - (size_t)k * nodes);
+        const float qk = a.q[k];
+        double g = qk, dg = 0.0;
+        if (b > 0) {
             const double rb = (double)b * (double)h;
             const float r_hi = (float)rb, r_lo = (float)(rb - (double)r_hi);
             const float x = qk * r_hi;
             const float x_lo = fmaf(qk, r_hi, -x) + qk * r_lo;
             float s, c;
             sincos_rr2(x, x_lo, s, c);
-            // 1/r_b from the FP32 reciprocal with one Newton step in FP64
             const double y0 = (double)__frcp_rn(r_hi);
             const double rinv = y0 * (2.0 - rb * y0);
             g = (double)s * rinv;
             dg = ((double)qk * (double)c - g) * rinv;
         }
-        const double fi = a.ff[(size_t)k * T + ti], fj = a.ff[(size_t)k * T + tj];
-        double F[NH];
-        F[0] = fi * fj;
-        if (WATER) {
-            const double fw = (double)a.water_weight * (double)a.ff[(size_t)k * T + a.water_index];
-            F[1] = fw * fj;
-            F[2] = fw * fi;
-            F[3] = fw * fw;
+        gtab[idx] = g;
+        gtab[n + idx] = (double)h * dg;
+    }
+}
+
+// One CTA per q: partial[k][0] = sum over the present type pairs (t_i <= t_j)
+// of sum_c F_c(q) sum_b (W_cb g(q, r_b) + D_cb h g'(q, r_b)), in FP64, with
+// F_0 = f_ti f_tj and, with water, F_1 = w f_w f_tj, F_2 = w f_w f_ti,
+// F_3 = (w f_w)^2.  The node sums of a type pair are reduced over the CTA
+// before its factors apply.
+template <bool WATER>
+__global__ void __launch_bounds__(256)
+    forward_grid_eval_kernel(const DebyeArgs a, const double *hist, const double *gtab, int nodes,
+                             unsigned type_mask)
+{
+    constexpr int NH = kGridHists<WATER>;
+    __shared__ double s_w[8][NH];
+    const int k = blockIdx.x;
+    const int T = a.n_types;
+    const size_t n = (size_t)a.n_q * nodes;
+    const double *g = gtab + (size_t)k * nodes, *dg = gtab + n + (size_t)k * nodes;
+    double acc = 0.0;
+    for (int tp = 0; tp < T * T; ++tp) { // uniform over the CTA
+        const int ti = tp / T, tj = tp - ti * T;
+        if (tj < ti || !((type_mask >> ti) & 1u) || !((type_mask >> tj) & 1u))
+            continue;
+        const double *row = hist + (size_t)tp * NH * 2 * nodes;
+        double part[NH];
+#pragma unroll
+        for (int c = 0; c < NH; ++c)
+            part[c] = 0.0;
+        for (int b = threadIdx.x; b < nodes; b += blockDim.x) {
+            const double gb = g[b], dgb = dg[b];
+#pragma unroll
+            for (int c = 0; c < NH; ++c)
+                part[c] = fma(row[c * 2 * nodes + b], gb, fma(row[c * 2 * nodes + nodes + b], dgb,
+                                                            part[c]));
         }
 #pragma unroll
         for (int c = 0; c < NH; ++c)
-            acc += F[c] * (row[c * 2 * nodes + b] * g + row[c * 2 * nodes + nodes + b] * (double)h * dg);
-    }
 #pragma unroll
-    for (int m = 16; m >= 1; m >>= 1)
-        acc += __shfl_xor_sync(0xffffffffu, acc, m);
-    if ((threadIdx.x & 31) == 0)
-        s_w[threadIdx.x >> 5] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
-            s += s_w[w];
-        a.partial[k] = s; // partial[k][0]: one part per q
+            for (int m = 16; m >= 1; m >>= 1)
+                part[c] += __shfl_xor_sync(0xffffffffu, part[c], m);
+        __syncthreads(); // the previous type pair's s_w is read
+        if ((threadIdx.x & 31) == 0)
+#pragma unroll
+            for (int c = 0; c < NH; ++c)
+                s_w[threadIdx.x >> 5][c] = part[c];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const double fi = a.ff[(size_t)k * T + ti], fj = a.ff[(size_t)k * T + tj];
+            double F[NH];
+            F[0] = fi * fj;
+            if (WATER) {
+                const double fw =
+                    (double)a.water_weight * (double)a.ff[(size_t)k * T + a.water_index];
+                F[1] = fw * fj;
+                F[2] = fw * fi;
+                F[3] = fw * fw;
+            }
+#pragma unroll
+            for (int c = 0; c < NH; ++c) {
+                double s = 0.0;
+                for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+                    s += s_w[w][c];
+                acc += F[c] * s;
+            }
+        }
     }
+    if (threadIdx.x == 0)
+        a.partial[k] = acc; // partial[k][0]: one part per q
 }
 
 int forward_grid_hists(bool water) { return water ? kGridHists<true> : kGridHists<false>; }
@@ -197,7 +225,7 @@ int forward_grid_max_nodes(bool water)
 }
 
 template <bool WATER>
-static cudaError_t grid_launch(const DebyeArgs &a, double *hist, int nodes, float h,
+static cudaError_t grid_launch(const DebyeArgs &a, double *hist, double *gtab, int nodes, float h,
                                unsigned type_mask, cudaStream_t st)
 {
     cudaError_t e = cudaSuccess;
@@ -216,9 +244,22 @@ static cudaError_t grid_launch(const DebyeArgs &a, double *hist, int nodes, floa
         if (e != cudaSuccess)
             return e;
     }
-    forward_grid_eval_kernel<WATER><<<a.n_q, 256, 0, st>>>(a, hist, nodes, h, type_mask);
+    const size_t n = (size_t)a.n_q * nodes;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, 4096);
+    forward_grid_gtab_kernel<<<blocks, 256, 0, st>>>(a, gtab, nodes, h);
+    count_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return e;
+    forward_grid_eval_kernel<WATER><<<a.n_q, 256, 0, st>>>(a, hist, gtab, nodes, type_mask);
     count_launch();
     return cudaGetLastError();
+}
+
+size_t forward_grid_doubles(int n_types, int n_q, int nodes, bool water)
+{
+    return (size_t)forward_grid_hists(water) * 2 * nodes * n_types * n_types +
+           2 * (size_t)n_q * nodes;
 }
 
 cudaError_t launch_forward_grid(const DebyeArgs &a, double *hist, int nodes, float h,
@@ -234,8 +275,10 @@ cudaError_t launch_forward_grid(const DebyeArgs &a, double *hist, int nodes, flo
                         st);
     if (e != cudaSuccess)
         return e;
-    return water ? grid_launch<true>(a, hist, nodes, h, type_mask, st)
-                 : grid_launch<false>(a, hist, nodes, h, type_mask, st);
+    // the g tables follow the histograms in the same buffer
+    double *gtab = hist + (size_t)forward_grid_hists(water) * 2 * nodes * a.n_types * a.n_types;
+    return water ? grid_launch<true>(a, hist, gtab, nodes, h, type_mask, st)
+                 : grid_launch<false>(a, hist, gtab, nodes, h, type_mask, st);
 }
 
 } // namespace rsx

@@ -481,7 +481,7 @@ rsx_status forward_device(rsx_debye *h)
                          pair_grid(h, &nodes, &step) && nodes <= forward_grid_max_nodes(water);
     if (gridded)
         RSX_TRY(ensure(&h->d_grid, h->grid_cap,
-                       (size_t)nodes * forward_grid_hists(water) * 2 * h->n_types * h->n_types,
+                       forward_grid_doubles(h->n_types, h->n_q, (int)nodes, water),
                        "forward histograms"));
     if (h->timing)
         RSX_TRY_CUDA(cudaEventRecord(h->ev_k0, h->st), "event");

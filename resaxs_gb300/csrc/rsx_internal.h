@@ -124,9 +124,13 @@ cudaError_t launch_adjoint_table(const DebyeArgs &a, float4 *tab, unsigned type_
                                  cudaStream_t st);
 // forward through the gridded pair-distance distribution (grid_kernels.cu):
 // non-uniform q grids; writes partial[k][0] (one part per q) from FP64
-// histograms `hist` ([n_types^2][hists][2][nodes]) on nodes r = b h
+// histograms ([n_types^2][hists][2][nodes] at the start of `hist`, followed
+// by the g tables) on nodes r = b h
 int forward_grid_hists(bool water);
 int forward_grid_max_nodes(bool water);
+// doubles the buffer of launch_forward_grid holds (histograms, then the
+// [2][n_q][nodes] tables of g and h g')
+size_t forward_grid_doubles(int n_types, int n_q, int nodes, bool water);
 cudaError_t launch_forward_grid(const DebyeArgs &a, double *hist, int nodes, float h,
                                 unsigned type_mask, bool water, cudaStream_t st);
 // the tables alone, for `n_members` members (batched passes)
