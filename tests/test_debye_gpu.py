@@ -221,6 +221,31 @@ def test_coincident_bodies_give_sinc_one(saxs):
     assert rel(out64, expect) < 1e-6
 
 
+def test_nonuniform_grid_edge_cases(saxs, oracle_lib):
+    """The gridded forward of non-uniform grids at its edges: no body, one
+    body, two coincident bodies (sinc(0) = 1, node 0), two bodies, and a
+    structure wide enough that its node count is past the shared-memory cap
+    (the direct-sine kernel then runs)."""
+    rng = np.random.default_rng(4)
+    q = np.sort(rng.uniform(0, 0.5, 29)).astype(np.float32)
+    q[0] = 0.0
+    ff = W.exp_form_factors(q, (6, 8), (1.0, 0.5))
+    out, _, cfg = gpu_curve(saxs, q, ff, np.zeros((0, 4), np.float32))
+    assert not cfg["uniform_q"] and np.all(out == 0)
+    one = W.pack_bodies(np.array([[1.0, 2.0, 3.0]]), np.array([1]))
+    _, out64, _ = gpu_curve(saxs, q, ff, one)
+    assert np.allclose(out64, ff[:, 1].astype(np.float64) ** 2, rtol=1e-12)
+    same = W.pack_bodies(np.array([[1.0, 2.0, 3.0], [1.0, 2.0, 3.0]]), np.array([0, 1]))
+    _, out64, _ = gpu_curve(saxs, q, ff, same)
+    assert rel(out64, (ff[:, 0].astype(np.float64) + ff[:, 1]) ** 2) < 1e-6
+    two = W.pack_bodies(np.array([[1.0, 2.0, 3.0], [4.5, -2.0, 7.25]]), np.array([0, 1]))
+    _, out64, _ = gpu_curve(saxs, q, ff, two)
+    assert rel(out64, oracle_lib.debye_f64(q, two, ff)) < TOL
+    wide = W.pack_bodies(rng.uniform(-2500, 2500, (300, 3)), rng.integers(0, 2, 300))
+    _, out64, _ = gpu_curve(saxs, q, ff, wide)
+    assert rel(out64, oracle_lib.debye_f64(q, wide, ff)) < TOL
+
+
 def test_q_zero_is_sum_squared(saxs):
     w = W.make_config(1, seed=16, n_override=500)
     _, out64, _ = gpu_curve(saxs, w.q, w.ff, w.bodies)
