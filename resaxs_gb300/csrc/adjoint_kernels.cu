@@ -91,9 +91,11 @@ cudaError_t launch_adjoint(const DebyeArgs &a, int q_slab, bool uniform, bool wa
 // One warp per node; grid (nodes / 4, n_types * n_types, members): member
 // m's tables from its dL/dI row lambda + m * n_q.  Whole warps return
 // together (the node sum shuffles over the warp).
+template <bool WATER>
 __global__ void __launch_bounds__(128)
     adjoint_table_kernel(const DebyeArgs a, float4 *tab, unsigned type_mask)
 {
+    constexpr int NT = kTableEntries<WATER>;
     const int lane = threadIdx.x & 31;
     const int b = blockIdx.x * 4 + (threadIdx.x >> 5);
     const int ti = blockIdx.y / a.n_types, tj = blockIdx.y % a.n_types, m = blockIdx.z;
@@ -101,15 +103,18 @@ __global__ void __launch_bounds__(128)
         return;
     const float h = a.adj_geom ? a.adj_geom[0] : a.adj_h;
     const size_t tp = (size_t)m * a.n_types * a.n_types + (size_t)(ti * a.n_types + tj);
-    const float4 v = adjoint_table_node(a, a.lambda + (size_t)m * a.n_q, ti, tj, b, h, lane);
-    if (lane == 0)
-        tab[tp * a.adj_nodes + b] = v;
+#pragma unroll
+    for (int c = 0; c < NT; ++c) {
+        const float4 v = adjoint_table_node(a, a.lambda + (size_t)m * a.n_q, ti, tj, b, h, lane, c);
+        if (lane == 0)
+            tab[(tp * a.adj_nodes + b) * NT + c] = v;
+    }
 }
 
-template <int IL>
+template <int IL, bool WATER>
 __global__ void __launch_bounds__(kBlockAtoms) adjoint_pairs_table_kernel(const DebyeArgs a)
 {
-    adjoint_table_item<IL>(a, blockIdx.x);
+    adjoint_table_item<IL, WATER>(a, blockIdx.x);
 }
 
 cudaError_t launch_adjoint_tables(const DebyeArgs &a, float4 *tab, unsigned type_mask,
@@ -118,25 +123,31 @@ cudaError_t launch_adjoint_tables(const DebyeArgs &a, float4 *tab, unsigned type
     if (a.n_types > 32 || a.adj_nodes < 2 || n_members < 1 || n_members > 65535)
         return cudaErrorInvalidValue;
     const dim3 g((a.adj_nodes + 3) / 4, a.n_types * a.n_types, n_members);
-    adjoint_table_kernel<<<g, 128, 0, st>>>(a, tab, type_mask);
+    adjoint_table_kernel<false><<<g, 128, 0, st>>>(a, tab, type_mask);
     count_launch();
     return cudaGetLastError();
 }
 
-cudaError_t launch_adjoint_table(const DebyeArgs &a, float4 *tab, unsigned type_mask,
+cudaError_t launch_adjoint_table(const DebyeArgs &a, float4 *tab, unsigned type_mask, bool water,
                                  cudaStream_t st)
 {
     if (a.n_items == 0)
         return cudaSuccess;
-    if (a.n_types > 32 || a.adj_nodes < 2)
+    if (a.n_types > 32 || a.adj_nodes < 2 || (water && !a.rsasa))
         return cudaErrorInvalidValue;
     const dim3 g((a.adj_nodes + 3) / 4, a.n_types * a.n_types, 1);
-    adjoint_table_kernel<<<g, 128, 0, st>>>(a, tab, type_mask);
+    if (water)
+        adjoint_table_kernel<true><<<g, 128, 0, st>>>(a, tab, type_mask);
+    else
+        adjoint_table_kernel<false><<<g, 128, 0, st>>>(a, tab, type_mask);
     count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;
-    adjoint_pairs_table_kernel<4><<<a.n_items, kBlockAtoms, 0, st>>>(a);
+    if (water)
+        adjoint_pairs_table_kernel<4, true><<<a.n_items, kBlockAtoms, 0, st>>>(a);
+    else
+        adjoint_pairs_table_kernel<4, false><<<a.n_items, kBlockAtoms, 0, st>>>(a);
     count_launch();
     return cudaGetLastError();
 }

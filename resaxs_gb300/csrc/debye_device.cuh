@@ -1041,7 +1041,7 @@ __device__ __forceinline__ void adj_scatter(const AdjPair &p, float A, float B, 
 }
 
 // ----------------------------------------------------------------------------
-// adjoint through tabulated pair functions (any q grid, no water)
+// adjoint through tabulated pair functions (any q grid)
 // ----------------------------------------------------------------------------
 //
 // For one item's type pair (t_i, t_j) the gradient of a pair needs only
@@ -1056,13 +1056,23 @@ __device__ __forceinline__ void adj_scatter(const AdjPair &p, float A, float B, 
 // (q_max h)^4 / 384 of sum|alpha| (1.6e-8 at q_max h = 0.05, the step the host
 // picks) -- smaller than the FP32 recurrence's.  A pair then costs two table
 // loads and ~25 FP32 operations instead of 4 per q.
+//
+// With the implicit water term alpha_k = lambda_k f~_i f~_j is linear in the
+// combinations 1, rsasa_i, rsasa_j and rsasa_i rsasa_j, with the factors
+// f_ti f_tj, w f_w f_tj, w f_w f_ti and (w f_w)^2: every node then holds four
+// entries, one per combination, and a pair weights them with its rsasa.
+template <bool WATER>
+constexpr int kTableEntries = WATER ? 4 : 1;
 
-// Node b of the table at r_b = b h (exact in double): A, h dA/dr, B, h dB/dr,
-// by one warp (lane l sums q l, l + 32, ...; FP64 partials combined by
-// shuffles; the result is valid in every lane).  sin/cos(q r_b) in FP32 with
-// the rounding of q r_b folded in as the low part (r_b is carried as hi + lo).
+// Entry c of node b of the table at r_b = b h (exact in double): A, h dA/dr,
+// B, h dB/dr with alpha_k = lambda_k x factor c (c = 0: f_ti f_tj; with water
+// 1: w f_w f_tj, 2: w f_w f_ti, 3: (w f_w)^2), by one warp (lane l sums q l,
+// l + 32, ...; FP64 partials combined by shuffles; the result is valid in
+// every lane).  sin/cos(q r_b) in FP32 with the rounding of q r_b folded in as
+// the low part (r_b is carried as hi + lo).
 __device__ __forceinline__ float4 adjoint_table_node(const DebyeArgs &a, const float *lambda,
-                                                     int ti, int tj, int b, float h, int lane)
+                                                     int ti, int tj, int b, float h, int lane,
+                                                     int c = 0)
 {
     const double rb = (double)b * (double)h;
     const float r_hi = (float)rb, r_lo = (float)(rb - (double)r_hi);
@@ -1071,8 +1081,13 @@ __device__ __forceinline__ float4 adjoint_table_node(const DebyeArgs &a, const f
         const float qk = a.q[k];
         if (qk == 0.f)
             continue; // d sinc(q r) / dr = 0 at q = 0: no term on either side
-        const float al = lambda[k] * a.ff[(size_t)k * a.n_types + ti] *
-                         a.ff[(size_t)k * a.n_types + tj];
+        const float *row = a.ff + (size_t)k * a.n_types;
+        const float fw = c > 0 ? a.water_weight * row[a.water_index] : 0.f;
+        const float factor = c == 0   ? row[ti] * row[tj]
+                             : c == 1 ? fw * row[tj]
+                             : c == 2 ? fw * row[ti]
+                                      : fw * fw;
+        const float al = lambda[k] * factor;
         const float x = qk * r_hi;
         const float x_lo = fmaf(qk, r_hi, -x) + qk * r_lo;
         float s, c;
@@ -1093,32 +1108,50 @@ __device__ __forceinline__ float4 adjoint_table_node(const DebyeArgs &a, const f
     return make_float4((float)A, (float)(h * dA), (float)B, (float)(h * dB));
 }
 
-// A(r) and B(r) of one pair from the table of its item's type pair.
+// A(r) and B(r) of one pair from the table of its item's type pair (nodes of
+// kTableEntries<WATER> entries; with water weighted by 1, rs_i, rs_j, rs_i rs_j).
+template <bool WATER>
 __device__ __forceinline__ void adjoint_table_eval(const float4 *tab, int n_nodes, float h,
-                                                   float inv_h, float r, float &A, float &B)
+                                                   float inv_h, float r, float rs_i, float rs_j,
+                                                   float &A, float &B)
 {
+    constexpr int NT = kTableEntries<WATER>;
     // node index: clamped into the table (a NaN distance reads node 0)
     const float u = fminf(fmaxf(r * inv_h, 0.f), (float)(n_nodes - 2));
     const int b = (int)u;
     const float t = fmaf(-(float)b, h, r) * inv_h; // (r - b h) / h with r - b h rounded once
-    const float4 p0 = __ldg(tab + b), p1 = __ldg(tab + b + 1);
     const float t2 = t * t, t3 = t2 * t;
     const float h01 = fmaf(-2.0f, t3, 3.0f * t2); // Hermite basis
     const float h00 = 1.0f - h01;
     const float h10 = t3 - 2.0f * t2 + t;
     const float h11 = t3 - t2;
-    A = fmaf(h00, p0.x, fmaf(h10, p0.y, fmaf(h01, p1.x, h11 * p1.y)));
-    B = fmaf(h00, p0.z, fmaf(h10, p0.w, fmaf(h01, p1.z, h11 * p1.w)));
+    float m[NT];
+    m[0] = 1.0f;
+    if (WATER) {
+        m[1] = rs_i;
+        m[2] = rs_j;
+        m[3] = rs_i * rs_j;
+    }
+    A = 0.f;
+    B = 0.f;
+#pragma unroll
+    for (int c = 0; c < NT; ++c) {
+        const float4 p0 = __ldg(tab + (size_t)b * NT + c), p1 = __ldg(tab + (size_t)(b + 1) * NT + c);
+        A = fmaf(m[c], fmaf(h00, p0.x, fmaf(h10, p0.y, fmaf(h01, p1.x, h11 * p1.y))), A);
+        B = fmaf(m[c], fmaf(h00, p0.z, fmaf(h10, p0.w, fmaf(h01, p1.z, h11 * p1.w))), B);
+    }
 }
 
 // Adjoint of one work item through the tables: every pair of the item reads
 // A and B of its type pair's table, then scatters as the other forms do.  IL
 // pairs per step keep IL table loads in flight.
-template <int IL>
+template <int IL, bool WATER = false>
 __device__ __forceinline__ void adjoint_table_item(const DebyeArgs &a, int item_idx)
 {
     static_assert(3 * IL <= 16, "the J side of a step is reduce-scattered as 16 values");
+    constexpr int NT = kTableEntries<WATER>;
     __shared__ float4 s_pos[kBlockAtoms];
+    __shared__ float s_rs[WATER ? kBlockAtoms : 1];
     __shared__ float s_gj[kBlockAtoms][3];
 
     const int tid = threadIdx.x;
@@ -1131,20 +1164,25 @@ __device__ __forceinline__ void adjoint_table_item(const DebyeArgs &a, int item_
     // the item's member (PairItem::pad; 0 for a single structure) owns its tables
     const float4 *tab =
         a.adj_tab +
-        ((size_t)it.pad * a.n_types * a.n_types + (size_t)(bi.type * a.n_types + tj)) * n_nodes;
+        ((size_t)it.pad * a.n_types * a.n_types + (size_t)(bi.type * a.n_types + tj)) * n_nodes *
+            NT;
     const float h = a.adj_geom ? a.adj_geom[0] : a.adj_h;
     const float inv_h = a.adj_geom ? a.adj_geom[1] : a.adj_inv_h;
 
     const int i = bi.start + tid;
     const bool valid_i = tid < bi.len;
     const float4 pi = valid_i ? a.pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float rs_i = (WATER && valid_i) ? a.rsasa[i] : 0.f;
     float gi0 = 0.f, gi1 = 0.f, gi2 = 0.f;
 
     for (int b = it.bj_begin; b < it.bj_end; ++b) {
         const BlockDesc bj = a.blocks[b];
         __syncthreads();
-        if (tid < bj.len)
+        if (tid < bj.len) {
             s_pos[tid] = a.pos[bj.start + tid];
+            if (WATER)
+                s_rs[tid] = a.rsasa[bj.start + tid];
+        }
         s_gj[tid][0] = 0.f;
         s_gj[tid][1] = 0.f;
         s_gj[tid][2] = 0.f;
@@ -1158,7 +1196,8 @@ __device__ __forceinline__ void adjoint_table_item(const DebyeArgs &a, int item_
                 // past the block's end: a repeated body, masked out below
                 const int j = min(jj + v, bj.len - 1);
                 pair_r(pi, s_pos[j], p[v].r, p[v].rinv, p[v].dx, p[v].dy, p[v].dz);
-                adjoint_table_eval(tab, n_nodes, h, inv_h, p[v].r, A[v], B[v]);
+                adjoint_table_eval<WATER>(tab, n_nodes, h, inv_h, p[v].r, rs_i,
+                                          WATER ? s_rs[j] : 0.f, A[v], B[v]);
             }
             // G d of the step's pairs (zero past the block's end); the I side
             // stays in registers, the J side (IL x 3 values) is reduce-scattered

@@ -1154,7 +1154,7 @@ static bool adjoint_table_geometry(const rsx_debye *h, int *nodes, float *step)
     double n = 0.0, st = 0.0;
     if (!pair_grid(h, &n, &st))
         return false;
-    const double bytes = n * h->n_types * h->n_types * sizeof(float4);
+    const double bytes = n * h->n_types * h->n_types * sizeof(float4) * (has_water(h) ? 4 : 1);
     if (!(n < 1e7) || bytes > 512.0 * 1024 * 1024)
         return false;
     *nodes = (int)n;
@@ -1179,10 +1179,11 @@ static rsx_status backward_impl(rsx_debye *h, const float *dl_diq)
     a.grad = h->d_grad;
     int nodes = 0;
     float step = 0.f;
-    const bool tables = h->pair_tables && !has_water(h) && h->n_types <= 32 &&
-                        adjoint_table_geometry(h, &nodes, &step);
+    const bool tables =
+        h->pair_tables && h->n_types <= 32 && adjoint_table_geometry(h, &nodes, &step);
     if (tables) {
-        RSX_TRY(ensure(&h->d_adj_tab, h->adj_tab_cap, (size_t)nodes * h->n_types * h->n_types,
+        RSX_TRY(ensure(&h->d_adj_tab, h->adj_tab_cap,
+                       (size_t)nodes * h->n_types * h->n_types * (has_water(h) ? 4 : 1),
                        "adjoint tables"));
         a.adj_tab = h->d_adj_tab;
         a.adj_nodes = nodes;
@@ -1193,7 +1194,8 @@ static rsx_status backward_impl(rsx_debye *h, const float *dl_diq)
     if (h->timing)
         RSX_TRY_CUDA(cudaEventRecord(h->ev_k0, h->st), "event");
     if (tables)
-        RSX_LAUNCH(launch_adjoint_table(a, h->d_adj_tab, type_mask, h->st), "adjoint kernels");
+        RSX_LAUNCH(launch_adjoint_table(a, h->d_adj_tab, type_mask, has_water(h), h->st),
+                   "adjoint kernels");
     else
         RSX_LAUNCH(launch_adjoint(a, slab_for(h), h->uniform, has_water(h), h->st),
                    "adjoint kernel");

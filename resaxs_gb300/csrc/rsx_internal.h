@@ -55,7 +55,9 @@ struct DebyeArgs {
     const float *lambda;     // [n_q] dL/dI(q)
     double *grad;            // [n][3] sorted-order FP64 gradient accumulators
     // adjoint through tabulated pair functions: [member][n_types * n_types]
-    // [adj_nodes] nodes (A, h A', B, h B') at r = b * h, b = 0 .. adj_nodes - 1;
+    // [adj_nodes] nodes (A, h A', B, h B') at r = b * h, b = 0 .. adj_nodes - 1,
+    // with water four per node ([adj_nodes][4]: the factor products f_i f_j,
+    // f_w f_j, f_w f_i, f_w^2 that rsasa weights 1, rs_i, rs_j, rs_i rs_j);
     // h and 1/h are adj_h / adj_inv_h, or adj_geom[0] / [1] when adj_geom is set
     // (a device copy, for captured graphs whose step changes between replays)
     const float4 *adj_tab;
@@ -120,7 +122,7 @@ cudaError_t launch_forward(const DebyeArgs &a, int q_slab, bool uniform, bool wa
 cudaError_t launch_assemble(const AssembleArgs &a, cudaStream_t st);
 // adjoint through tabulated pair functions: builds the tables of the present
 // type pairs into `tab` ([n_types^2][adj_nodes] float4), then the pair pass
-cudaError_t launch_adjoint_table(const DebyeArgs &a, float4 *tab, unsigned type_mask,
+cudaError_t launch_adjoint_table(const DebyeArgs &a, float4 *tab, unsigned type_mask, bool water,
                                  cudaStream_t st);
 // forward through the gridded pair-distance distribution (grid_kernels.cu):
 // non-uniform q grids; writes partial[k][0] (one part per q) from FP64

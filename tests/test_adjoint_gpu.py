@@ -62,14 +62,35 @@ def test_backward_on_every_small_theta_level(S, oracle_lib, diag, tables):
     assert e_norm < 2e-5 and e_max < 1e-4, (e_norm, e_max)
 
 
-def test_backward_general_q_and_water(S, oracle_lib):
+@pytest.mark.parametrize("tables", [True, False])
+@pytest.mark.parametrize("ww", [0.6, -1.2])
+def test_backward_uniform_q_and_water(S, oracle_lib, tables, ww):
+    """Water on a uniform grid: the tables hold one entry per rsasa
+    combination (1, rs_i, rs_j, rs_i rs_j); without them the rotation form
+    with per-pair water factors runs."""
+    w = W.make_config(3, seed=34, n_override=500)
+    rng = np.random.default_rng(6)
+    lam = rng.normal(size=len(w.q)).astype(np.float32)
+    rs = rng.uniform(0, 1, w.n).astype(np.float32)
+    with S.Debye(w.q, w.ff, w.n, pair_tables=tables) as d:
+        d.set_water(ww, 3, rs)
+        d.calc(w.bodies)
+        g = d.backward(lam, f64=True)
+    ref = oracle_lib.debye_grad_f64(w.q, lam.astype(np.float64), w.bodies, w.ff, rsasa=rs,
+                                    water_weight=ww, water_index=3)
+    e_norm, e_max = grad_err(g, ref)
+    assert e_norm < 2e-5 and e_max < 1e-4, (e_norm, e_max)
+
+
+@pytest.mark.parametrize("tables", [True, False])
+def test_backward_general_q_and_water(S, oracle_lib, tables):
     w = W.make_config(1, seed=32, n_override=400)
     rng = np.random.default_rng(5)
     q = np.sort(rng.uniform(0, 0.5, 29)).astype(np.float32)
     ff = W.exp_form_factors(q, W.Z5, rng.uniform(0.5, 2.0, 5))
     lam = rng.normal(size=len(q)).astype(np.float32)
     rs = rng.uniform(0, 1, w.n).astype(np.float32)
-    with S.Debye(q, ff, w.n) as d:
+    with S.Debye(q, ff, w.n, pair_tables=tables) as d:
         d.set_water(0.6, 3, rs)
         d.calc(w.bodies)
         g = d.backward(lam, f64=True)
