@@ -559,11 +559,43 @@ int delta_groups(const DeltaArgs &a)
     return std::max(1, std::min(std::min(kDeltaGroups, a.n_mtiles), a.max_groups));
 }
 
+static cudaError_t delta_wide_tail(const DeltaArgs &a, int k0, int width, cudaStream_t st)
+{
+    switch (width / 16) {
+    case 1:
+        return delta_wide_launch<16>(a, k0, 1, st);
+    case 2:
+        return delta_wide_launch<32>(a, k0, 1, st);
+    case 3:
+        return delta_wide_launch<48>(a, k0, 1, st);
+    case 4:
+        return delta_wide_launch<64>(a, k0, 1, st);
+    case 5:
+        return delta_wide_launch<80>(a, k0, 1, st);
+    case 6:
+        return delta_wide_launch<96>(a, k0, 1, st);
+    case 7:
+        return delta_wide_launch<112>(a, k0, 1, st);
+    default: // a 64-q plan never needs a wider remainder slab
+        return cudaErrorInvalidValue;
+    }
+}
+
 // Uniform grids and q_slab 64 / 128: the forward's wide slab plan restricted
-// to 64-q main slabs (the two chains of a pair already interleave).
-static cudaError_t launch_delta_wide(const DeltaArgs &a, cudaStream_t st)
+// to 64-q main slabs (the two chains of a pair already interleave).  As in
+// the forward, the remainder slab goes to the aux stream when there is one,
+// so that its CTAs fill the last wave of the main launch.
+static cudaError_t launch_delta_wide(const DeltaArgs &a, cudaStream_t st, const AuxStream *aux)
 {
     const WidePlan p = wide_plan(a.n_q, 64);
+    const bool split = aux && p.full > 0 && p.tail_len > 0;
+    if (split) {
+        cudaError_t e = cudaEventRecord(aux->fork, st);
+        if (e == cudaSuccess)
+            e = cudaStreamWaitEvent(aux->stream, aux->fork, 0);
+        if (e != cudaSuccess)
+            return e;
+    }
     if (p.full > 0) {
         cudaError_t e = p.main == 64 ? delta_wide_launch<64>(a, 0, p.full, st)
                                      : delta_wide_launch<112>(a, 0, p.full, st);
@@ -572,24 +604,14 @@ static cudaError_t launch_delta_wide(const DeltaArgs &a, cudaStream_t st)
     }
     if (p.tail_len == 0)
         return cudaSuccess;
-    switch (p.tail_w / 16) {
-    case 1:
-        return delta_wide_launch<16>(a, p.tail_k0, 1, st);
-    case 2:
-        return delta_wide_launch<32>(a, p.tail_k0, 1, st);
-    case 3:
-        return delta_wide_launch<48>(a, p.tail_k0, 1, st);
-    case 4:
-        return delta_wide_launch<64>(a, p.tail_k0, 1, st);
-    case 5:
-        return delta_wide_launch<80>(a, p.tail_k0, 1, st);
-    case 6:
-        return delta_wide_launch<96>(a, p.tail_k0, 1, st);
-    case 7:
-        return delta_wide_launch<112>(a, p.tail_k0, 1, st);
-    default: // a 64-q plan never needs a wider remainder slab
-        return cudaErrorInvalidValue;
-    }
+    if (!split)
+        return delta_wide_tail(a, p.tail_k0, p.tail_w, st);
+    cudaError_t e = delta_wide_tail(a, p.tail_k0, p.tail_w, aux->stream);
+    // joined even after a failed launch, so that `st` never runs ahead of
+    // work queued on the aux stream
+    const cudaError_t ej = cudaEventRecord(aux->join, aux->stream);
+    const cudaError_t ew = ej == cudaSuccess ? cudaStreamWaitEvent(st, aux->join, 0) : ej;
+    return e != cudaSuccess ? e : ew;
 }
 
 int delta_parts(const DeltaArgs &a, int q_slab, bool uniform)
@@ -597,12 +619,13 @@ int delta_parts(const DeltaArgs &a, int q_slab, bool uniform)
     return (uniform && q_slab >= 64) ? a.n_blocks * delta_groups(a) : a.n_blocks;
 }
 
-cudaError_t launch_delta(const DeltaArgs &a, int q_slab, bool uniform, cudaStream_t st)
+cudaError_t launch_delta(const DeltaArgs &a, int q_slab, bool uniform, cudaStream_t st,
+                         const AuxStream *aux)
 {
     if (a.n_blocks == 0 || a.k == 0)
         return cudaSuccess;
     if (uniform && q_slab >= 64)
-        return launch_delta_wide(a, st);
+        return launch_delta_wide(a, st, aux);
     switch (q_slab > 32 ? 32 : q_slab) { // two chains per pair: at most 32 q per slab
     case 8:
         return delta_qs<8>(a, uniform, st);

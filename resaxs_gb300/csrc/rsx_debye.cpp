@@ -706,7 +706,7 @@ rsx_status delta_update(rsx_debye *h, const rsx_body *moved, const unsigned *idx
     int *d_idx = reinterpret_cast<int *>(h->d_moved + off_idx);
     if (h->timing)
         RSX_TRY_CUDA(cudaEventRecord(h->ev_k0, h->st), "event");
-    RSX_LAUNCH(launch_delta(a, slab_for(h), h->uniform, h->st), "delta kernel");
+    RSX_LAUNCH(launch_delta(a, slab_for(h), h->uniform, h->st, &h->aux), "delta kernel");
     if (h->timing)
         RSX_TRY_CUDA(cudaEventRecord(h->ev_k1, h->st), "event");
     RSX_LAUNCH(launch_assemble(assemble_args(h, delta_parts(a, slab_for(h), h->uniform), 1),

@@ -121,7 +121,8 @@ cudaError_t launch_forward(const DebyeArgs &a, int q_slab, bool uniform, bool wa
                            cudaStream_t st, const AuxStream *aux = nullptr);
 cudaError_t launch_assemble(const AssembleArgs &a, cudaStream_t st);
 // adjoint through tabulated pair functions: builds the tables of the present
-// type pairs into `tab` ([n_types^2][adj_nodes] float4), then the pair pass
+// type pairs into `tab` ([n_types^2][adj_nodes] float4, times 4 with water),
+// then the pair pass
 cudaError_t launch_adjoint_table(const DebyeArgs &a, float4 *tab, unsigned type_mask, bool water,
                                  cudaStream_t st);
 // forward through the gridded pair-distance distribution (grid_kernels.cu):
@@ -138,7 +139,8 @@ cudaError_t launch_forward_grid(const DebyeArgs &a, double *hist, int nodes, flo
 // the tables alone, for `n_members` members (batched passes)
 cudaError_t launch_adjoint_tables(const DebyeArgs &a, float4 *tab, unsigned type_mask,
                                   int n_members, cudaStream_t st);
-cudaError_t launch_delta(const DeltaArgs &a, int q_slab, bool uniform, cudaStream_t st);
+cudaError_t launch_delta(const DeltaArgs &a, int q_slab, bool uniform, cudaStream_t st,
+                         const AuxStream *aux = nullptr);
 // partial sums per q that launch_delta writes (the assembly's n_parts)
 int delta_parts(const DeltaArgs &a, int q_slab, bool uniform);
 int delta_groups(const DeltaArgs &a);

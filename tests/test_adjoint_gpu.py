@@ -100,6 +100,40 @@ def test_backward_general_q_and_water(S, oracle_lib, tables):
     assert e_norm < 2e-5 and e_max < 1e-4, (e_norm, e_max)
 
 
+@pytest.mark.parametrize("tables", [True, False])
+@pytest.mark.parametrize("uniform", [True, False])
+def test_backward_edge_cases(S, oracle_lib, tables, uniform):
+    """One body (no pair: a zero gradient), two bodies, and a coincident
+    pair beside a third body (the coincident pair adds nothing: d sinc/dr
+    vanishes at r = 0 and so does the direction), on a uniform and a
+    non-uniform q grid."""
+    rng = np.random.default_rng(9)
+    if uniform:
+        q = np.linspace(0, 0.5, 33).astype(np.float32)
+    else:
+        q = np.sort(rng.uniform(0, 0.5, 33)).astype(np.float32)
+        q[0] = 0.0
+    ff = W.exp_form_factors(q, (6, 8), (1.0, 0.5))
+    lam = rng.normal(size=len(q)).astype(np.float32)
+    cases = [
+        W.pack_bodies(np.array([[1.0, 2.0, 3.0]]), np.array([1])),
+        W.pack_bodies(np.array([[1.0, 2.0, 3.0], [4.5, -2.0, 7.25]]), np.array([0, 1])),
+        W.pack_bodies(np.array([[1.0, 2.0, 3.0], [1.0, 2.0, 3.0], [-3.0, 0.5, 2.0]]),
+                      np.array([0, 1, 1])),
+    ]
+    for bodies in cases:
+        with S.Debye(q, ff, len(bodies), pair_tables=tables) as d:
+            d.calc(bodies)
+            g = np.asarray(d.backward(lam, f64=True), np.float64)
+        assert g.shape == (len(bodies), 3) and np.all(np.isfinite(g))
+        if len(bodies) == 1:
+            assert np.all(g == 0)
+            continue
+        ref = oracle_lib.debye_grad_f64(q, lam.astype(np.float64), bodies, ff)
+        e_norm, e_max = grad_err(g, ref)
+        assert e_norm < 2e-5 and e_max < 1e-4, (len(bodies), e_norm, e_max)
+
+
 def test_autograd_wrapper_vs_finite_differences(S, oracle_lib):
     """64 seeded coordinates, FP64 central differences with h = 1e-4 A (the
     represented FP32 step is used as the divisor)."""
