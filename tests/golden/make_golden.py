@@ -4,7 +4,8 @@ Run in a container that has the reference sources (default /root/reference):
 
     python tests/golden/make_golden.py [reference_root]
 
-Outputs (committed; the GPU machine has no reference tree):
+Outputs (committed, so that tests on machines without the reference tree
+can use them):
 
 * ``test1888.npz`` -- the reference's own known-answer fixture
   (test_resaxs/test1888.{pos_matrix,ff_db,q_vec,Iq_vec}.txt: 1888 bodies,

@@ -1,5 +1,5 @@
 """CPU tests of the oracle itself: it must reproduce the reference's own known
-answers before it may judge the GPU path."""
+answers before the GPU path is checked against it."""
 import numpy as np
 import pytest
 
