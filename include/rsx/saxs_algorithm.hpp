@@ -174,8 +174,6 @@ public:
         check(rsx_debye_create(params_.qq_.data(), (int)params_.qq_.size(), ff.factors_.data(),
                                n_f, (int)params_.n_bodies_, &o, &h_));
         ff.clear_dirty();
-        params_.get_implicit_water_params().set_water_weight(
-            params_.get_implicit_water_params().water_weight_);
         computing_ = false;
     }
 
@@ -184,7 +182,11 @@ public:
         require(h_ != nullptr, error::SAXS_ARGS_NOT_SET, "initialize() was not called");
         require(bodies.size() == params_.n_bodies_, error::SAXS_INVALID_ARG,
                 "different number of bodies expected in calc_curve()");
-        push_params();
+        // a full calculation always takes the current water parameters, dirty
+        // or not, as the reference's calc_curve sets the weight argument on
+        // every call (saxs_alg_cl_gpu_pt_wf.cpp:433-438); this also carries
+        // them into a handle made by a later initialize()
+        push_params(true);
         out_Iqq.resize(params_.qq_.size());
         check(rsx_debye_calc(h_, bodies.data(), out_Iqq.data()));
         computing_ = true;
@@ -225,7 +227,7 @@ private:
             throw error(code, msg);
     }
 
-    void push_params()
+    void push_params(bool water_always = false)
     {
         auto &ff = params_.get_ff_params();
         auto &w = params_.get_implicit_water_params();
@@ -234,7 +236,7 @@ private:
             check(rsx_debye_set_factors(h_, ff.factors_.data(), n_f));
             ff.clear_dirty();
         }
-        if (w.is_dirty()) {
+        if (w.is_dirty() || water_always) {
             const int widx = ff.water_ff_index_ >= 0 ? ff.water_ff_index_ : 0;
             const auto &rs = w.rsasa();
             check(rsx_debye_set_water(h_, (float)w.water_weight_, widx,

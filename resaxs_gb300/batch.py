@@ -7,7 +7,8 @@ import ctypes
 
 import numpy as np
 
-from ._lib import DebyeOptions, check, lib
+from . import _lib
+from ._lib import DebyeOptions, ResaxsError, check, lib
 
 __all__ = ["DebyeBatch"]
 
@@ -54,8 +55,14 @@ class DebyeBatch:
 
     def _pack(self, members):
         if isinstance(members, np.ndarray):
-            return np.ascontiguousarray(members, np.float32)
-        return np.ascontiguousarray(np.concatenate(members, axis=0), np.float32)
+            b = np.ascontiguousarray(members, np.float32).reshape(-1)
+        else:
+            b = np.ascontiguousarray(np.concatenate(members, axis=0), np.float32).reshape(-1)
+        # the C calls read every member's bodies, 4 floats each
+        if b.size < 4 * self.n_total:
+            raise ResaxsError(_lib.RSX_INVALID_ARG,
+                              f"need {self.n_total} bodies over all members, got {b.size // 4}")
+        return b
 
     def forward(self, members) -> np.ndarray:
         b = self._pack(members)
@@ -66,6 +73,9 @@ class DebyeBatch:
     def set_targets(self, targets, sigma):
         t = np.ascontiguousarray(targets, np.float32).reshape(-1)
         s = np.ascontiguousarray(sigma, np.float32).reshape(-1)
+        # the C call reads n_members x n_q values from each
+        if t.size < self.n_members * self.n_q or s.size < self.n_members * self.n_q:
+            raise ResaxsError(_lib.RSX_INVALID_ARG, "targets and sigma must be n_members x n_q")
         check(lib().rsx_batch_set_targets(self._h, t, s))
 
     def forward_chi2_backward(self, members):

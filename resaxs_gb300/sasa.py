@@ -33,6 +33,8 @@ class DotSphereSasa:
         if unit_dots is None:
             unit_dots = fibonacci_dots(n_dots)
         self.unit = np.ascontiguousarray(unit_dots, np.float32)
+        if self.unit.ndim != 2 or self.unit.shape[1] != 3:
+            raise ResaxsError(_lib.RSX_INVALID_ARG, "unit dots must be [n_dots][3]")
         self.n = int(n_atoms)
         self.n_dots = len(self.unit)
         self.probe = float(probe)
@@ -58,18 +60,24 @@ class DotSphereSasa:
     def __exit__(self, *exc):
         self.close()
 
+    def _inputs(self, atoms, radii):
+        # the C calls read n atoms of 4 floats and n radii
+        atoms = np.ascontiguousarray(atoms, np.float32).reshape(-1)
+        radii = np.ascontiguousarray(radii, np.float32).reshape(-1)
+        if atoms.size < 4 * self.n or radii.size < self.n:
+            raise ResaxsError(_lib.RSX_INVALID_ARG, f"need {self.n} atoms and {self.n} radii")
+        return atoms, radii
+
     def counts(self, atoms, radii) -> np.ndarray:
-        atoms = np.ascontiguousarray(atoms, np.float32)
-        radii = np.ascontiguousarray(radii, np.float32)
+        atoms, radii = self._inputs(atoms, radii)
         out = np.zeros(self.n, np.uint32)
-        check(lib().rsx_sasa_counts(self._h, atoms.reshape(-1), radii, out))
+        check(lib().rsx_sasa_counts(self._h, atoms, radii, out))
         return out
 
     def rsasa(self, atoms, radii) -> np.ndarray:
-        atoms = np.ascontiguousarray(atoms, np.float32)
-        radii = np.ascontiguousarray(radii, np.float32)
+        atoms, radii = self._inputs(atoms, radii)
         out = np.zeros(self.n, np.float32)
-        check(lib().rsx_sasa_calc(self._h, atoms.reshape(-1), radii, out))
+        check(lib().rsx_sasa_calc(self._h, atoms, radii, out))
         return out
 
     def stats(self):

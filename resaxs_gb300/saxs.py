@@ -89,18 +89,31 @@ class Debye:
     # parameters ----------------------------------------------------------
     def set_factors(self, factors):
         factors = _f32(factors)
+        # the C call reads n_q rows of n_factors values
+        if factors.ndim != 2 or factors.shape[0] != self.n_q:
+            raise ResaxsError(_lib.RSX_INVALID_ARG, "factor table must be [n_q][n_factors]")
         check(lib().rsx_debye_set_factors(self._h, factors.reshape(-1), factors.shape[-1]))
 
     def set_water(self, weight: float, water_index: int, rsasa=None):
         ptr = None
         if rsasa is not None:
-            self._rsasa_keep = _f32(rsasa)
+            keep = _f32(rsasa).reshape(-1)
+            # the C call reads one value per body
+            if keep.size != self.n:
+                raise ResaxsError(_lib.RSX_INVALID_ARG, "rsasa needs one value per body")
+            self._rsasa_keep = keep
             ptr = self._rsasa_keep.ctypes.data
         check(lib().rsx_debye_set_water(self._h, float(weight), int(water_index), ptr))
 
     # computation ---------------------------------------------------------
+    def _need(self, a, count: int, what: str):
+        # the C calls read `count` floats from the pointer they are given
+        if a.size < count:
+            raise ResaxsError(_lib.RSX_INVALID_ARG, f"{what}: need {count} values, got {a.size}")
+        return a
+
     def calc(self, bodies) -> np.ndarray:
-        bodies = _f32(bodies)
+        bodies = self._need(_f32(bodies), 4 * self.n, "bodies")
         out = np.zeros(self.n_q, np.float32)
         check(lib().rsx_debye_calc(self._h, bodies.reshape(-1), out))
         return out
@@ -108,22 +121,23 @@ class Debye:
     def calc_shard(self, bodies, shard: int, n_shards: int) -> np.ndarray:
         """This shard's additive FP64 contribution to I(q) (rsx_debye_calc_shard);
         the sum over shards 0..n_shards-1 is the full curve."""
-        bodies = _f32(bodies)
+        bodies = self._need(_f32(bodies), 4 * self.n, "bodies")
         out = np.zeros(self.n_q, np.float64)
         check(lib().rsx_debye_calc_shard(self._h, bodies.reshape(-1), int(shard), int(n_shards),
                                          out))
         return out
 
     def recalc_range(self, bodies, start: int, length: int) -> np.ndarray:
-        bodies = _f32(bodies)
+        bodies = self._need(_f32(bodies), 4 * min(int(start) + int(length), self.n),
+                            "bodies vector too small in recalc_range")
         out = np.zeros(self.n_q, np.float32)
         check(lib().rsx_debye_recalc_range(self._h, bodies.reshape(-1), int(start), int(length),
                                            out))
         return out
 
     def recalc_indices(self, moved, idx) -> np.ndarray:
-        moved = _f32(moved)
-        idx = np.ascontiguousarray(idx, dtype=np.uint32)
+        idx = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1)
+        moved = self._need(_f32(moved), 4 * len(idx), "moved bodies")
         out = np.zeros(self.n_q, np.float32)
         check(lib().rsx_debye_recalc_indices(self._h, moved.reshape(-1), idx, len(idx), out))
         return out
@@ -152,7 +166,7 @@ class Debye:
         return k.value, c.value
 
     def backward(self, dl_diq, f64: bool = False) -> np.ndarray:
-        lam = _f32(dl_diq)
+        lam = self._need(_f32(dl_diq).reshape(-1), self.n_q, "dL/dI")
         if f64:
             g = np.zeros((self.n, 3), np.float64)
             check(lib().rsx_debye_backward_f64(self._h, lam, g.reshape(-1)))
@@ -162,8 +176,8 @@ class Debye:
         return g
 
     def chi2_backward(self, target, sigma, want_grad: bool = True):
-        target = _f32(target)
-        sigma = _f32(sigma)
+        target = self._need(_f32(target).reshape(-1), self.n_q, "target curve")
+        sigma = self._need(_f32(sigma).reshape(-1), self.n_q, "sigma")
         c2 = ctypes.c_double()
         g = np.zeros((self.n, 3), np.float32) if want_grad else None
         check(lib().rsx_debye_chi2_backward(self._h, target, sigma, ctypes.byref(c2),
@@ -302,14 +316,14 @@ class SaxsAlgorithm:
         p.get_ff_params().clear_dirty()
         self._computing = False
 
-    def _push_params(self):
+    def _push_params(self, water_always: bool = False):
         p = self._params
         ff = p.get_ff_params()
         w = p.get_implicit_water_params()
         if ff.is_dirty():
             self._d.set_factors(ff.factors)
             ff.clear_dirty()
-        if w.is_dirty():
+        if w.is_dirty() or water_always:
             idx = ff.water_ff_index if ff.water_ff_index >= 0 else 0
             self._d.set_water(w.water_weight, idx, w.rsasa)
             w.clear_dirty()
@@ -330,7 +344,11 @@ class SaxsAlgorithm:
         if len(bodies) != self._params.n_bodies:
             raise ResaxsError(_lib.RSX_INVALID_ARG,
                               "different number of bodies expected in calc_curve()")
-        self._push_params()
+        # a full calculation always takes the current water parameters, as the
+        # reference's calc_curve sets the weight argument on every call
+        # (saxs_alg_cl_gpu_pt_wf.cpp:433-438); this also carries them into a
+        # handle made by a later initialize()
+        self._push_params(water_always=True)
         res = self._d.calc(bodies)
         self._computing = True
         return self._emit(out_iqq, res)

@@ -272,6 +272,28 @@ def test_invalid_type_rejected(saxs):
         assert e.value.code == _lib.RSX_INVALID_ARG
 
 
+def test_short_host_arrays_rejected_before_the_call(saxs):
+    """The Python handles check array sizes before handing pointers to the C
+    calls, which read a fixed count from each; the handle stays usable."""
+    from resaxs_gb300 import _lib
+    q = W.q_grid(8, 0.5)
+    ff = np.ones((8, 2), np.float32)
+    b = W.pack_bodies(np.arange(12, dtype=np.float32).reshape(4, 3), np.array([0, 1, 0, 1]))
+    with saxs.Debye(q, ff, 4) as d:
+        for call in (lambda: d.calc(b[:3]), lambda: d.set_factors(ff[:7]),
+                     lambda: d.set_water(0.5, 1, np.zeros(3, np.float32)),
+                     lambda: d.recalc_indices(b[:1], np.array([0, 1], np.uint32)),
+                     lambda: d.backward(np.ones(7, np.float32))):
+            with pytest.raises(_lib.ResaxsError) as e:
+                call()
+            assert e.value.code == _lib.RSX_INVALID_ARG
+        d.calc(b)
+        with pytest.raises(_lib.ResaxsError) as e:
+            d.recalc_range(b[:2], 1, 3)
+        assert e.value.code == _lib.RSX_INVALID_ARG
+        assert np.all(np.isfinite(d.calc(b)))
+
+
 def test_permutation_and_translation_invariance_full_size(saxs):
     """Size-independent properties at the full 20,000-body size."""
     w = W.make_config(2, seed=0)
