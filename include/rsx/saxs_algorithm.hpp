@@ -153,6 +153,8 @@ public:
     {
         if (h_)
             rsx_debye_destroy(h_);
+        if (sasa_)
+            rsx_sasa_destroy(sasa_);
     }
 
     saxs_params<FLT_T> &access_params() { return params_; }
@@ -167,6 +169,9 @@ public:
         if (h_)
             rsx_debye_destroy(h_);
         h_ = nullptr;
+        if (sasa_)
+            rsx_sasa_destroy(sasa_);
+        sasa_ = nullptr;
         rsx_debye_options o;
         rsx_debye_default_options(&o);
         o.device = params_.device_;
@@ -186,6 +191,7 @@ public:
         // or not, as the reference's calc_curve sets the weight argument on
         // every call (saxs_alg_cl_gpu_pt_wf.cpp:433-438); this also carries
         // them into a handle made by a later initialize()
+        update_rsasa(bodies, true);
         push_params(true);
         out_Iqq.resize(params_.qq_.size());
         check(rsx_debye_calc(h_, bodies.data(), out_Iqq.data()));
@@ -199,6 +205,7 @@ public:
                 "recalc_curve() called before an initial call to calc_curve()");
         require(bodies.size() >= (size_t)upd_start + upd_length, error::SAXS_INVALID_ARG,
                 "bodies vector too small in recalc_curve()");
+        update_rsasa(bodies, upd_length > 0);
         push_params();
         out_Iqq.resize(params_.qq_.size());
         check(rsx_debye_recalc_range(h_, bodies.data(), upd_start, upd_length, out_Iqq.data()));
@@ -245,8 +252,47 @@ private:
         }
     }
 
+    // The water term's rsasa, as the reference's GPU algorithm keeps it
+    // (saxs_alg_cl_gpu_pt_wf.cpp:82-96, 333-401): with a non-zero water
+    // weight every update of the bodies recomputes rsasa from all bodies with
+    // the dot-sphere SASA (32 dodecahedron/icosahedron dots per atom, probe
+    // 1.8 A, the atomic radius of each body's type), unless no_rsasa_recalc_
+    // is set and rsasa values are present.  Values a caller wrote through
+    // access_rsasa() therefore survive only with no_rsasa_recalc_ set (the
+    // reference overwrites them on the first update in any case).
+    void update_rsasa(const std::vector<rsx_body> &bodies, bool moved)
+    {
+        auto &w = params_.get_implicit_water_params();
+        if (w.water_weight_ == 0)
+            return;
+        const size_t n = params_.n_bodies_;
+        const bool present = w.rsasa().size() >= n;
+        if (present && (w.no_rsasa_recalc_ || !moved))
+            return;
+        require(bodies.size() >= n, error::SAXS_INVALID_ARG,
+                "the water term's SASA needs every body");
+        if (!sasa_) {
+            float dots[32 * 3];
+            check(rsx_sasa_dodeca_icosa_dots(dots));
+            check(rsx_sasa_create((int)n, dots, 32, 1.8f, params_.device_, &sasa_));
+        }
+        float radius_of_type[16];
+        check(rsx_ff_radii(radius_of_type));
+        std::vector<float> radii(n);
+        for (size_t i = 0; i < n; ++i) {
+            const unsigned t = get_factor_index(bodies[i]);
+            require(t < 16, error::SAXS_INVALID_ARG,
+                    "the water term's SASA needs an atomic type (0..15) on every body");
+            radii[i] = radius_of_type[t];
+        }
+        auto &rs = w.access_rsasa(); // marks the water params dirty: pushed next
+        rs.resize(n);
+        check(rsx_sasa_calc(sasa_, bodies.data(), radii.data(), rs.data()));
+    }
+
     saxs_params<FLT_T> params_;
     rsx_debye *h_ = nullptr;
+    rsx_sasa *sasa_ = nullptr;
     bool computing_ = false;
 };
 

@@ -297,6 +297,7 @@ class SaxsAlgorithm:
     def __init__(self, **debye_kwargs):
         self._params = SaxsParams()
         self._d = None
+        self._sasa = None
         self._kw = debye_kwargs
         self._computing = False
 
@@ -312,6 +313,9 @@ class SaxsAlgorithm:
             raise ResaxsError(_lib.RSX_ARGS_NOT_SET, "no form-factor table set")
         if self._d is not None:
             self._d.close()
+        if self._sasa is not None:
+            self._sasa.close()
+            self._sasa = None
         self._d = Debye(p.qq, ff, p.n_bodies, device=p.device, **self._kw)
         p.get_ff_params().clear_dirty()
         self._computing = False
@@ -327,6 +331,36 @@ class SaxsAlgorithm:
             idx = ff.water_ff_index if ff.water_ff_index >= 0 else 0
             self._d.set_water(w.water_weight, idx, w.rsasa)
             w.clear_dirty()
+
+    def _update_rsasa(self, bodies, moved: bool):
+        """The water term's rsasa as the reference's GPU algorithm keeps it
+        (saxs_alg_cl_gpu_pt_wf.cpp:82-96, 333-401): with a non-zero water weight
+        every update of the bodies recomputes rsasa from all bodies with the
+        dot-sphere SASA (32 dodecahedron/icosahedron dots, probe 1.8 A, the
+        atomic radius of each body's type), unless ``no_rsasa_recalc`` is set
+        and rsasa values are present."""
+        w = self._params.get_implicit_water_params()
+        if w.water_weight == 0:
+            return
+        n = self._params.n_bodies
+        present = w.rsasa is not None and len(w.rsasa) >= n
+        if present and (w.no_rsasa_recalc or not moved):
+            return
+        from .sasa import DotSphereSasa, dodeca_icosa_dots
+        bodies = np.ascontiguousarray(bodies, np.float32).reshape(-1, 4)
+        if len(bodies) < n:
+            raise ResaxsError(_lib.RSX_INVALID_ARG, "the water term's SASA needs every body")
+        types = bodies[:n].view(np.uint32)[:, 3]
+        if types.size and types.max() >= 16:
+            raise ResaxsError(_lib.RSX_INVALID_ARG,
+                              "the water term's SASA needs an atomic type (0..15) on every body")
+        radii = np.zeros(16, np.float32)
+        check(lib().rsx_ff_radii(radii))
+        if self._sasa is None:
+            self._sasa = DotSphereSasa(n, unit_dots=dodeca_icosa_dots(), probe=1.8,
+                                       device=self._params.device)
+        w.access_rsasa()
+        w.rsasa = self._sasa.rsasa(bodies[:n], radii[types])
 
     @staticmethod
     def _emit(out, values):
@@ -348,6 +382,7 @@ class SaxsAlgorithm:
         # reference's calc_curve sets the weight argument on every call
         # (saxs_alg_cl_gpu_pt_wf.cpp:433-438); this also carries them into a
         # handle made by a later initialize()
+        self._update_rsasa(bodies, moved=True)
         self._push_params(water_always=True)
         res = self._d.calc(bodies)
         self._computing = True
@@ -359,6 +394,7 @@ class SaxsAlgorithm:
                               "recalc_curve() called before an initial call to calc_curve()")
         if len(bodies) < upd_start + upd_length:
             raise ResaxsError(_lib.RSX_INVALID_ARG, "bodies vector too small in recalc_curve()")
+        self._update_rsasa(bodies, moved=upd_length > 0)
         self._push_params()
         res = self._d.recalc_range(bodies, upd_start, upd_length)
         return self._emit(out_iqq, res)

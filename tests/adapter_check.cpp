@@ -10,14 +10,20 @@
 //       in.bin:  int32 n, n_q, n_types, water_index, start, length;
 //                float q[n_q], factors[n_q][n_types], bodies[n][4], rsasa[n],
 //                radius_of_type[n_types]
-//       out.bin: float curves[6][n_q], then float rsasa_out[n]
+//       out.bin: float curves[8][n_q], then float rsasa_out[n],
+//                water_rsasa[n], water_rsasa_moved[n]
 //         0 calc_curve(bodies)
 //         1 recalc_curve after bodies [start, start+length) moved by +0.3 A in x
 //         2 after revert() to the committed state of curve 0, recalc_curve
 //           with the same bodies moved by +0.6 A instead
 //         3 calc_curve of the +0.6 A bodies after commit()
-//         4 calc_curve(bodies) with water weight 0.7 and the given rsasa
+//         4 calc_curve(bodies) with water weight 0.7, the given rsasa and
+//           no_rsasa_recalc_ set (the given values are kept)
 //         5 the same after a second initialize() (water params already pushed)
+//         6 calc_curve(bodies) with water weight 0.7 and no_rsasa_recalc_
+//           cleared: rsasa comes from the adapter's own SASA (water_rsasa)
+//         7 then recalc_curve of the +0.3 A bodies: rsasa recomputed
+//           (water_rsasa_moved)
 //       rsasa_out: calc_rsasa with 960 Fibonacci dots, probe 1.4
 #include "rsx/saxs_algorithm.hpp"
 
@@ -117,7 +123,7 @@ int run_gpu(const char *in_path, const char *out_path)
         moved2[i].x += 0.6f;
     }
 
-    std::vector<std::vector<float>> curves(6);
+    std::vector<std::vector<float>> curves(8);
     auto alg = rsx::algorithm::create_saxs_gpu();
     auto &params = alg->access_params();
     params.initialize(q, bodies, {0});
@@ -134,10 +140,16 @@ int run_gpu(const char *in_path, const char *out_path)
 
     auto &water = params.get_implicit_water_params();
     water.set_water_weight(0.7f);
+    water.no_rsasa_recalc_ = true;
     water.access_rsasa() = rsasa;
     alg->calc_curve(bodies, curves[4]);
     alg->initialize(); // a new handle; the water params are no longer dirty
     alg->calc_curve(bodies, curves[5]);
+    water.no_rsasa_recalc_ = false;
+    alg->calc_curve(bodies, curves[6]);
+    const std::vector<float> water_rsasa = water.rsasa();
+    alg->recalc_curve(moved, start, length, curves[7]);
+    const std::vector<float> water_rsasa_moved = water.rsasa();
 
     std::vector<float> dots(960 * 3);
     rsx::check(rsx_sasa_fibonacci_dots(960, dots.data()));
@@ -154,7 +166,14 @@ int run_gpu(const char *in_path, const char *out_path)
         }
         o.write(reinterpret_cast<const char *>(c.data()), std::streamsize(c.size() * 4));
     }
-    o.write(reinterpret_cast<const char *>(rsasa_out.data()), std::streamsize(rsasa_out.size() * 4));
+    const std::vector<float> *tails[] = {&rsasa_out, &water_rsasa, &water_rsasa_moved};
+    for (const std::vector<float> *v : tails) {
+        if ((int)v->size() != n) {
+            std::fprintf(stderr, "rsasa of %zu values, want %d\n", v->size(), n);
+            return 3;
+        }
+        o.write(reinterpret_cast<const char *>(v->data()), std::streamsize(v->size() * 4));
+    }
     return o ? 0 : 4;
 }
 

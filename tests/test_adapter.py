@@ -7,8 +7,9 @@ On the CPU: the header compiles against librsx, and the interface's error
 paths raise rsx::error with the reference's codes (resaxs.hpp:212-220),
 including initialize() without a CUDA device (no CPU path).  On the GPU: the
 curves of calc_curve / recalc_curve / commit / revert, with and without the
-implicit-water term and across a second initialize(), against the FP64
-oracle, and calc_rsasa against the strict-FP32 oracle counts."""
+implicit-water term (given rsasa, and the adapter's own SASA of the bodies
+as the reference computes it) and across a second initialize(), against the
+FP64 oracle, and calc_rsasa against the strict-FP32 oracle counts."""
 import os
 import subprocess
 
@@ -66,8 +67,9 @@ def test_adapter_curves_and_rsasa(adapter_exe, oracle_lib, tmp_path):
                        text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     raw = np.fromfile(outp, np.float32)
-    assert raw.size == 6 * n_q + n
-    curves, got_rsasa = raw[:6 * n_q].reshape(6, n_q), raw[6 * n_q:]
+    assert raw.size == 8 * n_q + 3 * n
+    curves = raw[:8 * n_q].reshape(8, n_q)
+    got_rsasa, water_rsasa, water_rsasa_moved = raw[8 * n_q:].reshape(3, n)
 
     moved, moved2 = w.bodies.copy(), w.bodies.copy()
     moved[start:start + length, 0] += np.float32(0.3)
@@ -91,3 +93,20 @@ def test_adapter_curves_and_rsasa(adapter_exe, oracle_lib, tmp_path):
     counts = oracle_lib.sasa_counts(w.bodies, radius_of_type[types], dots, 1.4)
     want = counts.astype(np.float32) / np.float32(960)
     assert np.array_equal(got_rsasa, want)
+
+    # the water term's own SASA: 32 dodecahedron/icosahedron dots, probe 1.8 A,
+    # the atomic radius of each body's type (saxs_alg_cl_gpu_pt_wf.cpp:82-96)
+    from resaxs_gb300 import _lib
+    from resaxs_gb300.sasa import dodeca_icosa_dots
+    atomic_radii = np.zeros(16, np.float32)
+    _lib.check(_lib.lib().rsx_ff_radii(atomic_radii))
+    ico = dodeca_icosa_dots()
+    for bodies, got, curve in ((w.bodies, water_rsasa, curves[6]),
+                               (moved, water_rsasa_moved, curves[7])):
+        c = oracle_lib.sasa_counts(bodies, atomic_radii[types], ico, 1.8)
+        rs = c.astype(np.float32) / np.float32(32)
+        assert np.array_equal(got, rs)
+        ref = oracle_lib.debye_f64(w.q, bodies, w.ff, rsasa=rs, water_weight=0.7,
+                                   water_index=water_index)
+        assert rel(curve, ref) < TOL
+    assert rel(curves[6], ref_w) > 1e-4
