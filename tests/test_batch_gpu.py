@@ -163,3 +163,13 @@ def test_batch_errors():
         with pytest.raises(_lib.ResaxsError) as e:
             b.forward(bad)
         assert e.value.code == _lib.RSX_INVALID_ARG
+        # short host arrays are refused before the C calls read from them
+        good = W.pack_bodies(np.arange(15, dtype=np.float32).reshape(5, 3),
+                             np.array([0, 1, 0, 1, 0]))
+        for call in (lambda: b.forward(good[:4]),
+                     lambda: b.set_targets(np.ones((1, 16), np.float32),
+                                           np.ones((2, 16), np.float32))):
+            with pytest.raises(_lib.ResaxsError) as e:
+                call()
+            assert e.value.code == _lib.RSX_INVALID_ARG
+        assert np.all(np.isfinite(b.forward(good)))

@@ -138,3 +138,10 @@ def test_bad_inputs_rejected():
             s.counts(bad, np.ones(3, np.float32))
     with pytest.raises(_lib.ResaxsError):
         DotSphereSasa(3, unit_dots=np.zeros((4097, 3), np.float32))
+    # short host arrays are refused before the C call reads n values from them
+    with DotSphereSasa(3, n_dots=32) as s:
+        for args in ((atoms[:2], np.ones(3, np.float32)), (atoms, np.ones(2, np.float32))):
+            with pytest.raises(_lib.ResaxsError) as e:
+                s.rsasa(*args)
+            assert e.value.code == _lib.RSX_INVALID_ARG
+        assert s.counts(atoms, np.ones(3, np.float32)).shape == (3,)
