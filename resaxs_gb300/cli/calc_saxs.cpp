@@ -529,7 +529,9 @@ int main(int argc, char **argv)
         std::vector<float> q = ref.q;
         if (q.empty()) {
             q.resize(a.q_n);
-            const float step = (a.q_n > 0) ? (a.q_max - a.q_min) / (a.q_n - 1) : 0;
+            // one q value is q_min (the reference divides by q_n - 1 = 0 there
+            // and writes NaN, calc_saxs.cpp:60-62)
+            const float step = (a.q_n > 1) ? (a.q_max - a.q_min) / (a.q_n - 1) : 0;
             for (unsigned i = 0; i < a.q_n; ++i)
                 q[i] = a.q_min + i * step;
         }
