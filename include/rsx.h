@@ -88,6 +88,12 @@ rsx_status rsx_debug_wide_plan(int n_q, int q_slab, int *out);
 rsx_status rsx_debug_shard_items(const rsx_body *bodies, int n_bodies, int n_factors,
                                  int max_items, int n_shards, int *bounds, double *pairs);
 
+/* Host-only view of the autotuning cache (the q-slab winners, loaded once from
+ * the file named by RSX_AUTOTUNE_CACHE when it is set): 1 and *q_slab when
+ * `key` has an entry, else 0.  Lines of the file whose value is not a q-slab
+ * size rsx_debye_create accepts (8, 16, 32, 64, 128) are ignored. */
+int rsx_debug_autotune_lookup(const char *key, int *q_slab);
+
 /* Measures the sustained FP32 FMA rate of `device` (-1 = current) with a
  * register-resident FMA-chain kernel on every SM: *fma_per_s = lane FMAs per
  * second.  The denominator of the pair*q roofline. */

@@ -83,6 +83,7 @@ SIGNATURES = [
     ("rsx_debug_wide_plan", _st, [_i, _i, np.ctypeslib.ndpointer(np.int32)]),
     ("rsx_debug_shard_items", _st, [_f32p, _i, _i, _i, _i, np.ctypeslib.ndpointer(np.int32),
                                     _vp]),
+    ("rsx_debug_autotune_lookup", _i, [ctypes.c_char_p, ctypes.POINTER(_i)]),
     ("rsx_debye_recalc_range", _st, [_vp, _f32p, _u, _u, _f32p]),
     ("rsx_debye_recalc_indices", _st, [_vp, _f32p, _u32p, _u, _f32p]),
     ("rsx_debye_commit", _st, [_vp]),

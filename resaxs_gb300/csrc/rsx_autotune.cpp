@@ -5,6 +5,7 @@
 // The cache lives in the process; when RSX_AUTOTUNE_CACHE names a file it is
 // also loaded from and appended to it (one "key value" line per entry).
 #include "rsx_autotune.h"
+#include "rsx.h"
 
 #include <cstdio>
 #include <cstdlib>
@@ -14,6 +15,8 @@
 #include <sstream>
 
 namespace rsx {
+
+static bool valid_q_slab(long v) { return v == 8 || v == 16 || v == 32 || v == 64 || v == 128; }
 
 static std::mutex g_mu;
 static std::map<std::string, int> g_cache;
@@ -33,7 +36,14 @@ static void load_file_locked()
         const auto sp = line.rfind(' ');
         if (sp == std::string::npos)
             continue;
-        g_cache[line.substr(0, sp)] = std::atoi(line.c_str() + sp + 1);
+        // the file is outside the library's control: keep only q-slab sizes
+        // that rsx_debye_create accepts, so an edited or damaged line can
+        // never select a kernel shape that does not exist
+        char *end = nullptr;
+        const long v = std::strtol(line.c_str() + sp + 1, &end, 10);
+        if (end == line.c_str() + sp + 1 || *end != '\0' || !valid_q_slab(v))
+            continue;
+        g_cache[line.substr(0, sp)] = (int)v;
     }
 }
 
@@ -89,3 +99,12 @@ void autotune_clear()
 } // namespace rsx
 
 extern "C" void rsx_autotune_clear(void) { rsx::autotune_clear(); }
+
+extern "C" int rsx_debug_autotune_lookup(const char *key, int *q_slab)
+{
+    int v = 0;
+    if (!key || !q_slab || !rsx::autotune_lookup(key, &v))
+        return 0;
+    *q_slab = v;
+    return 1;
+}

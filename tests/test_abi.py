@@ -141,3 +141,33 @@ def test_theta_level_thresholds(librsx):
     assert lv(1, dq, float("inf")) == 0
     assert lv(1, dq, float("nan")) == 0
     assert lv(1, dq, -1.0) == 0
+
+
+def test_autotune_cache_file_keeps_only_valid_slabs(tmp_path):
+    """The q-slab cache file named by RSX_AUTOTUNE_CACHE is read once per
+    process; lines whose value is not a q-slab size rsx_debye_create accepts
+    are ignored.  Run in a fresh process so the file is loaded there."""
+    import subprocess
+    import sys
+    cache = tmp_path / "slabs.txt"
+    cache.write_text("dev|forward|14|201|5|1|0 128\n"
+                     "dev|forward|10|101|5|1|0 48\n"
+                     "dev|forward|11|101|5|1|0 -16\n"
+                     "dev|forward|12|101|5|1|0 32x\n"
+                     "no_value_line\n"
+                     "dev|forward|13|64|2|0|1 16\n")
+    code = (
+        "import ctypes\n"
+        "from resaxs_gb300 import _lib\n"
+        "L = _lib.lib()\n"
+        "for k in ['dev|forward|14|201|5|1|0', 'dev|forward|10|101|5|1|0',\n"
+        "          'dev|forward|11|101|5|1|0', 'dev|forward|12|101|5|1|0',\n"
+        "          'dev|forward|13|64|2|0|1', 'missing']:\n"
+        "    v = ctypes.c_int(0)\n"
+        "    print(L.rsx_debug_autotune_lookup(k.encode(), ctypes.byref(v)), v.value)\n")
+    env = dict(os.environ, RSX_AUTOTUNE_CACHE=str(cache))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True,
+                       cwd=ROOT, env=env, timeout=120)
+    assert r.returncode == 0, r.stderr
+    rows = [tuple(map(int, line.split())) for line in r.stdout.split("\n") if line.strip()]
+    assert rows == [(1, 128), (0, 0), (0, 0), (0, 0), (1, 16), (0, 0)]
