@@ -213,3 +213,52 @@ def test_cli_self_test_flag(cli, tmp_path, oracle_lib):
     # the written curve is the average of 3 models; -t compares it with the
     # first model alone, as the reference's verify_result does
     assert np.isfinite(chisq) and chisq >= 0
+
+
+def test_pdb_reader_survives_damaged_files(tmp_path):
+    """Seeded damage to a PDB file (cut, overwritten, repeated, dropped lines,
+    random bytes, stray MODEL/ENDMDL/END records): the reader returns a status
+    and never crashes, and rsx_pdb_read fills exactly the bodies rsx_pdb_count
+    announced.  Runs in a child process so that a crash fails only this test."""
+    import subprocess
+    import sys
+    code = r'''
+import ctypes, sys
+import numpy as np
+from resaxs_gb300 import _lib
+L = _lib.lib()
+src = open(sys.argv[1], "rb").read().split(b"\n")
+rng = np.random.default_rng(11)
+for it in range(150):
+    lines = list(src)
+    for _ in range(int(rng.integers(1, 40))):
+        i = int(rng.integers(0, len(lines)))
+        op, ln = int(rng.integers(0, 6)), lines[i]
+        if op == 0 and ln:
+            lines[i] = ln[: int(rng.integers(0, len(ln) + 1))]
+        elif op == 1 and ln:
+            j = int(rng.integers(0, len(ln)))
+            lines[i] = ln[:j] + bytes([int(rng.integers(0, 256))]) + ln[j + 1:]
+        elif op == 2:
+            lines.insert(i, rng.integers(0, 256, int(rng.integers(0, 200))).astype(np.uint8).tobytes())
+        elif op == 3:
+            lines.insert(i, [b"MODEL     9", b"ENDMDL", b"END", b"TER", b"ATOM", b"HETATM"][int(rng.integers(0, 6))])
+        elif op == 4:
+            del lines[i]
+        else:
+            lines[i] = ln * int(rng.integers(2, 6))
+    path = sys.argv[2] + "/f%d.pdb" % it
+    open(path, "wb").write(b"\n".join(lines))
+    nm, nb = ctypes.c_int(), ctypes.c_int()
+    if L.rsx_pdb_count(path.encode(), ctypes.byref(nm), ctypes.byref(nb)) != 0:
+        continue
+    out = np.zeros((max(nb.value, 1), 4), np.float32)
+    sizes = np.zeros(max(nm.value, 1), np.int32)
+    st = L.rsx_pdb_read(path.encode(), 0, out.reshape(-1), nb.value, sizes, nm.value)
+    assert st != 0 or sizes[: nm.value].sum() == nb.value, path
+print("ok")
+'''
+    r = subprocess.run([sys.executable, "-c", code, os.path.join(GOLD, "synthetic_a.pdb"),
+                        str(tmp_path)], capture_output=True, text=True,
+                       cwd=ROOT, timeout=300)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stderr[-2000:]
