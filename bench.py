@@ -1,10 +1,10 @@
 """Benchmark of the Debye hot path on GB300 (one JSON line on rank 0).
 
-Workload (the configuration the headline metric is quoted on): the full Debye
-forward I(q) of N = 20,000 bodies, 5 types, 201 q on [0, 0.5] 1/A (a compact
-seeded random-walk chain, Rg ~ 25 A).  One step = one full forward of that
-structure.  The unit of work is one pair*q term f_i f_j sinc(q r_ij) over the
-N(N-1)/2 unordered pairs.
+Workload (the largest configuration that fits one GPU): the full Debye forward
+I(q) of N = 200,000 bodies, a random-walk chain folded into a 60 A sphere,
+8 types (Z in {1,6,7,8,15,16,26,30}, f_t(q) = Z_t exp(-b_t q^2)), 512 q on
+[0, 1.0] 1/A.  One step = one full forward of that structure: N(N-1)/2 x 512
+= 1.024e13 pair*q terms f_i f_j sinc(q r_ij).
 
 * ``value``   : pair*q/s with the bodies resident in HBM (kernels only), timed
                 with CUDA events on librsx's stream; L2 is flushed (a 256 MB
@@ -17,15 +17,21 @@ N(N-1)/2 unordered pairs.
                 rate measured on this GPU (rsx_measure_fp32_fma_rate).  The
                 bound of a direct evaluation (one SFU sine per pair*q, 16 per
                 clock per SM = FMA rate / 8) is reported beside it.
-* ``cpu_baseline``: the reference's host_debye<double,float> loop (port in
+* ``cpu_baseline``: the reference's host_debye<double,float> loop (the port in
                 oracle/, bit-identical to the compiled original on x86) on the
-                host cores, on a bounded q sample, extrapolated to all q.
-* ``extras``  : the other configurations' figures (incremental steps, SASA,
-                forward+adjoint, precision, batching) when their paths exist.
+                host cores over a bounded sample of the same workload: every
+                sample is a set of rows of the lower triangle (all x < y for
+                each sampled row y) over all 512 q.  The reference cannot run
+                this structure whole: its N x N double matrix would take
+                320 GB and is indexed with int (N <= 46,340).
+* ``extras``  : the other configurations' figures (the N = 20,000 forward,
+                incremental steps, SASA, forward+adjoint, batching).
 
 With --gpus N under torchrun every rank computes its own independently seeded
 structure (weak scaling, no collective); value = all ranks' pair*q / max time.
-``--impl reference`` times the reference CPU path on the same config instead.
+``--impl reference`` times the reference CPU path on the same workload
+instead: every step is one row sample as above, every step timed; it also
+runs one whole, un-extrapolated forward of the N = 20,000, 201-q structure.
 """
 from __future__ import annotations
 
@@ -43,8 +49,21 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
-METRIC = "Debye Gpair·q/s (full forward, N=20000, Q=201)"
-UNIT = "Gpair·q/s"
+METRIC = "Debye Gpair\u00b7q/s & % FP32/SFU peak; fwd+adjoint vs plain fwd time at 1e-5 rel err"
+UNIT = "Gpair\u00b7q/s"
+HEADLINE = 4          # N = 200,000, 512 q
+REF_ROWS = 32         # rows of the lower triangle per reference sample
+
+
+def headline_config(w):
+    """The ``config`` object both arms print (identical keys and values)."""
+    from resaxs_gb300 import workloads as W
+    return {"workload": W.CONFIG_NAMES[HEADLINE], "n_bodies": w.n, "n_q": len(w.q),
+            "n_types": int(w.ff.shape[1]), "q_range": [float(w.q[0]), float(w.q[-1])],
+            "structure": "random-walk chain folded into a 60 A sphere",
+            "pair_q_per_step": w.pair_q,
+            "l2": "GPU arm: flushed between timed steps by a 256 MB write outside the "
+                  "events (the inputs, 3.2 MB, are L2-resident); CPU arm: not applicable"}
 
 
 def parse():
@@ -123,25 +142,59 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline_forward(w, threads: int, q_sample: int | None = None):
-    """The reference host_debye<double,float> loop (oracle port) on a q sample:
-    full distance matrix + `q_sample` q values split over the threads; the
-    per-q cost is extrapolated to every q (the reference's cost is linear in Q
-    after the matrix)."""
+def ref_rows(n: int, n_rows: int, sample: int) -> np.ndarray:
+    """Rows of the lower triangle timed in reference sample ``sample``: spread
+    evenly over [1, n), shifted per sample so that the samples visit
+    different rows.  Row y holds the y pairs (x, y), x < y."""
+    base = np.linspace(1, n - 1, n_rows)
+    shift = (sample * 7919) % max(1, (n - 1) // n_rows)
+    return np.clip(np.round(base + shift), 1, n - 1).astype(np.int32)
+
+
+def cpu_sample(w, threads: int, sample: int, n_rows: int = REF_ROWS):
+    """One timed sample of the reference host_debye<double,float> loop (port
+    in oracle/) on ``w``: the distance rows and the q loop of ``n_rows`` rows
+    over every q, the q loop split over ``threads``.  Returns (pair*q, s)."""
     from oracle import oracle
-    threads = threads or os.cpu_count() or 1
-    if q_sample is None:
-        q_sample = max(threads, 2)
-    sel = np.linspace(0, len(w.q) - 1, q_sample).round().astype(int)
+    rows = ref_rows(w.n, n_rows, sample)
     t0 = time.perf_counter()
-    _, t_matrix = oracle.refport_host_debye(w.q[sel], w.bodies, w.ff[sel], threads=threads)
-    t_total = time.perf_counter() - t0
-    t_q = (t_total - t_matrix) / q_sample
-    t_full = t_matrix + t_q * len(w.q)
-    return {"value": w.pair_q / t_full / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"host_debye<double,float> port (N x N distance matrix + q loop) on "
-                      f"{q_sample} of {len(w.q)} q, {threads} threads; matrix {t_matrix:.2f} s, "
-                      f"{t_q:.2f} s per q, extrapolated to all q = {t_full:.1f} s per forward"}
+    oracle.refport_host_debye_rows(w.q, w.bodies, w.ff, rows, threads=threads)
+    dt = time.perf_counter() - t0
+    return int(rows.astype(np.int64).sum()) * len(w.q), dt
+
+
+def cpu_baseline_forward(w, threads: int, samples: int = 4):
+    """The reference CPU path on a bounded sample of the headline workload
+    (``samples`` row samples; about 10 s on 16 cores)."""
+    threads = threads or os.cpu_count() or 1
+    pq = t = 0.0
+    for s in range(samples):
+        a, b = cpu_sample(w, threads, 1000 + s)
+        pq += a
+        t += b
+    v = pq / t / 1e9
+    return {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"host_debye<double,float> port over {samples} samples of {REF_ROWS} rows "
+                      f"of the lower triangle (all x < y of each row, all {len(w.q)} q): "
+                      f"{pq:.3e} pair*q in {t:.2f} s on {threads} threads",
+            "seconds": t, "pair_q_timed": pq,
+            "extrapolated_full_forward_s": w.pair_q / (v * 1e9)}
+
+
+def cpu_full_forward_n20000(threads: int):
+    """One whole, un-extrapolated host_debye<double,float> port forward of the
+    N = 20,000, 201-q structure (its N x N matrix is 3.2 GB), q loop split
+    over ``threads``."""
+    from oracle import oracle
+    from resaxs_gb300 import workloads as W
+    w = W.make_config(2, seed=0)
+    t0 = time.perf_counter()
+    _, t_matrix = oracle.refport_host_debye(w.q, w.bodies, w.ff, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"workload": W.CONFIG_NAMES[2], "n_bodies": w.n, "n_q": len(w.q),
+            "pair_q": w.pair_q, "seconds": dt, "matrix_s": t_matrix,
+            "value": w.pair_q / dt / 1e9, "unit": UNIT, "cores": threads,
+            "what": "whole forward, every q, no extrapolation"}
 
 
 def cpu_baseline_sasa(threads: int):
@@ -166,26 +219,32 @@ def run_reference(args):
     if rank != 0:
         return 0
     from resaxs_gb300 import workloads as W
-    w = W.make_config(2, seed=0)
+    w = W.make_config(HEADLINE, seed=0)
     threads = args.cpu_threads or os.cpu_count() or 1
-    # each step is a bounded sample (~3 s on 16 cores); at most 10 timed
-    # steps and 1 warm-up keep the run within a few minutes
-    steps, warmup = min(args.steps, 10), min(args.warmup, 1)
-    vals = []
-    for s in range(warmup + steps):
-        cb = cpu_baseline_forward(w, threads, q_sample=threads)
-        if s >= warmup:
-            vals.append(cb["value"])
-    v = statistics.median(vals)
-    cb["value"] = v
+    pq = t = 0.0
+    for s in range(args.warmup + args.steps):
+        a, b = cpu_sample(w, threads, s)
+        if s >= args.warmup:
+            pq += a
+            t += b
+    v = pq / t / 1e9
+    cb = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+          "sample": f"every step: host_debye<double,float> port over {REF_ROWS} rows of the "
+                    f"lower triangle (all x < y of each row, all {len(w.q)} q), {threads} "
+                    f"threads; {pq:.3e} pair*q timed in {t:.2f} s over {args.steps} steps"}
     line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": world,
-            "steps": steps, "warmup": warmup,
-            "ms_per_step": w.pair_q / (v * 1e9) * 1e3, "higher_is_better": True,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t / max(args.steps, 1) * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": W.CONFIG_NAMES[2], "n_bodies": w.n, "n_q": len(w.q),
-                       "n_types": w.ff.shape[1], "l2": "n/a (CPU)"},
+            "config": headline_config(w),
             "cpu_baseline": cb,
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "pair_q_per_timed_step": pq / max(args.steps, 1),
+            "extrapolated": {"full_forward_s": w.pair_q / (v * 1e9),
+                             "how": "the headline structure's N(N-1)/2 x 512 pair*q at the "
+                                    "timed rate; not run (320 GB matrix, int-indexed)"}}
+    if not args.no_extras:
+        line["full_forward_n20000_q201"] = cpu_full_forward_n20000(threads)
     print(json.dumps(line), flush=True)
     return 0
 
@@ -204,7 +263,7 @@ def main():
     from resaxs_gb300 import workloads as W
     from resaxs_gb300.saxs import Debye
 
-    w = W.make_config(2, seed=rank)
+    w = W.make_config(HEADLINE, seed=rank)
     d = Debye(w.q, w.ff, w.n, device=local, timing=True)
     d.calc(w.bodies)                      # upload + first result
     stream = torch.cuda.ExternalStream(_lib.lib().rsx_debye_stream(d.handle),
@@ -272,7 +331,7 @@ def main():
         sfu_peak = fma.value / 8.0 / 1e9  # one SFU sine per pair*q: 16 per clock per SM
         k_ms = statistics.median(kernel_ms)
         achieved = w.pair_q / (k_ms * 1e-3) / 1e9
-        prof = os.path.join(ROOT, "profiles", "debye_forward_traffic.json")
+        prof = os.path.join(ROOT, "profiles", "debye_forward_traffic_n200000_q512.json")
         traffic = None
         if os.path.exists(prof):
             traffic = json.load(open(prof)).get("dram_bytes_per_launch")
@@ -282,12 +341,10 @@ def main():
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": W.CONFIG_NAMES[2], "n_bodies": w.n, "n_q": len(w.q),
-                       "n_types": w.ff.shape[1], "pair_q_per_step": w.pair_q,
-                       "l2": "flushed between steps (256 MB write, outside the timed events)",
-                       "q_slab": cfg["q_slab"], "work_items": cfg["n_items"],
-                       "uniform_q_recurrence": cfg["uniform_q"],
-                       "wall_s_timed_loop": t_wall},
+            "config": headline_config(w),
+            "run": {"q_slab": cfg["q_slab"], "work_items": cfg["n_items"],
+                    "uniform_q_recurrence": cfg["uniform_q"], "wall_s_timed_loop": t_wall,
+                    "kernel_launches_per_step": launches / max(args.steps, 1)},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak,
                          "unit": UNIT, "frac": achieved / peak, "traffic": traffic,
                          "kernel_ms": k_ms,
@@ -302,7 +359,7 @@ def main():
         }
         threads = args.cpu_threads or os.cpu_count() or 1
         try:
-            line["cpu_baseline"] = cpu_baseline_forward(w, threads, q_sample=threads)
+            line["cpu_baseline"] = cpu_baseline_forward(w, threads)
             if not args.no_extras:
                 line["cpu_baseline"]["sasa"] = cpu_baseline_sasa(threads)
         except Exception as e:  # report, do not hide

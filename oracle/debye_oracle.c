@@ -727,3 +727,92 @@ double orc_refport_host_debye_mt(const float *v_q, int n_q, const float *v_bodie
     free(r);
     return t_matrix;
 }
+
+/* ---- the same loop over a sample of rows of the lower triangle ---------- */
+
+typedef struct {
+    const float *v_q;
+    int k0, k1, n, n_rows;
+    const int *rows;
+    const double *r;       /* [n_rows][n]: row y's distances to x < y */
+    const float *factors;  /* [n_q][n] */
+    double *out;           /* [n_q] */
+} rows_arg;
+
+/* host_debye.cpp:74-104 for the rows y in `rows` only: the inner sum over
+ * x < y, multiplied by F_q(y) and added to the partial, in the order and
+ * mixed float/double arithmetic of the reference (auto terms and the final
+ * "2 * Iq + auto" belong to the whole curve and are left out). */
+static void *rows_worker(void *p)
+{
+    rows_arg *a = (rows_arg *)p;
+    for (int k = a->k0; k < a->k1; k++) {
+        double q = a->v_q[k];
+        double Iq = 0;
+        const float *Fq = &a->factors[(size_t)k * a->n];
+        for (int s = 0; s < a->n_rows; s++) {
+            const int y = a->rows[s];
+            const double *ry = &a->r[(size_t)s * a->n];
+            double Fqy = Fq[y];
+            double inner_sum = 0;
+            for (int x = 0; x < y; x++) {
+                double v1 = 1;
+                if (q != 0) {
+                    double qr = q * ry[x];
+                    v1 = sin(qr) / qr;
+                }
+                inner_sum += Fq[x] * v1;
+            }
+            Iq += inner_sum * Fqy;
+        }
+        a->out[k] = Iq;
+    }
+    return NULL;
+}
+
+int orc_refport_host_debye_rows(const float *v_q, int n_q, const float *v_bodies,
+                                int n_bodies, const float *t_factors, int n_factors,
+                                const int *rows, int n_rows, double *out_partial,
+                                int n_threads)
+{
+    for (int s = 0; s < n_rows; s++)
+        if (rows[s] < 0 || rows[s] >= n_bodies)
+            return -1;
+    int nt = pick_threads(n_threads);
+    if (nt > n_q)
+        nt = n_q;
+    /* the distance rows, as host_debye.cpp:58-61 fills its matrix */
+    double *r = (double *)malloc(sizeof(double) * (size_t)n_rows * (n_bodies > 0 ? n_bodies : 1));
+    float *factors = port_factors(v_bodies, n_bodies, n_q, t_factors, n_factors);
+    if (!r || !factors) {
+        free(r);
+        free(factors);
+        return -2;
+    }
+    for (int s = 0; s < n_rows; s++) {
+        const int y = rows[s];
+        for (int x = 0; x < y; x++)
+            r[(size_t)s * n_bodies + x] = port_distance(&v_bodies[4 * x], &v_bodies[4 * y]);
+    }
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nt);
+    rows_arg *args = (rows_arg *)malloc(sizeof(rows_arg) * nt);
+    for (int t = 0; t < nt; ++t) {
+        args[t].v_q = v_q;
+        args[t].k0 = (int)((long)n_q * t / nt);
+        args[t].k1 = (int)((long)n_q * (t + 1) / nt);
+        args[t].n = n_bodies;
+        args[t].n_rows = n_rows;
+        args[t].rows = rows;
+        args[t].r = r;
+        args[t].factors = factors;
+        args[t].out = out_partial;
+        pthread_create(&th[t], NULL, rows_worker, &args[t]);
+    }
+    for (int t = 0; t < nt; ++t)
+        pthread_join(th[t], NULL);
+    free(th);
+    free(args);
+    free(factors);
+    free(r);
+    return 0;
+}

@@ -67,6 +67,10 @@ def lib():
         L.orc_refport_host_debye.argtypes = [_f32p, i, _f32p, i, _f32p, i, _f32p]
         L.orc_refport_host_debye_mt.argtypes = [_f32p, i, _f32p, i, _f32p, i, _f32p, i]
         L.orc_refport_host_debye_mt.restype = d
+        _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+        L.orc_refport_host_debye_rows.argtypes = [_f32p, i, _f32p, i, _f32p, i, _i32p, i,
+                                                  _f64p, i]
+        L.orc_refport_host_debye_rows.restype = i
         L.orc_sasa_counts.argtypes = [_f32p, _f32p, i, _f32p, i, ctypes.c_float, _u32p, i, i]
         L.orc_fibonacci_unit_dots.argtypes = [i, _f32p]
         _lib = L
@@ -154,6 +158,22 @@ def refport_host_debye(q, bodies, ff, threads=1):
     t = lib().orc_refport_host_debye_mt(q, len(q), bodies.reshape(-1), len(bodies),
                                         ff.reshape(-1), ff.shape[1], out, int(threads))
     return out, t
+
+
+def refport_host_debye_rows(q, bodies, ff, rows, threads=0):
+    """host_debye<double,float> port over the rows ``rows`` of the lower
+    triangle only: returns the FP64 partial sum per q (see rsx_oracle.h)."""
+    q = _c(q, np.float32)
+    bodies = _c(bodies, np.float32)
+    ff = _c(ff, np.float32)
+    rows = _c(rows, np.int32)
+    out = np.zeros(len(q), np.float64)
+    rc = lib().orc_refport_host_debye_rows(q, len(q), bodies.reshape(-1), len(bodies),
+                                           ff.reshape(-1), ff.shape[1], rows, len(rows), out,
+                                           int(threads))
+    if rc != 0:
+        raise ValueError(f"orc_refport_host_debye_rows failed ({rc})")
+    return out
 
 
 def sasa_counts(atoms, radii, unit_dots, probe, use_cells=True, threads=0):

@@ -72,6 +72,20 @@ double orc_refport_host_debye_mt(const float *v_q, int n_q, const float *v_bodie
                                  int n_bodies, const float *t_factors,
                                  int n_factors, float *out_v_iq, int n_threads);
 
+/* The loop of orc_refport_host_debye_mt restricted to the rows `rows` of the
+ * lower triangle (host_debye.cpp:74-104 for y in rows, x < y): out_partial[k]
+ * = sum over those rows of F_q(y) * sum_{x<y} F_q(x) sinc(q r_xy), in the
+ * reference's order and mixed float/double arithmetic, with the distance
+ * rows built as host_debye.cpp:58-61 builds its matrix.  The q loop is split
+ * over n_threads.  This times the reference's CPU path on a bounded sample of
+ * a structure whose N x N matrix does not fit in memory (host_debye indexes
+ * that matrix with int, so it cannot run past N = 46,340 at all).  Returns 0,
+ * -1 for a row index outside [0, n_bodies), -2 when allocation fails. */
+int orc_refport_host_debye_rows(const float *v_q, int n_q, const float *v_bodies,
+                                int n_bodies, const float *t_factors, int n_factors,
+                                const int *rows, int n_rows, double *out_partial,
+                                int n_threads);
+
 /* Strict-FP32 dot-sphere SASA counts: restates the occlusion test of
  * calc_rsasa (resaxslib/src/rsasa_dot_spheres.cl:94-163):
  *   ext_i = r_i + P;  dot = unit_k * ext_i;  sdot = dot + p_i     (per component)

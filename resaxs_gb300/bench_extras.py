@@ -1,9 +1,9 @@
 """Secondary measurements of bench.py: one entry per benchmark configuration
 besides the headline forward (incremental recalc + SASA, forward+adjoint,
-precision, batching).  Every figure is a librsx timing on the GPU.  Parity of
-these paths (drift of the running curve, SASA counts, per-q error at 200,000
-bodies) is established by the GPU tests against the FP64 oracle
-(tests/test_precision_gpu.py, tests/test_sasa_gpu.py, tests/test_recalc_gpu.py);
+the N = 20,000 forward, batching).  Every figure is a librsx timing on the
+GPU.  Parity of these paths (drift of the running curve, SASA counts, per-q
+error) is established by the GPU tests against the FP64 oracle
+(tests/test_debye_gpu.py, tests/test_sasa_gpu.py, tests/test_recalc_gpu.py);
 the drift figure below compares the running curve with a fresh GPU calculation."""
 from __future__ import annotations
 
@@ -118,23 +118,31 @@ def adjoint(device: int):
             "grad_finite": bool(np.all(np.isfinite(g)))}
 
 
-def precision(device: int):
-    """Config 4: N=200,000 in a 60 A sphere, 8 types, Q=512 on [0,1]."""
+def forward_n20000(device: int, reps: int = 10):
+    """Config 2's full forward (N = 20,000 compact chain, 5 types, 201 q on
+    [0, 0.5]): pair kernels timed with CUDA events, median of ``reps``."""
     from . import workloads as W
     from .saxs import Debye
-    w = W.make_config(4, seed=0)
+    w = W.make_config(2, seed=0)
     with Debye(w.q, w.ff, w.n, device=device, timing=True) as d:
         d.calc(w.bodies)
+        for _ in range(3):
+            d.forward_resident()
+            d.sync()
         ms = []
-        for _ in range(2):
+        for _ in range(reps):
             d.forward_resident()
             d.sync()
             ms.append(d.timing()[0])
-    k_ms = min(ms)
-    return {"workload": "N=200000 Q=512 T=8", "forward_kernel_ms": k_ms,
-            "gpairq_per_s": w.pair_q / (k_ms * 1e-3) / 1e9,
-            "parity": "per-q relative error vs the FP64 oracle on a uniform q subset "
-                      "(tests/test_precision_gpu.py)"}
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            d.calc(w.bodies)
+        api_ms = (time.perf_counter() - t0) / reps * 1e3
+        cfg = d.config()
+    k_ms = statistics.median(ms)
+    return {"workload": W.CONFIG_NAMES[2], "pair_q": w.pair_q, "forward_kernel_ms": k_ms,
+            "gpairq_per_s": w.pair_q / (k_ms * 1e-3) / 1e9, "api_ms": api_ms,
+            "api_gpairq_per_s": w.pair_q / (api_ms * 1e-3) / 1e9, "config": cfg}
 
 
 def _batching(device: int, n_members: int, n_lo: int, n_hi: int, seed: int = 0):
@@ -197,8 +205,8 @@ def batching(device: int):
 
 def run_all(device: int):
     out = {}
-    for name, fn in (("recalc", recalc), ("sasa", sasa), ("adjoint", adjoint),
-                     ("precision", precision), ("batching", batching)):
+    for name, fn in (("forward_n20000_q201", forward_n20000), ("recalc", recalc),
+                     ("sasa", sasa), ("adjoint", adjoint), ("batching", batching)):
         t0 = time.perf_counter()
         try:
             out[name] = fn(device)
