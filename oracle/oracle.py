@@ -4,8 +4,9 @@ Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import
 this module.  The product library (``resaxs_gb300``) never does.
 
 ``liboracle.so`` is the C restatement in this folder (debye_oracle.c,
-sasa_oracle.c); ``_ref/libref_host_debye.so`` is the reference's own
-``host_debye.cpp`` compiled by ``build_ref.sh`` where the reference tree exists.
+sasa_oracle.c); ``_ref/libref_host_debye.so`` holds the reference's own CPU
+code (host_debye, the PDB reader, the dot generators and the CPU SASA),
+compiled by ``build_ref.sh`` from the reference tree where it exists.
 """
 from __future__ import annotations
 
@@ -22,13 +23,15 @@ REF_PATH = os.path.join(HERE, "_ref", "libref_host_debye.so")
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 _u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 
 
 def build(cc: str = "gcc") -> str:
     """Compile liboracle.so from the C restatement (seconds)."""
     objs = []
     for src, extra in (("debye_oracle.c", ["-O3", "-fno-math-errno"]),
-                       ("sasa_oracle.c", ["-ffp-contract=off"])):
+                       ("sasa_oracle.c", ["-ffp-contract=off"]),
+                       ("rsasa_cpu_port.c", ["-ffp-contract=off"])):
         obj = os.path.join(HERE, src.replace(".c", ".o"))
         subprocess.check_call([cc, "-O2", "-fPIC", "-std=c11", "-D_GNU_SOURCE", *extra,
                                "-c", os.path.join(HERE, src), "-o", obj])
@@ -39,9 +42,11 @@ def build(cc: str = "gcc") -> str:
     return LIB_PATH
 
 
-def build_ref(reference_root: str = "/root/reference") -> str | None:
-    """Compile the reference's host_debye.cpp into _ref/ when the tree exists."""
-    if not os.path.isfile(os.path.join(reference_root, "resaxslib", "src", "host_debye.cpp")):
+def build_ref(reference_root: str) -> str | None:
+    """Compile the reference's CPU sources into _ref/ when ``reference_root``
+    holds the reference tree (None otherwise)."""
+    if not reference_root or not os.path.isfile(
+            os.path.join(reference_root, "resaxslib", "src", "host_debye.cpp")):
         return None
     subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), reference_root])
     return REF_PATH
@@ -67,12 +72,18 @@ def lib():
         L.orc_refport_host_debye.argtypes = [_f32p, i, _f32p, i, _f32p, i, _f32p]
         L.orc_refport_host_debye_mt.argtypes = [_f32p, i, _f32p, i, _f32p, i, _f32p, i]
         L.orc_refport_host_debye_mt.restype = d
-        _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
         L.orc_refport_host_debye_rows.argtypes = [_f32p, i, _f32p, i, _f32p, i, _i32p, i,
                                                   _f64p, i]
         L.orc_refport_host_debye_rows.restype = i
         L.orc_sasa_counts.argtypes = [_f32p, _f32p, i, _f32p, i, ctypes.c_float, _u32p, i, i]
         L.orc_fibonacci_unit_dots.argtypes = [i, _f32p]
+        f = ctypes.c_float
+        L.orc_sasa_counts_typed.argtypes = [_f32p, i, _f32p, i, _f32p, i, f, _u32p, i]
+        L.orc_sasa_counts_typed.restype = i
+        L.orc_refport_rsasa_typed.argtypes = [_f32p, i, _f32p, i, _f32p, _i32p, f, _f32p, i]
+        L.orc_refport_rsasa_typed.restype = i
+        L.orc_refport_rsasa_unit.argtypes = [_f32p, i, _f32p, _f32p, i, f, _u32p, i]
+        L.orc_refport_rsasa_unit.restype = i
         _lib = L
     return _lib
 
@@ -86,8 +97,45 @@ def ref_lib():
         L.ref_host_debye_df.argtypes = [_f32p, i, _f32p, i, _f32p, i, _f32p]
         L.ref_host_debye_ff.argtypes = [_f32p, i, _f32p, i, _f32p, i, _f32p]
         L.ref_host_debye_dd.argtypes = [_f64p, i, _f64p, i, _f64p, i, _f64p]
+        if hasattr(L, "ref_sasa_dots"):
+            f = ctypes.c_float
+            L.ref_sasa_dots.argtypes = [i, f, f, f, _f32p, i]
+            L.ref_sasa_dots.restype = i
+            L.ref_rsasa_cpu.argtypes = [_f32p, i, f, f, _f32p]
+            L.ref_rsasa_cpu.restype = i
         _ref = L
     return _ref
+
+
+SASA_DOT_KINDS = {"latitude": 0, "32": 1, "fibonacci": 2, "dodecahedron": 3, "dodeca_icosa": 4}
+
+
+def ref_sasa_dots(kind: str, radius: float, dot_density: float, probe: float) -> np.ndarray:
+    """The reference's dot sphere of one type ((n, 4) float32: x, y, z and the
+    radius in w), from the compiled dot_spheres_params generators."""
+    L = ref_lib()
+    if L is None or not hasattr(L, "ref_sasa_dots"):
+        raise RuntimeError("the compiled reference (oracle/_ref) is not available")
+    out = np.zeros((8192, 4), np.float32)
+    n = L.ref_sasa_dots(SASA_DOT_KINDS[kind], float(radius), float(dot_density), float(probe),
+                        out, len(out))
+    if n < 0:
+        raise ValueError(f"ref_sasa_dots failed ({n})")
+    return out[:n].copy()
+
+
+def ref_rsasa_cpu(atoms, dot_density: float, probe: float) -> np.ndarray:
+    """The reference's CPU SASA (rsasa_cpu_alg<float,float>::calc_rsasa):
+    rsasa per atom of float4 bodies with type bits in .w."""
+    L = ref_lib()
+    if L is None or not hasattr(L, "ref_rsasa_cpu"):
+        raise RuntimeError("the compiled reference (oracle/_ref) is not available")
+    atoms = _c(atoms, np.float32)
+    out = np.zeros(len(atoms), np.float32)
+    rc = L.ref_rsasa_cpu(atoms.reshape(-1), len(atoms), float(dot_density), float(probe), out)
+    if rc != 0:
+        raise ValueError(f"ref_rsasa_cpu failed ({rc})")
+    return out
 
 
 def _c(a, dt):
@@ -184,6 +232,55 @@ def sasa_counts(atoms, radii, unit_dots, probe, use_cells=True, threads=0):
     lib().orc_sasa_counts(atoms.reshape(-1), radii, len(atoms), unit_dots.reshape(-1),
                           len(unit_dots), ctypes.c_float(probe), counts, int(bool(use_cells)),
                           int(threads))
+    return counts
+
+
+def sasa_counts_typed(atoms, type_radii, dot_map, probe, threads=0):
+    """Exact counts with pre-scaled per-type dots (dot_map: (n_types, stride,
+    4) float32, non-finite x = padding); see rsx_oracle.h."""
+    atoms = _c(atoms, np.float32)
+    type_radii = _c(type_radii, np.float32)
+    dot_map = _c(dot_map, np.float32)
+    n_types, stride = dot_map.shape[0], dot_map.shape[1]
+    counts = np.zeros(len(atoms), np.uint32)
+    rc = lib().orc_sasa_counts_typed(atoms.reshape(-1), len(atoms), type_radii, n_types,
+                                     dot_map.reshape(-1), stride, ctypes.c_float(probe), counts,
+                                     int(threads))
+    if rc != 0:
+        raise ValueError(f"orc_sasa_counts_typed failed ({rc})")
+    return counts
+
+
+def refport_rsasa_typed(atoms, type_radii, dot_sets, probe, threads=0):
+    """Port of the reference CPU SASA with per-type dot sets (a list of (n_t,
+    4) arrays, one per type): rsasa per atom."""
+    atoms = _c(atoms, np.float32)
+    type_radii = _c(type_radii, np.float32)
+    start = np.zeros(len(dot_sets) + 1, np.int32)
+    start[1:] = np.cumsum([len(d) for d in dot_sets])
+    dots = _c(np.concatenate([np.asarray(d, np.float32).reshape(-1, 4) for d in dot_sets]),
+              np.float32)
+    out = np.zeros(len(atoms), np.float32)
+    rc = lib().orc_refport_rsasa_typed(atoms.reshape(-1), len(atoms), type_radii, len(dot_sets),
+                                       dots.reshape(-1), start, ctypes.c_float(probe), out,
+                                       int(threads))
+    if rc != 0:
+        raise ValueError(f"orc_refport_rsasa_typed failed ({rc})")
+    return out
+
+
+def refport_rsasa_unit(atoms, radii, unit_dots, probe, threads=0):
+    """Port of the reference CPU SASA with per-atom radii and unit dots scaled
+    by r_i + P: accessible-dot counts per atom."""
+    atoms = _c(atoms, np.float32)
+    radii = _c(radii, np.float32)
+    unit_dots = _c(unit_dots, np.float32)
+    counts = np.zeros(len(atoms), np.uint32)
+    rc = lib().orc_refport_rsasa_unit(atoms.reshape(-1), len(atoms), radii,
+                                      unit_dots.reshape(-1), len(unit_dots),
+                                      ctypes.c_float(probe), counts, int(threads))
+    if rc != 0:
+        raise ValueError(f"orc_refport_rsasa_unit failed ({rc})")
     return counts
 
 

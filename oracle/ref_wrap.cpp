@@ -4,6 +4,8 @@
 // Test infrastructure only: the product never loads it.
 #include "host_debye.hpp"
 
+#include <memory>
+
 extern "C" void ref_host_debye_df(const float *q, int n_q, const float *bodies, int n_bodies,
                                   const float *ff, int n_factors, float *out)
 {
@@ -74,6 +76,69 @@ extern "C" int ref_parse_pdb(const char *path, float *out, int cap_bodies, int *
             }
         }
         return (int)models.size();
+    } catch (...) {
+        return -1;
+    }
+}
+
+// Dot-sphere SASA of the reference (resaxslib/src/rsasa_algorithm.cpp:60-208,
+// resaxslib/src/rsasa_cpu_alg.cpp:33-185), compiled from those unmodified
+// files together with the OpenCL SASA class their factory instantiates
+// (never called here; see shim/CL/cl.hpp).
+#include "rsasa_algorithm.hpp"
+
+namespace {
+typedef resaxs::algorithm::rsasa<float, float> rsasa_ff;
+}
+
+// One type's dot sphere as dot_spheres_params generates it for a body of
+// `radius`: kind 0 = create_dots (latitude rings, the CPU algorithm's set,
+// rsasa_algorithm.cpp:60-89), 1 = create_32_dots, 2 = create_fibonacci_dots
+// (:96-116), 3 = create_dodecahedron_dots, 4 = create_dodeca_icosa_dots
+// (:156-208, the OpenCL algorithm's set).  out_xyzw receives the dots as
+// x, y, z, w (w = radius, as the reference stores it); returns the number of
+// dots, or -1 for a bad kind, -2 when cap is too small.
+extern "C" int ref_sasa_dots(int kind, float radius, float dot_density, float probe,
+                             float *out_xyzw, int cap)
+{
+    rsasa_ff::dot_spheres_params p(dot_density, probe);
+    std::vector<cl_float4> d;
+    switch (kind) {
+    case 0: d = p.create_dots(radius); break;
+    case 1: d = p.create_32_dots(radius); break;
+    case 2: d = p.create_fibonacci_dots(radius); break;
+    case 3: d = p.create_dodecahedron_dots(radius); break;
+    case 4: d = p.create_dodeca_icosa_dots(radius); break;
+    default: return -1;
+    }
+    if ((int)d.size() > cap)
+        return -2;
+    for (size_t i = 0; i < d.size(); ++i)
+        std::memcpy(out_xyzw + 4 * i, d[i].s, 16);
+    return (int)d.size();
+}
+
+// rsasa_cpu_alg<float,float> through the reference's own factory and
+// interface: rsasa<float>::create<algorithm>(rsasa_dot_spheres), initialize
+// with dot_spheres_params(dot_density, probe), calc_rsasa.  atoms are float4
+// bodies with the type index bits in .w; out_rsasa[i] = accessible dots /
+// dots of atom i's type.  Returns 0, or the resaxs::error code on failure.
+extern "C" int ref_rsasa_cpu(const float *atoms, int n_atoms, float dot_density, float probe,
+                             float *out_rsasa)
+{
+    try {
+        std::unique_ptr<resaxs::algorithm::i_rsasa<float, float, resaxs::algorithm::algorithm>> alg(
+            rsasa_ff::create<resaxs::algorithm::algorithm>(resaxs::algorithm::rsasa_dot_spheres));
+        rsasa_ff::dot_spheres_params p(dot_density, probe);
+        alg->initialize(&p);
+        std::vector<cl_float4> a((size_t)n_atoms);
+        std::memcpy(a.data(), atoms, 16 * (size_t)n_atoms);
+        std::vector<float> r((size_t)n_atoms);
+        alg->calc_rsasa(a, r);
+        std::memcpy(out_rsasa, r.data(), sizeof(float) * (size_t)n_atoms);
+        return 0;
+    } catch (const resaxs::error &e) {
+        return e.err() != 0 ? e.err() : -1;
     } catch (...) {
         return -1;
     }

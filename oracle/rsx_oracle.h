@@ -99,6 +99,35 @@ void orc_sasa_counts(const float *atoms, const float *radii, int n_atoms,
                      const float *unit_dots, int n_dots, float probe,
                      unsigned *counts, int use_cells, int n_threads);
 
+/* The same occlusion test with pre-scaled dots per atom type, the layout of
+ * the reference's OpenCL dot map (rsasa_cl_gpu_alg.cpp:59-89): dot k of an
+ * atom of type t is dot_map[4*(t*stride + k) + 0..2] (x, y, z; w unused), a
+ * dot whose x is not finite is padding and never counts; atom radii come
+ * from type_radii[t].  dot = d + p_i (per component, FP32); occluded iff
+ * (P + r_b)^2 - |dot - p_b|^2 > 1e-4f as above.  Exact (cell list sized by
+ * the largest dot distance).  Returns 0, or -1 for a type index >= n_types
+ * or a non-finite position. */
+int orc_sasa_counts_typed(const float *atoms, int n_atoms, const float *type_radii,
+                          int n_types, const float *dot_map, int stride, float probe,
+                          unsigned *counts, int n_threads);
+
+/* Port of rsasa_cpu_alg<float,float>::calc_rsasa (rsasa_cpu_alg.cpp:112-185)
+ * with its 6 A voxel grid (bb_grid.hpp:130-266), in FP32 without
+ * contraction, bit-identical to the compiled reference on x86; its neighbour
+ * prune assumes radii <= 1.5 A (max_radius) as the reference's does.  Typed
+ * form: radii and pre-scaled dot sets per type as the reference builds them
+ * (type_radii[t]; dots_xyzw[4*k], k in [dot_start[t], dot_start[t+1]) for
+ * type t); out_rsasa[i] = accessible / dots of the type.  Unit form: per-atom
+ * radii, dot k of atom i at unit_k * (r_i + P), out_counts[i] = accessible
+ * dots.  Atoms are split over n_threads (the reference runs one thread).
+ * Return 0, -1 for a type index >= n_types, -2 when allocation fails. */
+int orc_refport_rsasa_typed(const float *atoms, int n_atoms, const float *type_radii,
+                            int n_types, const float *dots_xyzw, const int *dot_start,
+                            float probe, float *out_rsasa, int n_threads);
+int orc_refport_rsasa_unit(const float *atoms, int n_atoms, const float *radii,
+                           const float *unit_dots, int n_dots, float probe,
+                           unsigned *out_counts, int n_threads);
+
 /* Fibonacci unit dots as generated by create_fibonacci_dots
  * (resaxslib/src/rsasa_algorithm.cpp:96-116) with n = n_dots / 2 (n_dots
  * even) and ext_radius = 1: out is [n_dots][3] FP32, bit-for-bit the unit

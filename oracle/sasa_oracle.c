@@ -207,3 +207,171 @@ void orc_sasa_counts(const float *atoms, const float *radii, int n_atoms,
     free(J.cell_items);
     pthread_mutex_destroy(&J.mu);
 }
+
+/* ---- typed dot maps: pre-scaled dots per atom type ---------------------- */
+
+typedef struct {
+    const float *atoms, *type_radii, *dot_map;
+    int n, n_types, stride;
+    float probe;
+    const float *reach;    /* per atom: max |dot| of its type + P + margin */
+    unsigned *counts;
+    float lo[3], cell;
+    int dims[3];
+    int *cell_start, *cell_items;
+    float rmax;
+    int next;
+    pthread_mutex_t mu;
+} typed_job;
+
+static unsigned atom_type(const float *atoms, int i)
+{
+    unsigned t;
+    memcpy(&t, &atoms[4 * i + 3], 4);
+    return t;
+}
+
+static void typed_cell_of(const typed_job *J, const float *p, int c[3])
+{
+    for (int a = 0; a < 3; ++a) {
+        int v = (int)floorf((p[a] - J->lo[a]) / J->cell);
+        if (v < 0)
+            v = 0;
+        if (v >= J->dims[a])
+            v = J->dims[a] - 1;
+        c[a] = v;
+    }
+}
+
+static void *typed_worker(void *arg)
+{
+    typed_job *J = (typed_job *)arg;
+    int *nb = (int *)malloc(sizeof(int) * (size_t)(J->n > 0 ? J->n : 1));
+    for (;;) {
+        pthread_mutex_lock(&J->mu);
+        const int i = J->next++;
+        pthread_mutex_unlock(&J->mu);
+        if (i >= J->n)
+            break;
+        const float *pi = &J->atoms[4 * i];
+        int n_nb = 0, c[3];
+        typed_cell_of(J, pi, c);
+        for (int x = c[0] - 1; x <= c[0] + 1; ++x)
+            for (int y = c[1] - 1; y <= c[1] + 1; ++y)
+                for (int z = c[2] - 1; z <= c[2] + 1; ++z) {
+                    if (x < 0 || y < 0 || z < 0 || x >= J->dims[0] || y >= J->dims[1] ||
+                        z >= J->dims[2])
+                        continue;
+                    const int cid = (x * J->dims[1] + y) * J->dims[2] + z;
+                    for (int s = J->cell_start[cid]; s < J->cell_start[cid + 1]; ++s)
+                        nb[n_nb++] = J->cell_items[s];
+                }
+        const unsigned t = atom_type(J->atoms, i);
+        const float *dots = &J->dot_map[4 * (size_t)t * J->stride];
+        unsigned cnt = 0;
+        for (int k = 0; k < J->stride; ++k) {
+            if (!isfinite(dots[4 * k]))
+                continue; /* padding: not a dot */
+            float sd[3];
+            for (int a = 0; a < 3; ++a)
+                sd[a] = dots[4 * k + a] + pi[a];
+            int occ = 0;
+            for (int s = 0; s < n_nb && !occ; ++s) {
+                const int b = nb[s];
+                occ = occluded(sd, &J->atoms[4 * b],
+                               J->type_radii[atom_type(J->atoms, b)], J->probe);
+            }
+            cnt += occ ? 0u : 1u;
+        }
+        J->counts[i] = cnt;
+    }
+    free(nb);
+    return NULL;
+}
+
+int orc_sasa_counts_typed(const float *atoms, int n_atoms, const float *type_radii,
+                          int n_types, const float *dot_map, int stride, float probe,
+                          unsigned *counts, int n_threads)
+{
+    if (n_atoms <= 0)
+        return 0;
+    typed_job J;
+    memset(&J, 0, sizeof J);
+    J.atoms = atoms;
+    J.type_radii = type_radii;
+    J.dot_map = dot_map;
+    J.n = n_atoms;
+    J.n_types = n_types;
+    J.stride = stride;
+    J.probe = probe;
+    J.counts = counts;
+    /* largest dot distance over the types, largest radius over the atoms */
+    float ext = 0.0f, hi[3], rmax = 0.0f;
+    for (int t = 0; t < n_types; ++t)
+        for (int k = 0; k < stride; ++k) {
+            const float *d = &dot_map[4 * ((size_t)t * stride + k)];
+            if (!isfinite(d[0]))
+                continue;
+            const double r = sqrt((double)d[0] * d[0] + (double)d[1] * d[1] + (double)d[2] * d[2]);
+            if (r > ext)
+                ext = (float)r;
+        }
+    float amax = 0.0f;
+    for (int a = 0; a < 3; ++a)
+        J.lo[a] = hi[a] = atoms[a];
+    for (int i = 0; i < n_atoms; ++i) {
+        const unsigned t = atom_type(atoms, i);
+        if ((int)t >= n_types)
+            return -1;
+        for (int a = 0; a < 3; ++a) {
+            const float v = atoms[4 * i + a];
+            if (!isfinite(v))
+                return -1;
+            if (v < J.lo[a])
+                J.lo[a] = v;
+            if (v > hi[a])
+                hi[a] = v;
+            if (fabsf(v) > amax)
+                amax = fabsf(v);
+        }
+        if (type_radii[t] > rmax)
+            rmax = type_radii[t];
+    }
+    /* an occluder b of a dot of atom i lies within |dot| + P + r_b of atom i
+     * (plus the rounding of the dot's position) */
+    J.cell = ext + probe + rmax + 0.01f + 8e-6f * amax;
+    long total = 1;
+    for (int a = 0; a < 3; ++a) {
+        J.dims[a] = (int)floorf((hi[a] - J.lo[a]) / J.cell) + 1;
+        total *= J.dims[a];
+    }
+    J.cell_start = (int *)calloc((size_t)total + 1, sizeof(int));
+    J.cell_items = (int *)malloc(sizeof(int) * (size_t)n_atoms);
+    int *cid = (int *)malloc(sizeof(int) * (size_t)n_atoms);
+    for (int i = 0; i < n_atoms; ++i) {
+        int c[3];
+        typed_cell_of(&J, &atoms[4 * i], c);
+        cid[i] = (c[0] * J.dims[1] + c[1]) * J.dims[2] + c[2];
+        J.cell_start[cid[i] + 1]++;
+    }
+    for (long c = 0; c < total; ++c)
+        J.cell_start[c + 1] += J.cell_start[c];
+    int *fill = (int *)malloc(sizeof(int) * (size_t)total);
+    memcpy(fill, J.cell_start, sizeof(int) * (size_t)total);
+    for (int i = 0; i < n_atoms; ++i)
+        J.cell_items[fill[cid[i]]++] = i;
+    free(fill);
+    free(cid);
+    pthread_mutex_init(&J.mu, NULL);
+    const int nt = pick_threads(n_threads);
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nt);
+    for (int t = 0; t < nt; ++t)
+        pthread_create(&th[t], NULL, typed_worker, &J);
+    for (int t = 0; t < nt; ++t)
+        pthread_join(th[t], NULL);
+    free(th);
+    free(J.cell_start);
+    free(J.cell_items);
+    pthread_mutex_destroy(&J.mu);
+    return 0;
+}

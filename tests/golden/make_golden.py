@@ -1,8 +1,8 @@
 """Regenerates the golden fixtures in this folder from the reference tree.
 
-Run in a container that has the reference sources (default /root/reference):
+Run in a container that has the reference sources:
 
-    python tests/golden/make_golden.py [reference_root]
+    python tests/golden/make_golden.py <reference_root>
 
 Outputs (committed, so that tests on machines without the reference tree
 can use them):
@@ -25,8 +25,19 @@ can use them):
   bodies the reference's own parse_pdb<float>::all_models_as_complex_atoms
   (resaxslib/src/parse_pdb.cpp, compiled into oracle/_ref) reads from them.
 
-``python tests/golden/make_golden.py [reference_root] --only pdb`` rewrites
-only the PDB fixtures.
+* ``sasa_ref.npz`` -- the reference's dot-sphere SASA: the 16 atom-type radii
+  of atomic_form_factors::calc_radii, the dot sets its dot_spheres_params
+  generators make for each type radius (create_dots at 5 dots/A^2 and probe
+  1.4 A -- the CPU algorithm's set; create_dodeca_icosa_dots at probe 1.8 A --
+  the OpenCL algorithm's set; create_fibonacci_dots, create_32_dots and
+  create_dodecahedron_dots at 1.4 A), and the rsasa of the reference's own
+  rsasa_cpu_alg<float,float>::calc_rsasa (rsasa_cpu_alg.cpp, compiled into
+  oracle/_ref) on three seeded structures: ``a`` uses only the types whose
+  radius is <= 1.5 A (there the reference's max_radius neighbour prune is
+  exact), ``b`` all 16 types, ``c`` a free (spread) chain.
+
+``python tests/golden/make_golden.py <reference_root> --only pdb`` (or
+``--only sasa``) rewrites only those fixtures.
 """
 from __future__ import annotations
 
@@ -107,10 +118,53 @@ def make_pdb_fixtures():
                         nonl_bodies=fb, nonl_sizes=sb)
 
 
-def main(ref_root="/root/reference", only=None):
+SASA_DENSITY = 5.0
+SASA_PROBE = 1.4
+SASA_TYPES_EXACT = (0, 2, 3, 4, 6, 10, 11)   # calc_radii <= 1.5 A
+
+
+def sasa_structure(name):
+    """The seeded structures of sasa_ref.npz: (atoms float4 with type bits)."""
+    import math
+    if name == "a":
+        n, rng, pool = 3000, np.random.default_rng(31), SASA_TYPES_EXACT
+        xyz = W.confined_chain(n, rng, 25.0 * (n / 20000) ** (1 / 3) * math.sqrt(5 / 3))
+    elif name == "b":
+        n, rng, pool = 2000, np.random.default_rng(32), tuple(range(16))
+        xyz = W.confined_chain(n, rng, 25.0 * (n / 20000) ** (1 / 3) * math.sqrt(5 / 3))
+    else:
+        n, rng, pool = 1500, np.random.default_rng(33), SASA_TYPES_EXACT
+        xyz = W.random_walk_chain(n, rng) + np.array([250.0, -40.0, 1000.0])
+    types = rng.choice(np.array(pool), n).astype(np.uint32)
+    return W.pack_bodies(xyz, types)
+
+
+def make_sasa_fixtures():
+    radii = np.load(os.path.join(HERE, "ff_ref.npz"))["radii"]
+    out = {"radii": radii, "density": np.float32(SASA_DENSITY), "probe": np.float32(SASA_PROBE)}
+    for kind, probe in (("latitude", SASA_PROBE), ("dodeca_icosa", 1.8), ("fibonacci", SASA_PROBE),
+                        ("32", SASA_PROBE), ("dodecahedron", SASA_PROBE)):
+        sets = [oracle.ref_sasa_dots(kind, r, SASA_DENSITY, probe) for r in radii]
+        out[f"dots_{kind}"] = np.concatenate(sets)
+        out[f"dots_{kind}_start"] = np.concatenate([[0], np.cumsum([len(d) for d in sets])]
+                                                  ).astype(np.int32)
+        out[f"dots_{kind}_probe"] = np.float32(probe)
+    for name in ("a", "b", "c"):
+        atoms = sasa_structure(name)
+        out[f"{name}_atoms"] = atoms
+        out[f"{name}_rsasa_ref"] = oracle.ref_rsasa_cpu(atoms, SASA_DENSITY, SASA_PROBE)
+    np.savez_compressed(os.path.join(HERE, "sasa_ref.npz"), **out)
+
+
+def main(ref_root=None, only=None):
+    ref_root = ref_root or os.environ.get("RESAXS_REFERENCE_ROOT")
     oracle.build()
     if oracle.build_ref(ref_root) is None:
-        raise SystemExit(f"reference tree not found at {ref_root}")
+        raise SystemExit(f"reference tree not found at {ref_root!r}")
+    if only in (None, "sasa"):
+        make_sasa_fixtures()
+    if only == "sasa":
+        return
     make_pdb_fixtures()
     if only == "pdb":
         return
