@@ -295,23 +295,45 @@ rsx_status rsx_sasa_fibonacci_dots(int n_dots, float *out_xyz);
 rsx_status rsx_sasa_dodeca_icosa_dots(float *out_xyz);
 
 /* rsasa_cl_gpu::initialize(dot_spheres_cl_params) (rsasa_cl_gpu_alg.cpp:38-57):
- * atom count, unit dot set (n_dots <= 4096) and probe radius fixed per handle. */
+ * atom count, unit dot set (n_dots <= 4096, finite) and probe radius fixed
+ * per handle.  Dot k of atom i sits at p_i + unit_k * (r_i + P). */
 rsx_status rsx_sasa_create(int n_atoms, const float *unit_dots, int n_dots, float probe,
                            int device, rsx_sasa **out);
+/* The reference's own dot layout: rsasa_cl_gpu::create_sphere_dots
+ * (rsasa_cl_gpu_alg.cpp:59-89) builds dots_map_[type * 32 + dot] from
+ * pre-scaled per-type dot spheres padded with -inf dots, and
+ * rsasa_cpu_alg::create_sphere_dots (rsasa_cpu_alg.cpp:46-61) keeps one
+ * pre-scaled set per type.  dot_map holds n_types x stride dots as x, y, z,
+ * w (w unused); a dot whose x is not finite is padding.  Dot k of an atom of
+ * type t sits at p_i + dot_map[t][k] (FP32 add, rsasa_dot_spheres.cl:108-110),
+ * and atom radii are type_radii[t] (rsasa_cl_gpu_alg.cpp:140-151).
+ * n_types <= 256, stride <= 4096. */
+rsx_status rsx_sasa_create_typed(int n_atoms, const float *dot_map, int n_types, int stride,
+                                 const float *type_radii, float probe, int device,
+                                 rsx_sasa **out);
 rsx_status rsx_sasa_destroy(rsx_sasa *h);
 
 /* Accessible-dot counts per atom (the uint buffer of do_recalc_rsasa,
- * rsasa_cl_gpu_alg.cpp:177-197): dot k of atom i sits at p_i + unit_k * (r_i + P)
- * and is occluded by atom b when (P + r_b)^2 - |dot - p_b|^2 > 1e-4, each
- * operation rounded to FP32 without contraction.  radii are per atom. */
+ * rsasa_cl_gpu_alg.cpp:177-197): a dot is occluded by atom b when
+ * (P + r_b)^2 - |dot - p_b|^2 > 1e-4, each operation rounded to FP32 without
+ * contraction; every atom, the dot's own included, is tested.  Unit-dot
+ * handles; radii are per atom. */
 rsx_status rsx_sasa_counts(rsx_sasa *h, const rsx_body *atoms, const float *radii,
                            unsigned *out_counts);
 
 /* i_rsasa::calc_rsasa / recalc_rsasa: rsasa_i = count_i / n_dots
- * (rsasa_cl_gpu_alg.cpp:153-197). */
+ * (rsasa_cl_gpu_alg.cpp:153-197).  Unit-dot handles. */
 rsx_status rsx_sasa_calc(rsx_sasa *h, const rsx_body *atoms, const float *radii, float *out_rsasa);
 
-/* Occlusion tests performed and kernel milliseconds of the last call. */
+/* The same for typed handles: atoms carry their type in .w; rsasa_i =
+ * count_i / dots of the atom's type (rsasa_cl_gpu_alg.cpp:189-196,
+ * rsasa_cpu_alg.cpp:181).  A type index >= n_types is RSX_INVALID_ARG. */
+rsx_status rsx_sasa_counts_typed(rsx_sasa *h, const rsx_body *atoms, unsigned *out_counts);
+rsx_status rsx_sasa_calc_typed(rsx_sasa *h, const rsx_body *atoms, float *out_rsasa);
+
+/* Occlusion tests to the first occluder (in the order the kernel visits the
+ * candidates) and GPU milliseconds (cell list + occlusion pass) of the last
+ * call. */
 rsx_status rsx_sasa_stats(rsx_sasa *h, unsigned long long *tests, float *ms_kernel);
 
 /* Batched ensembles (no reference counterpart: the reference evaluates an

@@ -111,6 +111,10 @@ SIGNATURES = [
     ("rsx_sasa_fibonacci_dots", _st, [_i, _f32p]),
     ("rsx_sasa_dodeca_icosa_dots", _st, [_f32p]),
     ("rsx_sasa_create", _st, [_i, _f32p, _i, ctypes.c_float, _i, ctypes.POINTER(_vp)]),
+    ("rsx_sasa_create_typed", _st, [_i, _f32p, _i, _i, _f32p, ctypes.c_float, _i,
+                               ctypes.POINTER(_vp)]),
+    ("rsx_sasa_counts_typed", _st, [_vp, _f32p, _u32p]),
+    ("rsx_sasa_calc_typed", _st, [_vp, _f32p, _f32p]),
     ("rsx_sasa_destroy", _st, [_vp]),
     ("rsx_sasa_counts", _st, [_vp, _f32p, _f32p, _u32p]),
     ("rsx_sasa_calc", _st, [_vp, _f32p, _f32p, _f32p]),

@@ -79,7 +79,8 @@ def sasa(device: int):
             "kernel_ms": k_ms, "occlusion_tests": int(tests),
             "gtests_per_s": tests / (k_ms * 1e-3) / 1e9, "dots_per_s": w.n * 960 / (k_ms * 1e-3),
             "exposed_dots": int(c.sum()),
-            "parity": "bit-exact counts vs the strict-FP32 oracle (tests/test_sasa_gpu.py)"}
+            "parity": "bit-exact counts vs the strict-FP32 oracle, and vs the reference's own "
+                      "CPU SASA on its dot sets (tests/test_sasa_gpu.py)"}
 
 
 def adjoint(device: int):

@@ -1,13 +1,21 @@
 // Dot-sphere SASA handle behind the C ABI: replaces rsasa_cl_gpu<float,float>
-// (resaxslib/src/rsasa_cl_gpu_alg.cpp) -- host cell list, one H2D copy per
-// call, counts back.  Dot sets are generated here from the reference's
-// formulas (resaxslib/src/rsasa_algorithm.cpp).
+// (resaxslib/src/rsasa_cl_gpu_alg.cpp) and rsasa_cpu_alg<float,float>
+// (resaxslib/src/rsasa_cpu_alg.cpp).  Two forms:
+//  * unit: one set of unit directions, dot = unit * (r_i + P), radii per atom;
+//  * typed: the reference's own layout, pre-scaled dots per atom type with
+//    padding (dots_map_[type * stride + dot], rsasa_cl_gpu_alg.cpp:59-89) and
+//    radii per type.
+// Per call: one pass over the atoms on the host (checks, bounding box), one
+// H2D copy, the cell list and the occlusion pass on the GPU, counts back.
+// Dot sets are generated here from the reference's formulas
+// (resaxslib/src/rsasa_algorithm.cpp).
 #include "rsx_host.h"
 #include "rsx_sasa_internal.h"
 
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <numeric>
 #include <vector>
 
 using namespace rsx;
@@ -16,12 +24,23 @@ struct rsx_sasa {
     int device = -1;
     cudaStream_t st = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    int n = 0, n_dots = 0;
+    int n = 0;
+    bool typed = false;
+    int n_types = 1, n_dots = 0; // n_dots: unit form
     float probe = 0.f;
-    std::vector<float> unit;
-    float *d_unit = nullptr;
-    unsigned char *d_buf = nullptr, *h_buf = nullptr;
-    size_t buf_cap = 0;
+    float unit_reach = 0.f;
+    std::vector<float> type_radius, dot_reach;
+    std::vector<int> dots_of_type; // accessible-dot denominator per type (typed form)
+    float4 *d_dots = nullptr;
+    int *d_group_base = nullptr, *d_group_count = nullptr;
+    float *d_dot_reach = nullptr, *d_type_radius = nullptr;
+    // per-call buffers
+    unsigned char *d_in = nullptr, *h_in = nullptr; // atoms float4 [n] | radii [n]
+    float4 *d_atoms = nullptr;
+    int *d_cell_of = nullptr, *d_rank_of = nullptr, *d_orig = nullptr, *d_type_of = nullptr;
+    int *d_cell_sorted = nullptr;
+    int *d_cell_count = nullptr, *d_cell_start = nullptr;
+    size_t cells_cap = 0;
     unsigned *d_counts = nullptr, *h_counts = nullptr;
     unsigned long long *d_tests = nullptr, *h_tests = nullptr;
     float last_ms = 0.f;
@@ -37,11 +56,14 @@ rsx_status sasa_release(rsx_sasa *h)
     DeviceGuard g(h->device);
     if (h->st)
         cudaStreamSynchronize(h->st);
-    dev_free(h->d_unit);
-    dev_free(h->d_buf);
-    dev_free(h->d_counts);
-    dev_free(h->d_tests);
-    host_free_pinned(h->h_buf);
+    for (void *p : {(void *)h->d_dots, (void *)h->d_group_base, (void *)h->d_group_count,
+                    (void *)h->d_dot_reach, (void *)h->d_type_radius, (void *)h->d_in,
+                    (void *)h->d_atoms, (void *)h->d_cell_of, (void *)h->d_rank_of,
+                    (void *)h->d_orig, (void *)h->d_type_of, (void *)h->d_cell_sorted,
+                    (void *)h->d_cell_count,
+                    (void *)h->d_cell_start, (void *)h->d_counts, (void *)h->d_tests})
+        dev_free(p);
+    host_free_pinned(h->h_in);
     host_free_pinned(h->h_counts);
     host_free_pinned(h->h_tests);
     if (h->e0)
@@ -54,94 +76,257 @@ rsx_status sasa_release(rsx_sasa *h)
     return RSX_OK;
 }
 
-// Cell list of the atoms on the host, packed into the pinned buffer:
-// atoms (float4 x,y,z,r) | cell coords (int3) | caller index | cell starts.
-rsx_status pack_cells(rsx_sasa *h, const rsx_body *atoms, const float *radii, SasaArgs &a,
-                      size_t &bytes_out)
+// Orders idx[b, e) so that every run of 32 dots is compact on the sphere:
+// halves along the axis of largest extent, cut at a multiple of 32.  The
+// counts do not depend on the order; the lanes of a warp then tend to meet
+// their first occluder together.
+void compact_groups(const std::vector<float4> &d, std::vector<int> &idx, int b, int e)
+{
+    const int n = e - b;
+    if (n <= 32)
+        return;
+    float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+    for (int k = b; k < e; ++k) {
+        const float v[3] = {d[idx[k]].x, d[idx[k]].y, d[idx[k]].z};
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], v[a]);
+            hi[a] = std::max(hi[a], v[a]);
+        }
+    }
+    int ax = 0;
+    for (int a = 1; a < 3; ++a)
+        if (hi[a] - lo[a] > hi[ax] - lo[ax])
+            ax = a;
+    const int groups = (n + 31) / 32;
+    const int cut = b + 32 * ((groups + 1) / 2);
+    auto key = [&](int k) { return ax == 0 ? d[k].x : (ax == 1 ? d[k].y : d[k].z); };
+    std::nth_element(idx.begin() + b, idx.begin() + cut, idx.begin() + e,
+                     [&](int p, int q) { return key(p) < key(q) || (key(p) == key(q) && p < q); });
+    compact_groups(d, idx, b, cut);
+    compact_groups(d, idx, cut, e);
+}
+
+// Appends one dot set as 32-dot groups (x not finite: padding) to `table`;
+// returns the number of groups and the largest |d| of its fully finite dots.
+int append_groups(const std::vector<float4> &set, std::vector<float4> &table, float *reach)
+{
+    std::vector<int> idx(set.size());
+    std::iota(idx.begin(), idx.end(), 0);
+    // dots with a non-finite y or z can never be occluded: they go last
+    auto finite3 = [&](int k) {
+        return std::isfinite(set[k].y) && std::isfinite(set[k].z);
+    };
+    const auto mid = std::stable_partition(idx.begin(), idx.end(), finite3);
+    compact_groups(set, idx, 0, (int)(mid - idx.begin()));
+    double r = 0.0;
+    for (auto it = idx.begin(); it != mid; ++it) {
+        const float4 &v = set[*it];
+        r = std::max(r, std::sqrt((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z));
+    }
+    *reach = (float)(r * (1.0 + 1e-6));
+    const int groups = ((int)set.size() + 31) / 32;
+    const float nan = std::nanf("");
+    for (int k = 0; k < groups * 32; ++k)
+        table.push_back(k < (int)set.size() ? set[idx[k]] : make_float4(nan, 0.f, 0.f, 0.f));
+    return groups;
+}
+
+rsx_status upload_dots(rsx_sasa *h, const std::vector<float4> &table,
+                       const std::vector<int> &base, const std::vector<int> &count)
+{
+    RSX_TRY(dev_alloc((void **)&h->d_dots, sizeof(float4) * std::max<size_t>(table.size(), 1),
+                      "sasa dots"));
+    RSX_TRY(dev_alloc((void **)&h->d_group_base, sizeof(int) * base.size(), "sasa groups"));
+    RSX_TRY(dev_alloc((void **)&h->d_group_count, sizeof(int) * count.size(), "sasa groups"));
+    RSX_TRY(dev_alloc((void **)&h->d_dot_reach, sizeof(float) * h->dot_reach.size(), "sasa reach"));
+    RSX_TRY(dev_alloc((void **)&h->d_type_radius, sizeof(float) * h->type_radius.size(),
+                      "sasa radii"));
+    const cudaMemcpyKind k = cudaMemcpyHostToDevice;
+    cudaError_t e = cudaMemcpyAsync(h->d_dots, table.data(), sizeof(float4) * table.size(), k, h->st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h->d_group_base, base.data(), sizeof(int) * base.size(), k, h->st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h->d_group_count, count.data(), sizeof(int) * count.size(), k, h->st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h->d_dot_reach, h->dot_reach.data(), sizeof(float) * h->dot_reach.size(),
+                            k, h->st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h->d_type_radius, h->type_radius.data(),
+                            sizeof(float) * h->type_radius.size(), k, h->st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(h->st); // the host vectors are temporaries
+    return cuda_status(e, "upload dots");
+}
+
+rsx_status new_handle(int n_atoms, float probe, int device, rsx_sasa **out)
+{
+    int dev = -1;
+    RSX_TRY(select_device(device, &dev));
+    DeviceGuard g(dev);
+    RSX_TRY_CUDA(cudaSetDevice(dev), "cudaSetDevice");
+    rsx_sasa *h = new rsx_sasa();
+    h->device = dev;
+    h->n = n_atoms;
+    h->probe = probe;
+    cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&h->e0);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&h->e1);
+    rsx_status s = cuda_status(e, "sasa stream/events");
+    const size_t n1 = (size_t)std::max(n_atoms, 1);
+    if (s == RSX_OK)
+        s = dev_alloc((void **)&h->d_in, (sizeof(float4) + sizeof(float)) * n1, "sasa atoms");
+    if (s == RSX_OK)
+        s = host_alloc_pinned((void **)&h->h_in, (sizeof(float4) + sizeof(float)) * n1,
+                              "sasa staging");
+    if (s == RSX_OK)
+        s = dev_alloc((void **)&h->d_atoms, sizeof(float4) * n1, "sasa cell atoms");
+    for (int **p : {&h->d_cell_of, &h->d_rank_of, &h->d_orig, &h->d_type_of, &h->d_cell_sorted})
+        if (s == RSX_OK)
+            s = dev_alloc((void **)p, sizeof(int) * n1, "sasa cell index");
+    if (s == RSX_OK)
+        s = dev_alloc((void **)&h->d_counts, sizeof(unsigned) * n1, "counts");
+    if (s == RSX_OK)
+        s = dev_alloc((void **)&h->d_tests, sizeof(unsigned long long), "tests");
+    if (s == RSX_OK)
+        s = host_alloc_pinned((void **)&h->h_counts, sizeof(unsigned) * n1, "pinned counts");
+    if (s == RSX_OK)
+        s = host_alloc_pinned((void **)&h->h_tests, sizeof(unsigned long long), "pinned tests");
+    if (s != RSX_OK) {
+        sasa_release(h);
+        return s;
+    }
+    *out = h;
+    return RSX_OK;
+}
+
+// Checks the atoms, stages them, builds the cell list and runs the occlusion
+// pass; counts land in h->h_counts.
+rsx_status run(rsx_sasa *h, const rsx_body *atoms, const float *radii)
 {
     const int n = h->n;
-    float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0}, rmax = 0.f;
+    // the staging buffer may still feed the previous call's copy
+    RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "sasa staging");
+    float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0}, amax = 0.f, rmax = 0.f, dmax = 0.f;
+    std::vector<char> present(h->typed ? h->n_types : 0, 0);
     for (int i = 0; i < n; ++i) {
         const float p[3] = {atoms[i].x, atoms[i].y, atoms[i].z};
         if (!std::isfinite(p[0]) || !std::isfinite(p[1]) || !std::isfinite(p[2]))
             return fail(RSX_INVALID_ARG, "atom " + std::to_string(i) + " has a non-finite position");
-        if (!(radii[i] >= 0.f) || !std::isfinite(radii[i]))
-            return fail(RSX_INVALID_ARG, "atom " + std::to_string(i) + " has an invalid radius");
+        if (h->typed) {
+            unsigned t;
+            std::memcpy(&t, &atoms[i].w, 4);
+            if (t >= (unsigned)h->n_types)
+                return fail(RSX_INVALID_ARG, "atom " + std::to_string(i) + " has type " +
+                                                 std::to_string(t) + " outside the dot map");
+            present[t] = 1;
+        } else {
+            if (!(radii[i] >= 0.f) || !std::isfinite(radii[i]))
+                return fail(RSX_INVALID_ARG, "atom " + std::to_string(i) + " has an invalid radius");
+            rmax = std::max(rmax, radii[i]);
+        }
         for (int c = 0; c < 3; ++c) {
             if (i == 0 || p[c] < lo[c])
                 lo[c] = p[c];
             if (i == 0 || p[c] > hi[c])
                 hi[c] = p[c];
+            amax = std::max(amax, std::fabs(p[c]));
         }
-        rmax = std::max(rmax, radii[i]);
     }
-    // a dot of atom i can only be occluded by an atom within r_i + r_b + 2P
-    double cell = 2.0 * rmax + 2.0 * h->probe + 0.02;
+    if (h->typed) {
+        for (int t = 0; t < h->n_types; ++t)
+            if (present[t]) {
+                rmax = std::max(rmax, h->type_radius[t]);
+                dmax = std::max(dmax, h->dot_reach[t]);
+            }
+    } else {
+        dmax = (rmax + h->probe) * h->unit_reach;
+    }
+    // an occluder of a dot of atom i lies within |d| + P + r_b of it; the
+    // kernel's reach adds `margin` for the rounding of the dot's position
+    const float margin = 0.01f + 8e-6f * amax;
+    double cell = ((double)dmax * 1.000001 + h->probe + rmax + margin) * 1.001 + 1e-3;
     int dims[3];
     for (;;) {
         double total = 1.0;
         for (int c = 0; c < 3; ++c) {
-            dims[c] = (int)std::floor((hi[c] - lo[c]) / cell) + 1;
+            dims[c] = (int)std::floor(((double)hi[c] - lo[c]) / cell) + 1;
             total *= dims[c];
         }
         if (total <= 4.0 * n + 4096.0)
             break;
         cell *= 1.5; // sparse, wide boxes: fewer, larger cells (still exact)
     }
-    const int n_cells = dims[0] * dims[1] * dims[2];
-    const size_t off_cell = sizeof(float4) * (size_t)n;
-    const size_t off_orig = off_cell + sizeof(int) * 3 * (size_t)n;
-    const size_t off_start = off_orig + sizeof(int) * (size_t)n;
-    const size_t bytes = off_start + sizeof(int) * (size_t)(n_cells + 1);
-    if (bytes > h->buf_cap) {
-        dev_free(h->d_buf);
-        host_free_pinned(h->h_buf);
-        h->d_buf = h->h_buf = nullptr;
-        h->buf_cap = 0;
-        const size_t cap = bytes + bytes / 4 + 4096;
-        RSX_TRY(dev_alloc((void **)&h->d_buf, cap, "sasa cells"));
-        RSX_TRY(host_alloc_pinned((void **)&h->h_buf, cap, "sasa staging"));
-        h->buf_cap = cap;
+    const size_t n_cells = (size_t)dims[0] * dims[1] * dims[2];
+    if (n_cells + 1 > h->cells_cap) {
+        dev_free(h->d_cell_count);
+        dev_free(h->d_cell_start);
+        h->d_cell_count = h->d_cell_start = nullptr;
+        h->cells_cap = 0;
+        const size_t cap = n_cells + n_cells / 4 + 1024;
+        RSX_TRY(dev_alloc((void **)&h->d_cell_count, sizeof(int) * cap, "sasa cells"));
+        RSX_TRY(dev_alloc((void **)&h->d_cell_start, sizeof(int) * cap, "sasa cells"));
+        h->cells_cap = cap;
     }
-    // the staging buffer may still feed the previous call's copy
-    RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "sasa staging");
-    std::vector<int> cid(n), ccoord(3 * (size_t)n);
-    int *start = reinterpret_cast<int *>(h->h_buf + off_start);
-    std::memset(start, 0, sizeof(int) * (n_cells + 1));
-    for (int i = 0; i < n; ++i) {
-        const float p[3] = {atoms[i].x, atoms[i].y, atoms[i].z};
-        int c3[3];
-        for (int c = 0; c < 3; ++c) {
-            int v = (int)std::floor((p[c] - lo[c]) / cell);
-            c3[c] = std::min(std::max(v, 0), dims[c] - 1);
-            ccoord[3 * (size_t)i + c] = c3[c];
-        }
-        cid[i] = (c3[0] * dims[1] + c3[1]) * dims[2] + c3[2];
-        start[cid[i] + 1]++;
+    std::memcpy(h->h_in, atoms, sizeof(float4) * (size_t)n);
+    size_t bytes = sizeof(float4) * (size_t)n;
+    if (!h->typed) {
+        std::memcpy(h->h_in + bytes, radii, sizeof(float) * (size_t)n);
+        bytes += sizeof(float) * (size_t)n;
     }
-    for (int c = 0; c < n_cells; ++c)
-        start[c + 1] += start[c];
-    std::vector<int> fill(start, start + n_cells);
-    float4 *pa = reinterpret_cast<float4 *>(h->h_buf);
-    int *pc = reinterpret_cast<int *>(h->h_buf + off_cell);
-    int *po = reinterpret_cast<int *>(h->h_buf + off_orig);
-    for (int i = 0; i < n; ++i) {
-        const int s = fill[cid[i]]++;
-        pa[s] = make_float4(atoms[i].x, atoms[i].y, atoms[i].z, radii[i]);
-        pc[3 * s + 0] = ccoord[3 * (size_t)i + 0];
-        pc[3 * s + 1] = ccoord[3 * (size_t)i + 1];
-        pc[3 * s + 2] = ccoord[3 * (size_t)i + 2];
-        po[s] = i;
+    SasaCellArgs c{};
+    c.atoms_in = reinterpret_cast<const float4 *>(h->d_in);
+    c.radii_in = h->typed ? nullptr : reinterpret_cast<const float *>(h->d_in + sizeof(float4) * n);
+    c.type_radius = h->d_type_radius;
+    c.cell_count = h->d_cell_count;
+    c.cell_start = h->d_cell_start;
+    c.cell_of = h->d_cell_of;
+    c.rank_of = h->d_rank_of;
+    c.atoms = h->d_atoms;
+    c.orig_index = h->d_orig;
+    c.type_of = h->d_type_of;
+    c.cell_sorted = h->d_cell_sorted;
+    c.n_atoms = n;
+    c.n_cells = (int)n_cells;
+    SasaArgs a{};
+    a.atoms = h->d_atoms;
+    a.orig_index = h->d_orig;
+    a.type_of = h->typed ? h->d_type_of : nullptr;
+    a.cell_id = h->d_cell_sorted;
+    a.cell_start = h->d_cell_start;
+    a.dots = h->d_dots;
+    a.group_base = h->d_group_base;
+    a.group_count = h->d_group_count;
+    a.dot_reach = h->d_dot_reach;
+    a.unit_reach = h->unit_reach;
+    a.typed = h->typed ? 1 : 0;
+    a.counts = h->d_counts;
+    a.tests = h->d_tests;
+    a.n_atoms = n;
+    a.probe = h->probe;
+    a.margin = margin;
+    for (int k = 0; k < 3; ++k) {
+        c.dims[k] = a.dims[k] = dims[k];
+        c.lo[k] = a.lo[k] = lo[k];
     }
-    a.atoms = reinterpret_cast<const float4 *>(h->d_buf);
-    a.cell_of = reinterpret_cast<const int *>(h->d_buf + off_cell);
-    a.orig_index = reinterpret_cast<const int *>(h->d_buf + off_orig);
-    a.cell_start = reinterpret_cast<const int *>(h->d_buf + off_start);
-    a.dims[0] = dims[0];
-    a.dims[1] = dims[1];
-    a.dims[2] = dims[2];
-    a.max_radius = rmax;
-    bytes_out = bytes;
+    c.inv_cell = a.inv_cell = 1.0 / cell;
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->d_in, h->h_in, bytes, cudaMemcpyHostToDevice, h->st),
+                 "upload atoms");
+    RSX_TRY_CUDA(cudaMemsetAsync(h->d_tests, 0, sizeof(unsigned long long), h->st), "zero tests");
+    RSX_TRY_CUDA(cudaEventRecord(h->e0, h->st), "event");
+    RSX_LAUNCH(launch_sasa_cells(c, h->st), "sasa cell list");
+    RSX_LAUNCH(launch_sasa(a, h->st), "sasa kernel");
+    RSX_TRY_CUDA(cudaEventRecord(h->e1, h->st), "event");
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->h_counts, h->d_counts, sizeof(unsigned) * n,
+                                 cudaMemcpyDeviceToHost, h->st),
+                 "read counts");
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->h_tests, h->d_tests, sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost, h->st),
+                 "read tests");
+    RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "sasa");
+    cudaEventElapsedTime(&h->last_ms, h->e0, h->e1);
+    h->last_tests = *h->h_tests;
     return RSX_OK;
 }
 
@@ -201,50 +386,75 @@ rsx_status rsx_sasa_create(int n_atoms, const float *unit_dots, int n_dots, floa
     if (!out)
         return fail(RSX_INVALID_ARG, "out handle pointer is null");
     *out = nullptr;
-    if (n_atoms < 0 || !unit_dots || n_dots <= 0 || n_dots > 4096 || !(probe >= 0.f) ||
-        !std::isfinite(probe))
+    if (n_atoms < 0 || !unit_dots || n_dots <= 0 || n_dots > 32 * kSasaMaxGroups ||
+        !(probe >= 0.f) || !std::isfinite(probe))
         return fail(RSX_INVALID_ARG, "need n_atoms >= 0, 1..4096 unit dots and probe >= 0");
-    int dev = -1;
-    RSX_TRY(select_device(device, &dev));
-    DeviceGuard g(dev);
-    cudaSetDevice(dev);
-    rsx_sasa *h = new rsx_sasa();
-    h->device = dev;
-    h->n = n_atoms;
+    std::vector<float4> set((size_t)n_dots);
+    for (int k = 0; k < n_dots; ++k) {
+        set[k] = make_float4(unit_dots[3 * k], unit_dots[3 * k + 1], unit_dots[3 * k + 2], 0.f);
+        if (!std::isfinite(set[k].x) || !std::isfinite(set[k].y) || !std::isfinite(set[k].z))
+            return fail(RSX_INVALID_ARG, "unit dot " + std::to_string(k) + " is not finite");
+    }
+    rsx_sasa *h = nullptr;
+    RSX_TRY(new_handle(n_atoms, probe, device, &h));
+    DeviceGuard g(h->device);
     h->n_dots = n_dots;
-    h->probe = probe;
-    h->unit.assign(unit_dots, unit_dots + 3 * (size_t)n_dots);
-    auto bail = [&](rsx_status s) {
+    std::vector<float4> table;
+    float reach = 0.f;
+    const int groups = append_groups(set, table, &reach);
+    h->unit_reach = reach;
+    h->dot_reach.assign(1, reach);
+    h->type_radius.assign(1, 0.f);
+    rsx_status s = upload_dots(h, table, {0}, {groups});
+    if (s != RSX_OK) {
         sasa_release(h);
         return s;
-    };
-    cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
-    if (e == cudaSuccess)
-        e = cudaEventCreate(&h->e0);
-    if (e == cudaSuccess)
-        e = cudaEventCreate(&h->e1);
-    if (e != cudaSuccess)
-        return bail(cuda_status(e, "sasa stream/events"));
-    rsx_status s;
-    if ((s = dev_alloc((void **)&h->d_unit, sizeof(float) * 3 * n_dots, "unit dots")) != RSX_OK)
-        return bail(s);
-    if ((s = dev_alloc((void **)&h->d_counts, sizeof(unsigned) * std::max(n_atoms, 1), "counts")) !=
-        RSX_OK)
-        return bail(s);
-    if ((s = dev_alloc((void **)&h->d_tests, sizeof(unsigned long long), "tests")) != RSX_OK)
-        return bail(s);
-    if ((s = host_alloc_pinned((void **)&h->h_counts, sizeof(unsigned) * std::max(n_atoms, 1),
-                               "pinned counts")) != RSX_OK)
-        return bail(s);
-    if ((s = host_alloc_pinned((void **)&h->h_tests, sizeof(unsigned long long), "pinned tests")) !=
-        RSX_OK)
-        return bail(s);
-    e = cudaMemcpyAsync(h->d_unit, h->unit.data(), sizeof(float) * 3 * n_dots,
-                        cudaMemcpyHostToDevice, h->st);
-    if (e == cudaSuccess)
-        e = cudaStreamSynchronize(h->st);
-    if (e != cudaSuccess)
-        return bail(cuda_status(e, "upload dots"));
+    }
+    *out = h;
+    return ok();
+}
+
+rsx_status rsx_sasa_create_typed(int n_atoms, const float *dot_map, int n_types, int stride,
+                                 const float *type_radii, float probe, int device,
+                                 rsx_sasa **out)
+{
+    if (!out)
+        return fail(RSX_INVALID_ARG, "out handle pointer is null");
+    *out = nullptr;
+    if (n_atoms < 0 || !dot_map || !type_radii || n_types <= 0 || n_types > kSasaMaxTypes ||
+        stride <= 0 || stride > 32 * kSasaMaxGroups || !(probe >= 0.f) || !std::isfinite(probe))
+        return fail(RSX_INVALID_ARG,
+                    "need n_atoms >= 0, 1..256 types, 1..4096 dots per type and probe >= 0");
+    for (int t = 0; t < n_types; ++t)
+        if (!(type_radii[t] >= 0.f) || !std::isfinite(type_radii[t]))
+            return fail(RSX_INVALID_ARG, "type " + std::to_string(t) + " has an invalid radius");
+    rsx_sasa *h = nullptr;
+    RSX_TRY(new_handle(n_atoms, probe, device, &h));
+    DeviceGuard g(h->device);
+    h->typed = true;
+    h->n_types = n_types;
+    h->type_radius.assign(type_radii, type_radii + n_types);
+    h->dot_reach.assign(n_types, 0.f);
+    h->dots_of_type.assign(n_types, 0);
+    std::vector<float4> table;
+    std::vector<int> base(n_types), count(n_types);
+    for (int t = 0; t < n_types; ++t) {
+        // a dot whose x is not finite is padding (rsasa_cl_gpu_alg.cpp:72-86)
+        std::vector<float4> set;
+        for (int k = 0; k < stride; ++k) {
+            const float *d = dot_map + 4 * ((size_t)t * stride + k);
+            if (std::isfinite(d[0]))
+                set.push_back(make_float4(d[0], d[1], d[2], 0.f));
+        }
+        h->dots_of_type[t] = (int)set.size();
+        base[t] = (int)(table.size() / 32);
+        count[t] = set.empty() ? 0 : append_groups(set, table, &h->dot_reach[t]);
+    }
+    rsx_status s = upload_dots(h, table, base, count);
+    if (s != RSX_OK) {
+        sasa_release(h);
+        return s;
+    }
     *out = h;
     return ok();
 }
@@ -260,6 +470,8 @@ rsx_status rsx_sasa_counts(rsx_sasa *h, const rsx_body *atoms, const float *radi
 {
     if (!h)
         return fail(RSX_ALG_NOT_INITIALIZED, "null rsx_sasa handle");
+    if (h->typed)
+        return fail(RSX_INVALID_ARG, "handle has a typed dot map: use rsx_sasa_counts_typed");
     if ((!atoms || !radii) && h->n > 0)
         return fail(RSX_INVALID_ARG, "atoms / radii are null");
     if (!out_counts)
@@ -267,30 +479,7 @@ rsx_status rsx_sasa_counts(rsx_sasa *h, const rsx_body *atoms, const float *radi
     RSX_TRY_CUDA(cudaSetDevice(h->device), "cudaSetDevice");
     if (h->n == 0)
         return ok();
-    SasaArgs a{};
-    size_t bytes = 0;
-    RSX_TRY(pack_cells(h, atoms, radii, a, bytes));
-    a.unit = h->d_unit;
-    a.counts = h->d_counts;
-    a.tests = h->d_tests;
-    a.n_atoms = h->n;
-    a.n_dots = h->n_dots;
-    a.probe = h->probe;
-    RSX_TRY_CUDA(cudaMemcpyAsync(h->d_buf, h->h_buf, bytes, cudaMemcpyHostToDevice, h->st),
-                 "upload cells");
-    RSX_TRY_CUDA(cudaMemsetAsync(h->d_tests, 0, sizeof(unsigned long long), h->st), "zero tests");
-    RSX_TRY_CUDA(cudaEventRecord(h->e0, h->st), "event");
-    RSX_LAUNCH(launch_sasa(a, h->st), "sasa kernel");
-    RSX_TRY_CUDA(cudaEventRecord(h->e1, h->st), "event");
-    RSX_TRY_CUDA(cudaMemcpyAsync(h->h_counts, h->d_counts, sizeof(unsigned) * h->n,
-                                 cudaMemcpyDeviceToHost, h->st),
-                 "read counts");
-    RSX_TRY_CUDA(cudaMemcpyAsync(h->h_tests, h->d_tests, sizeof(unsigned long long),
-                                 cudaMemcpyDeviceToHost, h->st),
-                 "read tests");
-    RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "sasa");
-    cudaEventElapsedTime(&h->last_ms, h->e0, h->e1);
-    h->last_tests = *h->h_tests;
+    RSX_TRY(run(h, atoms, radii));
     std::memcpy(out_counts, h->h_counts, sizeof(unsigned) * h->n);
     return ok();
 }
@@ -305,6 +494,40 @@ rsx_status rsx_sasa_calc(rsx_sasa *h, const rsx_body *atoms, const float *radii,
     RSX_TRY(rsx_sasa_counts(h, atoms, radii, c.data()));
     for (int i = 0; i < h->n; ++i) // rsasa_cl_gpu_alg.cpp:191-196
         out_rsasa[i] = static_cast<float>(c[i]) / h->n_dots;
+    return ok();
+}
+
+rsx_status rsx_sasa_counts_typed(rsx_sasa *h, const rsx_body *atoms, unsigned *out_counts)
+{
+    if (!h)
+        return fail(RSX_ALG_NOT_INITIALIZED, "null rsx_sasa handle");
+    if (!h->typed)
+        return fail(RSX_INVALID_ARG, "handle has unit dots: use rsx_sasa_counts");
+    if (!atoms && h->n > 0)
+        return fail(RSX_INVALID_ARG, "atoms are null");
+    if (!out_counts)
+        return fail(RSX_INVALID_ARG, "counts output is null");
+    RSX_TRY_CUDA(cudaSetDevice(h->device), "cudaSetDevice");
+    if (h->n == 0)
+        return ok();
+    RSX_TRY(run(h, atoms, nullptr));
+    std::memcpy(out_counts, h->h_counts, sizeof(unsigned) * h->n);
+    return ok();
+}
+
+rsx_status rsx_sasa_calc_typed(rsx_sasa *h, const rsx_body *atoms, float *out_rsasa)
+{
+    if (!h)
+        return fail(RSX_ALG_NOT_INITIALIZED, "null rsx_sasa handle");
+    if (!out_rsasa)
+        return fail(RSX_INVALID_ARG, "rsasa output is null");
+    std::vector<unsigned> c(std::max(h->n, 1));
+    RSX_TRY(rsx_sasa_counts_typed(h, atoms, c.data()));
+    for (int i = 0; i < h->n; ++i) { // rsasa_cl_gpu_alg.cpp:191-196: count / dots of the type
+        unsigned t;
+        std::memcpy(&t, &atoms[i].w, 4);
+        out_rsasa[i] = static_cast<float>(c[i]) / h->dots_of_type[t];
+    }
     return ok();
 }
 

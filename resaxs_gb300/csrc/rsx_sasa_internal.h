@@ -1,22 +1,59 @@
-// Arguments of the dot-sphere SASA kernel (sasa_kernels.cu).
+// Arguments of the dot-sphere SASA kernels (sasa_kernels.cu).
 #pragma once
 #include <cuda_runtime.h>
 
 namespace rsx {
 
-struct SasaArgs {
-    const float4 *atoms;      // [n_atoms] in cell order: x, y, z, radius
-    const int *orig_index;    // [n_atoms] caller index of each cell-ordered atom
-    const int *cell_of;       // [n_atoms][3] cell coordinates (cell order)
-    const int *cell_start;    // [n_cells + 1]
-    const float *unit;        // [n_dots][3] unit-sphere dots
-    unsigned *counts;         // [n_atoms] accessible dots, caller order
-    unsigned long long *tests; // optional: occlusion tests performed
-    int n_atoms, n_dots;
+// Upper bounds of the kernels' tables.
+constexpr int kSasaMaxGroups = 128;   // 32-dot groups per atom: <= 4096 dots
+constexpr int kSasaMaxTypes = 256;    // dot tables of the typed (per-type) form
+
+// Cell list built on the GPU from the atoms in caller order.
+struct SasaCellArgs {
+    const float4 *atoms_in;   // [n_atoms] caller order: x, y, z, w (type bits or unused)
+    const float *radii_in;    // [n_atoms] per-atom radii (unit form) or nullptr (typed form)
+    const float *type_radius; // [n_types] radius of each type (typed form)
+    int *cell_count;          // [n_cells + 1]; zero on entry to the bin kernel
+    int *cell_start;          // [n_cells + 1] exclusive prefix sum of cell_count
+    int *cell_of;             // [n_atoms] cell of each caller-order atom
+    int *rank_of;             // [n_atoms] slot inside its cell
+    float4 *atoms;            // [n_atoms] cell order: x, y, z, radius
+    int *orig_index;          // [n_atoms] caller index of each cell-ordered atom
+    int *type_of;             // [n_atoms] type of each cell-ordered atom (typed form)
+    int *cell_sorted;         // [n_atoms] cell of each cell-ordered atom
+    int n_atoms, n_cells;
     int dims[3];
-    float probe, max_radius;
+    float lo[3];
+    double inv_cell;
 };
 
+// Occlusion pass over the cell-ordered atoms: one warp per atom.
+struct SasaArgs {
+    const float4 *atoms;      // [n_atoms] cell order: x, y, z, radius
+    const int *orig_index;    // [n_atoms] caller index of each cell-ordered atom
+    const int *type_of;       // [n_atoms] type (typed form) or nullptr
+    const int *cell_id;       // [n_atoms] cell of each cell-ordered atom
+    const int *cell_start;    // [n_cells + 1]
+    // Dot tables in groups of 32 (spatially compact on the sphere); a dot
+    // whose x is not finite is padding.  Unit form: one table of unit
+    // directions, dot = unit * (r_i + P); typed form: one pre-scaled table
+    // per type, dot = d.
+    const float4 *dots;
+    const int *group_base;    // [n_types] first group of each type's table
+    const int *group_count;   // [n_types] groups of each type's table
+    const float *dot_reach;   // [n_types] largest |d| of each type's table (typed form)
+    float unit_reach;         // largest |u| of the unit table (unit form)
+    int typed;
+    unsigned *counts;         // [n_atoms] accessible dots, caller order
+    unsigned long long *tests; // optional: occlusion tests to the first occluder
+    int n_atoms;
+    int dims[3];
+    float lo[3];
+    double inv_cell;
+    float probe, margin;
+};
+
+cudaError_t launch_sasa_cells(const SasaCellArgs &c, cudaStream_t st);
 cudaError_t launch_sasa(const SasaArgs &a, cudaStream_t st);
 
 } // namespace rsx

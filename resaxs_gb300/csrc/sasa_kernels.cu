@@ -1,204 +1,465 @@
 // Dot-sphere SASA for sm_103a, written from scratch for this project.
 //
 // Semantics: the occlusion test of the reference's calc_rsasa kernel
-// (resaxslib/src/rsasa_dot_spheres.cl:94-163) with every operation rounded to
-// FP32 on its own (explicit __fmul_rn / __fadd_rn / __fsub_rn, so no FMA
-// contraction):
-//   ext_i = r_i + P;   dot = unit_k * ext_i;   sdot = dot + p_i
-//   w_b = (P + r_b) * (P + r_b);  d = sdot - p_b
-//   dist2 = (dx*dx + dy*dy) + dz*dz;   occluded iff (w_b - dist2) > 1e-4f
-// A dot counts as accessible when no atom (the atom itself included)
-// occludes it.  The occlusion is an OR over atoms, so any visiting order gives
-// the same count; only atoms within r_i + r_b + 2P (+0.01 A) of atom i can
-// occlude, which makes the cell-list prune exact.
+// (resaxslib/src/rsasa_dot_spheres.cl:94-163) and of its CPU algorithm
+// (resaxslib/src/rsasa_cpu_alg.cpp:62-69), every operation rounded to FP32
+// on its own (no FMA contraction):
+//   dot = d + p_i        d = unit_k * (r_i + P) (unit form) or the caller's
+//                        pre-scaled dot of atom i's type (typed form)
+//   w_b = (P + r_b) * (P + r_b);   dist2 = (dx*dx + dy*dy) + dz*dz
+//   occluded iff (w_b - dist2) > 1e-4f;  a dot whose x is not finite is padding
+// A dot is accessible when no atom (the atom itself included) occludes it.
+// The test is an OR over atoms, so any visiting order gives the same count.
 //
-// Mapping: one CTA of 128 threads per atom.  The CTA gathers the candidate
-// neighbours from the 27 surrounding cells into a shared-memory list (in
-// chunks of kNbCap), walking the atom's own cell first, then the face, edge
-// and corner neighbours, so the list runs roughly nearest first.  Dots are
-// then tested in two phases:
-//  * every thread tests each of its dots against the first kPhaseA entries
-//    (most buried dots meet an occluder there);
-//  * the dots still open are taken one at a time by their warp, which tests
-//    32 further neighbours per step (one per lane) until a ballot finds an
-//    occluder or the list ends.
-// A thread-per-dot loop over the whole list would run each warp as long as
-// its slowest dot (an exposed dot scans every candidate).
+// Cell list (built here from the caller-order atoms): a cell is at least as
+// wide as the largest reach |d| + P + r_b of any occluder, so the 27 cells
+// around an atom hold every atom that can occlude one of its dots.  Cells
+// are binned with atomics (the order inside a cell varies between calls;
+// the counts do not).
+//
+// Occlusion pass, one warp per atom:
+//  * the warp reads the 9 rows of 3 cells along z around the atom (each row
+//    is one contiguous range of the cell-ordered atoms) and keeps the atoms
+//    within reach in a shared-memory list (chunks of kListCap);
+//  * the list is sorted by distance band (8 bands; nearest atoms occlude
+//    most dots, so most dots meet their occluder in the first few
+//    candidates) into pairs for the FP32x2 units: (x0, x1, y0, y1),
+//    (z0, z1, -w0, -w1);
+//  * the atom's dots come in groups of 32 that are compact on the sphere
+//    (ordered so by the host), one dot per lane.  All lanes test the same
+//    candidates (shared-memory broadcast), four per step, two per FP32x2
+//    instruction; neighbouring dots tend to close on the same occluder, so
+//    the lanes of a group finish close together;
+//  * when a group is down to a few open dots with many candidates left, the
+//    warp takes those dots one at a time and tests 64 candidates per step
+//    (a pair per lane).
+// The subtraction s - b is formed as b + (-s) and w - dist2 as
+// -(dist2 + (-w)): negation is exact and round-to-nearest is symmetric, so
+// every value has the bits of the reference's expression.
 #include "rsx_internal.h"
 #include "rsx_sasa_internal.h"
 
 namespace rsx {
 
-constexpr int kSasaThreads = 128;
-constexpr int kNbCap = 1024;
-constexpr int kPhaseA = 96; // neighbours every thread tests per dot before the warp takes over
+constexpr int kSasaWarps = 4;      // warps (atoms) per CTA
+constexpr int kListCap = 192;      // candidates per warp in shared memory at a time (<= 8 rows)
+constexpr int kCoopLanes = 4;      // open dots at or below which the warp tests them one by one
+constexpr int kCoopMinPairs = 32;  // ... when at least this many candidate pairs remain
+constexpr unsigned kFull = 0xffffffffu;
 
-// The 27 cell offsets (dx, dy, dz) in order of distance: own cell, faces,
-// edges, corners.
-__constant__ signed char c_cell_order[27][3] = {
-    {0, 0, 0},   {-1, 0, 0},  {1, 0, 0},   {0, -1, 0},  {0, 1, 0},   {0, 0, -1},  {0, 0, 1},
-    {-1, -1, 0}, {-1, 1, 0},  {1, -1, 0},  {1, 1, 0},   {-1, 0, -1}, {-1, 0, 1},  {1, 0, -1},
-    {1, 0, 1},   {0, -1, -1}, {0, -1, 1},  {0, 1, -1},  {0, 1, 1},   {-1, -1, -1}, {-1, -1, 1},
-    {-1, 1, -1}, {-1, 1, 1},  {1, -1, -1}, {1, -1, 1},  {1, 1, -1},  {1, 1, 1}};
-
-__device__ __forceinline__ bool occludes(float sx, float sy, float sz, float4 b)
+// Cell coordinates in FP64: atoms closer than one cell width never land two
+// cells apart, whatever the grid's extent.
+__device__ __forceinline__ void cell_coords(float x, float y, float z, const float lo[3],
+                                            double inv_cell, const int dims[3], int c[3])
 {
-    const float dx = __fsub_rn(sx, b.x);
-    const float dy = __fsub_rn(sy, b.y);
-    const float dz = __fsub_rn(sz, b.z);
-    const float dist2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-    return __fsub_rn(b.w, dist2) > 0.0001f;
+    const float v[3] = {x, y, z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        int k = (int)floor(((double)v[a] - (double)lo[a]) * inv_cell);
+        c[a] = min(max(k, 0), dims[a] - 1);
+    }
 }
 
-__global__ void __launch_bounds__(kSasaThreads) sasa_kernel(const SasaArgs a)
+// ---- cell list --------------------------------------------------------------
+
+__global__ void sasa_bin_kernel(const SasaCellArgs c)
 {
-    __shared__ float4 s_nb[kNbCap]; // x, y, z, (P + r_b)^2
-    __shared__ int s_count;
-    __shared__ unsigned s_exposed;
-    __shared__ unsigned long long s_tests;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n_atoms)
+        return;
+    const float4 p = c.atoms_in[i];
+    int k[3];
+    cell_coords(p.x, p.y, p.z, c.lo, c.inv_cell, c.dims, k);
+    const int cid = (k[0] * c.dims[1] + k[1]) * c.dims[2] + k[2];
+    c.cell_of[i] = cid;
+    c.rank_of[i] = atomicAdd(&c.cell_count[cid], 1);
+}
 
-    const int i = blockIdx.x; // sorted (cell) order
-    const int tid = threadIdx.x;
-    const float4 pi = a.atoms[i]; // .w = radius
-    const float probe = a.probe;
-    const float ext = __fadd_rn(pi.w, probe);
-    const int dots_per_thread = (a.n_dots + kSasaThreads - 1) / kSasaThreads;
-    unsigned occluded = 0; // bit t: dot tid + t * kSasaThreads
-    for (int t = 0; t < dots_per_thread; ++t)
-        if (tid + t * kSasaThreads >= a.n_dots)
-            occluded |= 1u << t;
-    if (tid == 0) {
-        s_exposed = 0;
-        s_tests = 0;
+// Exclusive prefix sum of the cell counts by one CTA (cells number at most
+// 4 n + 4096), 4 cells per thread per tile.
+__global__ void __launch_bounds__(1024) sasa_scan_kernel(const int *count, int *start, int n)
+{
+    __shared__ int s_warp[32];
+    __shared__ int s_carry;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0)
+        s_carry = 0;
+    __syncthreads();
+    for (int base = 0; base < n; base += 4 * 1024) {
+        int v[4], sum = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int idx = base + threadIdx.x * 4 + k;
+            v[k] = idx < n ? count[idx] : 0;
+            sum += v[k];
+        }
+        int x = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(kFull, x, o);
+            if (lane >= o)
+                x += y;
+        }
+        if (lane == 31)
+            s_warp[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            int w = s_warp[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(kFull, w, o);
+                if (lane >= o)
+                    w += y;
+            }
+            s_warp[lane] = w;
+        }
+        __syncthreads();
+        int excl = s_carry + (warp ? s_warp[warp - 1] : 0) + x - sum;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int idx = base + threadIdx.x * 4 + k;
+            if (idx < n)
+                start[idx] = excl;
+            excl += v[k];
+        }
+        __syncthreads();
+        if (threadIdx.x == 1023)
+            s_carry = excl;
+        __syncthreads();
     }
-    unsigned long long tests = 0;
+    if (threadIdx.x == 0)
+        start[n] = s_carry;
+}
 
-    // cell of atom i and the candidate range
-    const int cx = a.cell_of[i * 3 + 0], cy = a.cell_of[i * 3 + 1], cz = a.cell_of[i * 3 + 2];
-    const float reach = pi.w + a.max_radius + 2.0f * probe + 0.01f;
-    const float reach2 = reach * reach;
+__global__ void sasa_scatter_kernel(const SasaCellArgs c)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n_atoms)
+        return;
+    const float4 p = c.atoms_in[i];
+    const int s = c.cell_start[c.cell_of[i]] + c.rank_of[i];
+    float r;
+    if (c.radii_in) {
+        r = c.radii_in[i];
+    } else {
+        const int t = (int)__float_as_uint(p.w);
+        r = c.type_radius[t];
+        c.type_of[s] = t;
+    }
+    c.atoms[s] = make_float4(p.x, p.y, p.z, r);
+    c.orig_index[s] = i;
+    c.cell_sorted[s] = c.cell_of[i];
+}
 
-    // iterate the 27 cells as a flat sequence of candidate atoms, in chunks
-    // that fit the shared list
-    int cell_idx = 0;      // 0..26
-    int cell_pos = 0;      // position inside the current cell
-    bool more = true;
-    while (more) {
-        __syncthreads();
-        if (tid == 0)
-            s_count = 0;
-        __syncthreads();
-        // thread 0 walks the cells; the CTA filters in parallel batches
-        // (all threads read the same loop state from registers computed identically)
-        while (true) {
-            // locate the next non-empty cell range (same on every thread)
-            int begin = 0, end = 0;
-            bool found = false;
-            while (cell_idx < 27) {
-                const int ox = c_cell_order[cell_idx][0], oy = c_cell_order[cell_idx][1],
-                          oz = c_cell_order[cell_idx][2];
-                const int x = cx + ox, y = cy + oy, z = cz + oz;
-                if (x >= 0 && y >= 0 && z >= 0 && x < a.dims[0] && y < a.dims[1] && z < a.dims[2]) {
-                    const int c = (x * a.dims[1] + y) * a.dims[2] + z;
-                    begin = a.cell_start[c] + cell_pos;
-                    end = a.cell_start[c + 1];
-                    if (begin < end) {
-                        found = true;
-                        break;
+cudaError_t launch_sasa_cells(const SasaCellArgs &c, cudaStream_t st)
+{
+    if (c.n_atoms == 0)
+        return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(c.cell_count, 0, sizeof(int) * (size_t)(c.n_cells + 1), st);
+    if (e != cudaSuccess)
+        return e;
+    const int blocks = (c.n_atoms + 255) / 256;
+    sasa_bin_kernel<<<blocks, 256, 0, st>>>(c);
+    sasa_scan_kernel<<<1, 1024, 0, st>>>(c.cell_count, c.cell_start, c.n_cells);
+    sasa_scatter_kernel<<<blocks, 256, 0, st>>>(c);
+    count_launch(3);
+    return cudaGetLastError();
+}
+
+// ---- occlusion pass ---------------------------------------------------------
+
+constexpr int kBuckets = 8;        // distance bands of the candidate sort
+constexpr int kRows = kListCap / 32;
+
+// Two candidates against one dot: bit 0 / bit 1 set when candidate 0 / 1 of
+// the pair occludes it.  A = (x0, x1, y0, y1), B = (z0, z1, -w0, -w1); n* are
+// the dot's negated coordinates in both halves.
+__device__ __forceinline__ unsigned occludes_pair(float2 nx, float2 ny, float2 nz, float4 A,
+                                                  float4 B)
+{
+    const float2 dx = __fadd2_rn(make_float2(A.x, A.y), nx);
+    const float2 dy = __fadd2_rn(make_float2(A.z, A.w), ny);
+    const float2 dz = __fadd2_rn(make_float2(B.x, B.y), nz);
+    const float2 d2 =
+        __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
+    const float2 e = __fadd2_rn(d2, make_float2(B.z, B.w)); // dist2 - w = -(w - dist2)
+    return (e.x < -1e-4f ? 1u : 0u) | (e.y < -1e-4f ? 2u : 0u);
+}
+
+// Dot g * 32 + lane of the atom at p (cell order) as an absolute position.
+__device__ __forceinline__ float3 dot_position(const SasaArgs &a, int group, int lane, float4 p,
+                                               float ext)
+{
+    const float4 d = a.dots[group * 32 + lane];
+    if (a.typed)
+        return make_float3(__fadd_rn(d.x, p.x), __fadd_rn(d.y, p.y), __fadd_rn(d.z, p.z));
+    return make_float3(__fadd_rn(__fmul_rn(d.x, ext), p.x), __fadd_rn(__fmul_rn(d.y, ext), p.y),
+                       __fadd_rn(__fmul_rn(d.z, ext), p.z));
+}
+
+// Tests every open dot of the atom against the n_pairs candidate pairs of the
+// warp's list (pair j: pairs[2j] = A, pairs[2j + 1] = B); updates the
+// per-group open masks.  A dot whose x is not finite never opens.
+__device__ void test_list(const SasaArgs &a, const float4 *pairs, int n_pairs, int n_cand,
+                          unsigned *s_open, int g0, int ng, float4 p, float ext, int lane,
+                          unsigned long long &tests_out)
+{
+    unsigned tests = 0; // < 4096 dots x kListCap candidates per call
+    for (int g = 0; g < ng; ++g) {
+        const unsigned open_m = s_open[g];
+        if (open_m == 0)
+            continue;
+        const float3 s = dot_position(a, g0 + g, lane, p, ext);
+        bool open = ((open_m >> lane) & 1u) && isfinite(s.x);
+        const float2 nx = make_float2(-s.x, -s.x), ny = make_float2(-s.y, -s.y),
+                     nz = make_float2(-s.z, -s.z);
+        int q = 0; // candidate pair
+        while (q < n_pairs) {
+            const unsigned act = __ballot_sync(kFull, open);
+            if (act == 0)
+                break;
+            if (__popc(act) <= kCoopLanes && n_pairs - q >= kCoopMinPairs) {
+                // the remaining open dots one at a time, a pair per lane per step
+                unsigned left = act;
+                while (left) {
+                    const int o = __ffs(left) - 1;
+                    left &= left - 1;
+                    const float ox = __shfl_sync(kFull, nx.x, o);
+                    const float oy = __shfl_sync(kFull, ny.x, o);
+                    const float oz = __shfl_sync(kFull, nz.x, o);
+                    const float2 ox2 = make_float2(ox, ox), oy2 = make_float2(oy, oy),
+                                 oz2 = make_float2(oz, oz);
+                    for (int r = q; r < n_pairs; r += 32) {
+                        const int pr = r + lane;
+                        const unsigned hm =
+                            pr < n_pairs ? occludes_pair(ox2, oy2, oz2, pairs[2 * pr],
+                                                         pairs[2 * pr + 1])
+                                         : 0u;
+                        const unsigned ball = __ballot_sync(kFull, hm != 0u);
+                        if (ball) {
+                            const int l = __ffs(ball) - 1;
+                            const unsigned h = __shfl_sync(kFull, hm, l);
+                            if (lane == o) {
+                                open = false;
+                                tests += (unsigned)(2 * (r + l) + __ffs(h));
+                            }
+                            break;
+                        }
                     }
                 }
-                ++cell_idx;
-                cell_pos = 0;
-            }
-            if (!found) {
-                more = false;
+                q = n_pairs;
                 break;
             }
-            // room left in the list decides how many candidates this batch takes
-            __syncthreads();
-            const int room = kNbCap - s_count;
-            __syncthreads();
-            if (room < kSasaThreads)
-                break; // list full enough: test dots, keep the walk state
-            const int take = min(end - begin, kSasaThreads);
-            if (tid < take) {
-                const float4 b = a.atoms[begin + tid];
-                const float dx = b.x - pi.x, dy = b.y - pi.y, dz = b.z - pi.z;
-                if (dx * dx + dy * dy + dz * dz < reach2) {
-                    const float e = __fadd_rn(probe, b.w);
-                    const int slot = atomicAdd(&s_count, 1);
-                    s_nb[slot] = make_float4(b.x, b.y, b.z, __fmul_rn(e, e));
-                }
+            const unsigned h =
+                occludes_pair(nx, ny, nz, pairs[2 * q], pairs[2 * q + 1]) |
+                (occludes_pair(nx, ny, nz, pairs[2 * q + 2], pairs[2 * q + 3]) << 2);
+            if (open && h) {
+                open = false;
+                tests += (unsigned)(2 * q + __ffs(h));
             }
-            cell_pos += take;
-            if (begin + take >= end) {
-                ++cell_idx;
-                cell_pos = 0;
-            }
+            q += 2;
         }
-        __syncthreads();
-        const int n_nb = s_count;
-        const int n_a = min(n_nb, kPhaseA);
-        const int lane = tid & 31, warp_base = tid & ~31;
-        // phase A: every thread, its own dots, the first n_a neighbours
-        unsigned open = 0; // bit t: dot t still open after phase A
-        for (int t = 0; t < dots_per_thread; ++t) {
-            if (occluded & (1u << t))
-                continue;
-            const int k = tid + t * kSasaThreads;
-            const float sx = __fadd_rn(__fmul_rn(a.unit[3 * k + 0], ext), pi.x);
-            const float sy = __fadd_rn(__fmul_rn(a.unit[3 * k + 1], ext), pi.y);
-            const float sz = __fadd_rn(__fmul_rn(a.unit[3 * k + 2], ext), pi.z);
-            int n = 0;
-            for (; n < n_a; ++n) {
-                if (occludes(sx, sy, sz, s_nb[n])) {
-                    occluded |= 1u << t;
-                    ++n;
-                    break;
-                }
-            }
-            tests += (unsigned long long)n;
-            if (!(occluded & (1u << t)) && n_nb > n_a)
-                open |= 1u << t;
-        }
-        // phase B: the warp takes its open dots one at a time, 32 neighbours a step
-        for (int t = 0; t < dots_per_thread; ++t) {
-            unsigned pending = __ballot_sync(0xffffffffu, (open >> t) & 1u);
-            while (pending) {
-                const int owner = __ffs(pending) - 1;
-                pending &= pending - 1;
-                const int k = warp_base + owner + t * kSasaThreads;
-                const float sx = __fadd_rn(__fmul_rn(a.unit[3 * k + 0], ext), pi.x);
-                const float sy = __fadd_rn(__fmul_rn(a.unit[3 * k + 1], ext), pi.y);
-                const float sz = __fadd_rn(__fmul_rn(a.unit[3 * k + 2], ext), pi.z);
-                int tested = n_nb - n_a;
-                for (int j0 = n_a; j0 < n_nb; j0 += 32) {
-                    const int j = j0 + lane;
-                    const bool hit = j < n_nb && occludes(sx, sy, sz, s_nb[j]);
-                    const unsigned ball = __ballot_sync(0xffffffffu, hit);
-                    if (ball) {
-                        tested = j0 - n_a + __ffs(ball);
-                        if (lane == owner)
-                            occluded |= 1u << t;
-                        break;
-                    }
-                }
-                if (lane == owner)
-                    tests += (unsigned long long)tested;
-            }
+        if (open)
+            tests += (unsigned)n_cand;
+        const unsigned m = __ballot_sync(kFull, open);
+        if (lane == 0)
+            s_open[g] = m;
+        __syncwarp();
+    }
+    tests_out += tests;
+}
+
+// Sorts the n staged candidates of the warp's list (list[q] = x, y, z, -w;
+// band[q] = distance band) by band, stable, into the pair layout in place,
+// and pads the pairs to a multiple of 4 candidates that never occlude.
+// Returns the number of pairs.
+__device__ int sort_into_pairs(float4 *list, unsigned char *band, int *s_count, int n, int lane)
+{
+    float4 v[kRows];
+    int b[kRows];
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) {
+        const int q = r * 32 + lane;
+        b[r] = kBuckets; // no candidate
+        v[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (q < n) {
+            v[r] = list[q];
+            b[r] = band[q];
         }
     }
+    if (lane < kBuckets)
+        s_count[lane] = 0;
+    __syncwarp();
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) {
+        if (r * 32 >= n)
+            break;
+        const unsigned m = __match_any_sync(kFull, b[r]);
+        if (b[r] < kBuckets && (m & lt) == 0u)
+            s_count[b[r]] += __popc(m);
+        __syncwarp();
+    }
+    // exclusive prefix over the bands (lanes 0..7)
+    int c = lane < kBuckets ? s_count[lane] : 0;
+    int x = c;
+#pragma unroll
+    for (int o = 1; o < kBuckets; o <<= 1) {
+        const int y = __shfl_up_sync(kFull, x, o);
+        if (lane >= o)
+            x += y;
+    }
+    __syncwarp();
+    if (lane < kBuckets)
+        s_count[lane] = x - c;
+    __syncwarp();
+    float *f = reinterpret_cast<float *>(list);
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) {
+        if (r * 32 >= n)
+            break;
+        const unsigned m = __match_any_sync(kFull, b[r]);
+        if (b[r] < kBuckets) {
+            const int pos = s_count[b[r]] + __popc(m & lt);
+            const int base = 8 * (pos >> 1) + (pos & 1);
+            f[base] = v[r].x;
+            f[base + 2] = v[r].y;
+            f[base + 4] = v[r].z;
+            f[base + 6] = v[r].w;
+        }
+        __syncwarp();
+        if (b[r] < kBuckets && (m & lt) == 0u)
+            s_count[b[r]] += __popc(m);
+        __syncwarp();
+    }
+    const int padded = (n + 3) & ~3;
+    if (lane < padded - n) {
+        const int k = n + lane;
+        f[8 * (k >> 1) + (k & 1)] = __int_as_float(0x7fc00000); // x = NaN: never occludes
+    }
+    __syncwarp();
+    return padded >> 1;
+}
+
+__global__ void __launch_bounds__(kSasaWarps * 32, 8) sasa_kernel(const SasaArgs a)
+{
+    __shared__ float4 s_list[kSasaWarps][kListCap]; // staged candidates, then pairs
+    __shared__ unsigned char s_band[kSasaWarps][kListCap];
+    __shared__ int s_count[kSasaWarps][kBuckets];
+    __shared__ unsigned s_open[kSasaWarps][kSasaMaxGroups];
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = blockIdx.x * kSasaWarps + warp; // cell order
+    if (i >= a.n_atoms)
+        return; // the whole warp leaves; no CTA-wide barrier follows
+    float4 *list = s_list[warp];
+    unsigned char *band = s_band[warp];
+    unsigned *open = s_open[warp];
+
+    const float4 p = a.atoms[i]; // .w = radius
+    const int t = a.typed ? a.type_of[i] : 0;
+    const int g0 = a.group_base[t], ng = a.group_count[t];
+    const float ext = __fadd_rn(p.w, a.probe);
+    // an occluder b of a dot of this atom lies within |d| + P + r_b of it
+    const float dot_reach = a.typed ? a.dot_reach[t] : ext * a.unit_reach;
+    const float reach = dot_reach * 1.000001f + a.probe + a.margin;
+    for (int g = lane; g < ng; g += 32)
+        open[g] = kFull; // narrowed to the valid dots by the first test_list
+    __syncwarp();
+
+    // the 9 rows of 3 cells along z around the atom's cell (contiguous in
+    // the cell-ordered atoms: z is the fastest cell coordinate)
+    int cc[3];
+    {
+        const int cid = a.cell_id[i]; // (x * dims1 + y) * dims2 + z
+        cc[2] = cid % a.dims[2];
+        cc[1] = (cid / a.dims[2]) % a.dims[1];
+        cc[0] = cid / (a.dims[2] * a.dims[1]);
+    }
+    const int z0 = max(cc[2] - 1, 0), z1 = min(cc[2] + 1, a.dims[2] - 1);
+    int row = 0, pos = 0, n_list = 0;
+    bool walk_done = false;
+    unsigned long long tests = 0;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    while (true) {
+        // gather until the list cannot take another 32 and the atom itself
+        while (!walk_done && n_list < kListCap - 32) {
+            int beg = 0, end = 0;
+            while (row < 9) {
+                const int x = cc[0] + row / 3 - 1, y = cc[1] + row % 3 - 1;
+                if (x >= 0 && y >= 0 && x < a.dims[0] && y < a.dims[1]) {
+                    const int c = (x * a.dims[1] + y) * a.dims[2];
+                    beg = a.cell_start[c + z0] + pos;
+                    end = a.cell_start[c + z1 + 1];
+                    if (beg < end)
+                        break;
+                }
+                ++row;
+                pos = 0;
+            }
+            if (row >= 9) {
+                walk_done = true;
+                break;
+            }
+            const int j = beg + lane;
+            bool keep = false;
+            float4 b = make_float4(0.f, 0.f, 0.f, 0.f);
+            float ratio = 0.f;
+            if (j < end && j != i) {
+                b = a.atoms[j];
+                const float dx = b.x - p.x, dy = b.y - p.y, dz = b.z - p.z;
+                const float lim = reach + b.w;
+                const float d2 = dx * dx + dy * dy + dz * dz;
+                keep = d2 < lim * lim;
+                ratio = __fdividef(d2, lim * lim); // the band is a heuristic: fast math
+
+            }
+            const unsigned m = __ballot_sync(kFull, keep);
+            if (keep) {
+                const int k = n_list + __popc(m & lt_mask);
+                const float e = __fadd_rn(a.probe, b.w);
+                list[k] = make_float4(b.x, b.y, b.z, -__fmul_rn(e, e));
+                band[k] = (unsigned char)min(kBuckets - 1,
+                                             (int)(kBuckets * ratio * rsqrtf(fmaxf(ratio, 1e-20f))));
+            }
+            n_list += __popc(m);
+            if (beg + 32 >= end) {
+                ++row;
+                pos = 0;
+            } else {
+                pos += 32;
+            }
+        }
+        if (walk_done) {
+            // the atom itself, last in the last list (it occludes its own
+            // dots only through rounding at very large coordinates)
+            if (lane == 0) {
+                const float e = __fadd_rn(a.probe, p.w);
+                list[n_list] = make_float4(p.x, p.y, p.z, -__fmul_rn(e, e));
+                band[n_list] = kBuckets - 1;
+            }
+            ++n_list;
+        }
+        __syncwarp();
+        const int n_pairs = sort_into_pairs(list, band, s_count[warp], n_list, lane);
+        test_list(a, list, n_pairs, n_list, open, g0, ng, p, ext, lane, tests);
+        n_list = 0;
+        __syncwarp();
+        if (walk_done)
+            break;
+    }
     unsigned exposed = 0;
-    for (int t = 0; t < dots_per_thread; ++t)
-        exposed += (occluded & (1u << t)) ? 0u : 1u;
-    atomicAdd(&s_exposed, exposed);
-    if (a.tests)
-        atomicAdd(&s_tests, tests);
-    __syncthreads();
-    if (tid == 0) {
-        a.counts[a.orig_index[i]] = s_exposed;
+    for (int g = lane; g < ng; g += 32)
+        exposed += __popc(open[g]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        exposed += __shfl_xor_sync(kFull, exposed, o);
+        tests += __shfl_xor_sync(kFull, tests, o);
+    }
+    if (lane == 0) {
+        a.counts[a.orig_index[i]] = exposed;
         if (a.tests)
-            atomicAdd(a.tests, s_tests);
+            atomicAdd(a.tests, tests);
     }
 }
 
@@ -206,9 +467,8 @@ cudaError_t launch_sasa(const SasaArgs &a, cudaStream_t st)
 {
     if (a.n_atoms == 0)
         return cudaSuccess;
-    if (a.n_dots > kSasaThreads * 32)
-        return cudaErrorInvalidValue;
-    sasa_kernel<<<a.n_atoms, kSasaThreads, 0, st>>>(a);
+    const int blocks = (a.n_atoms + kSasaWarps - 1) / kSasaWarps;
+    sasa_kernel<<<blocks, kSasaWarps * 32, 0, st>>>(a);
     count_launch();
     return cudaGetLastError();
 }

@@ -1,6 +1,8 @@
 """Dot-sphere SASA through librsx: ``DotSphereSasa`` owns an ``rsx_sasa``
-handle; ``RsasaAlgorithm`` mirrors resaxslib's ``i_rsasa`` interface
-(resaxslib/include/rsasa_algorithm.hpp:42-61)."""
+handle with one unit dot set and per-atom radii; ``TypedDotSphereSasa`` owns
+one with the reference's per-type pre-scaled dot map and per-type radii
+(resaxslib/src/rsasa_cl_gpu_alg.cpp:59-89); ``RsasaAlgorithm`` mirrors
+resaxslib's ``i_rsasa`` interface (resaxslib/include/rsasa_algorithm.hpp:42-61)."""
 from __future__ import annotations
 
 import ctypes
@@ -10,7 +12,8 @@ import numpy as np
 from . import _lib
 from ._lib import ResaxsError, check, lib
 
-__all__ = ["DotSphereSasa", "RsasaAlgorithm", "fibonacci_dots", "dodeca_icosa_dots"]
+__all__ = ["DotSphereSasa", "TypedDotSphereSasa", "RsasaAlgorithm", "fibonacci_dots",
+           "dodeca_icosa_dots", "dot_map_from_sets"]
 
 
 def fibonacci_dots(n_dots: int) -> np.ndarray:
@@ -78,6 +81,81 @@ class DotSphereSasa:
         atoms, radii = self._inputs(atoms, radii)
         out = np.zeros(self.n, np.float32)
         check(lib().rsx_sasa_calc(self._h, atoms, radii, out))
+        return out
+
+    def stats(self):
+        t = ctypes.c_ulonglong()
+        ms = ctypes.c_float()
+        check(lib().rsx_sasa_stats(self._h, ctypes.byref(t), ctypes.byref(ms)))
+        return int(t.value), float(ms.value)
+
+
+def dot_map_from_sets(dot_sets) -> np.ndarray:
+    """Per-type dot sets (a list of (n_t, 3 or 4) arrays) as one (n_types,
+    stride, 4) map padded with -inf dots, the layout of the reference's
+    dots_map_ (rsasa_cl_gpu_alg.cpp:72-86)."""
+    sets = [np.asarray(d, np.float32).reshape(len(d), -1) for d in dot_sets]
+    stride = max([len(d) for d in sets] + [1])
+    m = np.full((len(sets), stride, 4), -np.inf, np.float32)
+    for t, d in enumerate(sets):
+        m[t, :len(d), :3] = d[:, :3]
+        m[t, :len(d), 3] = 0.0
+    return m
+
+
+class TypedDotSphereSasa:
+    """Accessible-dot counts with the reference's own dot layout: pre-scaled
+    dots per atom type (``dot_map``: (n_types, stride, 4), a dot whose x is not
+    finite is padding) and one radius per type; atoms carry their type in
+    column 3."""
+
+    def __init__(self, n_atoms: int, dot_map, type_radii, probe: float, device: int = -1):
+        self.map = np.ascontiguousarray(dot_map, np.float32)
+        if self.map.ndim != 3 or self.map.shape[2] != 4:
+            raise ResaxsError(_lib.RSX_INVALID_ARG, "dot map must be [n_types][stride][4]")
+        self.type_radii = np.ascontiguousarray(type_radii, np.float32).reshape(-1)
+        if len(self.type_radii) < self.map.shape[0]:
+            raise ResaxsError(_lib.RSX_INVALID_ARG, "need one radius per type")
+        self.n = int(n_atoms)
+        self.probe = float(probe)
+        h = ctypes.c_void_p()
+        check(lib().rsx_sasa_create_typed(self.n, self.map.reshape(-1), self.map.shape[0],
+                                          self.map.shape[1], self.type_radii,
+                                          ctypes.c_float(self.probe), int(device),
+                                          ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().rsx_sasa_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _atoms(self, atoms):
+        atoms = np.ascontiguousarray(atoms, np.float32).reshape(-1)
+        if atoms.size < 4 * self.n:
+            raise ResaxsError(_lib.RSX_INVALID_ARG, f"need {self.n} atoms")
+        return atoms
+
+    def counts(self, atoms) -> np.ndarray:
+        out = np.zeros(self.n, np.uint32)
+        check(lib().rsx_sasa_counts_typed(self._h, self._atoms(atoms), out))
+        return out
+
+    def rsasa(self, atoms) -> np.ndarray:
+        out = np.zeros(self.n, np.float32)
+        check(lib().rsx_sasa_calc_typed(self._h, self._atoms(atoms), out))
         return out
 
     def stats(self):

@@ -1,7 +1,9 @@
-"""Dot-sphere SASA: GPU counts must equal the strict-FP32 oracle bit for bit."""
+"""Dot-sphere SASA: GPU counts must equal the strict-FP32 oracle and the
+reference's own CPU SASA bit for bit."""
 import numpy as np
 import pytest
 
+from conftest import sasa_dot_map
 from resaxs_gb300 import workloads as W
 
 
@@ -145,3 +147,107 @@ def test_bad_inputs_rejected():
                 s.rsasa(*args)
             assert e.value.code == _lib.RSX_INVALID_ARG
         assert s.counts(atoms, np.ones(3, np.float32)).shape == (3,)
+
+
+# ---- the reference's own dot layout (typed handles) -----------------------------
+
+
+def _types(atoms):
+    return np.ascontiguousarray(atoms, np.float32).view(np.uint32)[:, 3]
+
+
+@gpu
+@pytest.mark.parametrize("name", ["a", "b", "c"])
+def test_typed_counts_equal_reference_cpu_sasa(golden_sasa, name):
+    """The reference's per-type latitude dot sets (create_dots, 5 dots/A^2,
+    probe 1.4) through rsx_sasa_create_typed: counts and rsasa equal those of
+    the reference's compiled rsasa_cpu_alg<float,float>::calc_rsasa."""
+    from resaxs_gb300.sasa import TypedDotSphereSasa
+    g = golden_sasa
+    atoms = g[f"{name}_atoms"]
+    n_dots = np.diff(g["dots_latitude_start"])[_types(atoms)]
+    ref = g[f"{name}_rsasa_ref"]
+    with TypedDotSphereSasa(len(atoms), sasa_dot_map(g, "latitude"), g["radii"],
+                            float(g["probe"])) as s:
+        got = s.counts(atoms)
+        rs = s.rsasa(atoms)
+        tests, ms = s.stats()
+    assert np.array_equal(got.astype(np.int64), np.rint(ref * n_dots).astype(np.int64)), \
+        int(np.sum(got != np.rint(ref * n_dots)))
+    assert np.array_equal(rs.view(np.uint32), ref.view(np.uint32))
+    assert tests > 0 and ms > 0
+
+
+@gpu
+@pytest.mark.parametrize("kind", ["dodeca_icosa", "fibonacci", "32", "dodecahedron"])
+def test_typed_reference_dot_maps_match_oracle(oracle_lib, golden_sasa, kind):
+    """The reference's other generators, including the OpenCL algorithm's
+    dodeca-icosa map (32 dots per type, probe 1.8), on all 16 types."""
+    from resaxs_gb300.sasa import TypedDotSphereSasa
+    g = golden_sasa
+    atoms = g["b_atoms"]
+    dm = sasa_dot_map(g, kind)
+    probe = float(g[f"dots_{kind}_probe"])
+    with TypedDotSphereSasa(len(atoms), dm, g["radii"], probe) as s:
+        got = s.counts(atoms)
+    ref = oracle_lib.sasa_counts_typed(atoms, g["radii"], dm, probe)
+    assert np.array_equal(got, ref), int(np.sum(got != ref))
+
+
+@gpu
+def test_typed_and_unit_forms_agree(golden_sasa):
+    """Fibonacci dots: the reference's pre-scaled per-type set and the unit
+    set scaled in the kernel give the same counts."""
+    from resaxs_gb300.sasa import DotSphereSasa, TypedDotSphereSasa, fibonacci_dots
+    g = golden_sasa
+    atoms = g["a_atoms"]
+    radii = g["radii"][_types(atoms)]
+    with TypedDotSphereSasa(len(atoms), sasa_dot_map(g, "fibonacci"), g["radii"],
+                            float(g["probe"])) as s:
+        typed = s.counts(atoms)
+    with DotSphereSasa(len(atoms), probe=float(g["probe"]), unit_dots=fibonacci_dots(64)) as s:
+        unit = s.counts(atoms, radii)
+    assert np.array_equal(typed, unit)
+
+
+@gpu
+def test_typed_edge_cases(oracle_lib, golden_sasa):
+    """One atom; duplicates; a type whose dot set is all padding; atoms at
+    large coordinates; a dot map whose padding sits between dots."""
+    from resaxs_gb300.sasa import TypedDotSphereSasa
+    g = golden_sasa
+    dm = sasa_dot_map(g, "latitude")
+    dm[5, :] = -np.inf                       # type 5: no dots
+    dm[3, ::7] = np.nan                       # padding inside type 3's set
+    xyz = np.array([[0, 0, 0], [2.5, 0, 0], [2.5, 0, 0], [1e4, -3e4, 5e3], [1e4 + 3.1, -3e4, 5e3],
+                    [0, 0, 3.0], [-2.0, 1.0, 0.5]], np.float32)
+    atoms = W.pack_bodies(xyz, np.array([0, 3, 3, 2, 3, 5, 11], np.uint32))
+    for sub in (atoms[:1], atoms):
+        with TypedDotSphereSasa(len(sub), dm, g["radii"], 1.4) as s:
+            got = s.counts(sub)
+            rs = s.rsasa(sub)
+        ref = oracle_lib.sasa_counts_typed(sub, g["radii"], dm, 1.4)
+        assert np.array_equal(got, ref)
+        n_dots = np.isfinite(dm[:, :, 0]).sum(axis=1)[_types(sub)]
+        with np.errstate(invalid="ignore", divide="ignore"):
+            want = got.astype(np.float32) / n_dots.astype(np.float32)
+        assert np.array_equal(np.isnan(rs), np.isnan(want))
+        assert np.array_equal(rs[~np.isnan(rs)], want[~np.isnan(want)])
+
+
+@gpu
+def test_typed_bad_inputs(golden_sasa):
+    from resaxs_gb300 import _lib
+    from resaxs_gb300.sasa import TypedDotSphereSasa
+    g = golden_sasa
+    dm = sasa_dot_map(g, "dodeca_icosa")
+    atoms = W.pack_bodies(np.zeros((2, 3), np.float32), np.array([0, 16], np.uint32))
+    with TypedDotSphereSasa(2, dm, g["radii"], 1.8) as s:
+        with pytest.raises(_lib.ResaxsError) as e:
+            s.counts(atoms)                   # type 16 is outside the 16-type map
+        assert e.value.code == _lib.RSX_INVALID_ARG
+        status = _lib.lib().rsx_sasa_counts(s._h, atoms.reshape(-1), np.ones(2, np.float32),
+                                            np.zeros(2, np.uint32))
+        assert status == _lib.RSX_INVALID_ARG  # unit-form call on a typed handle
+    with pytest.raises(_lib.ResaxsError):
+        TypedDotSphereSasa(2, dm, -g["radii"], 1.8)
