@@ -182,22 +182,59 @@ __global__ void __launch_bounds__(256) noalloc_assemble_kernel(const NoAllocArgs
 }
 
 // Device address of the scratch array, looked up once per device with that
-// device current (the host-side name of a __device__ array is only a stand-in).
+// device current (the host-side name of a __device__ array is only a
+// stand-in), and again when the device's context was recreated since
+// (cudaDeviceReset unloads the module; the array may then sit elsewhere).
+// The context is told apart by its driver-assigned ID, read through the
+// runtime's driver entry points (no link against the driver library).
 static std::mutex g_setup_mu;
 static double *g_scratch_addr[kMaxDevices];
+static unsigned long long g_scratch_ctx[kMaxDevices];
+
+typedef int (*CtxGetCurrentFn)(void **);
+typedef int (*CtxGetIdFn)(void *, unsigned long long *);
+
+// ID of the context current on this thread, 0 when none is current or the
+// driver cannot tell (the address is then looked up again).  Called with
+// g_setup_mu held.
+static unsigned long long current_context_id()
+{
+    static bool looked_up = false;
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    if (!looked_up) {
+        looked_up = true;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", (void **)&get_current, 12000,
+                                             cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            get_current = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", (void **)&get_id, 12000,
+                                             cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            get_id = nullptr;
+    }
+    void *ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current && get_id && get_current(&ctx) == 0 && ctx && get_id(ctx, &id) == 0)
+        return id;
+    return 0;
+}
 
 static rsx_status scratch_address(int dev, double **out)
 {
     if (dev < 0 || dev >= kMaxDevices)
         return fail_static(RSX_INVALID_DEVICE, "device ordinal outside the supported range");
     std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_addr[dev]) {
+    const unsigned long long ctx = current_context_id();
+    if (!g_scratch_addr[dev] || ctx == 0 || ctx != g_scratch_ctx[dev]) {
         void *p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p)
             return fail_static(RSX_CUDA_ERROR,
                                "cudaGetSymbolAddress of the static scratch array failed");
         g_scratch_addr[dev] = static_cast<double *>(p);
+        g_scratch_ctx[dev] = current_context_id(); // the lookup made the context current
     }
     *out = g_scratch_addr[dev];
     return RSX_OK;

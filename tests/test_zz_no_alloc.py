@@ -9,8 +9,10 @@ run stopping at the first failure has run every other test before it.
 
 The test owns its device buffers (allocated here through torch, outside the
 entry point) and checks two calls in a row -- the array keeps the previous
-call's contents -- against the existing entry point, rsx_calc_saxs_curve_status,
-within the 1e-5 relative tolerance of the other parity tests."""
+call's contents -- against the FP64 oracle and the existing entry point,
+rsx_calc_saxs_curve_status, within the 1e-5 relative tolerance of the other
+parity tests; then a problem large enough that the pair sums of one work item
+cover several J blocks (the array would not hold one sum per block pair)."""
 import ctypes
 
 import numpy as np
@@ -52,7 +54,7 @@ def _noalloc_entry(torch, q, bodies, ff):
     return d_o.cpu().numpy()
 
 
-def test_noalloc_matches_existing_entry_twice():
+def test_noalloc_matches_oracle_and_existing_entry_twice(oracle_lib):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
@@ -61,9 +63,34 @@ def test_noalloc_matches_existing_entry_twice():
     second = W.make_config(4, seed=42, n_override=900)      # other q grid, 8 types
     for w in (first, second):
         got = _noalloc_entry(torch, w.q, w.bodies, w.ff)
-        ref = _existing_entry(w.q, w.bodies, w.ff)
         assert np.all(np.isfinite(got))
-        assert rel(got, ref) < TOL
+        assert rel(got, oracle_lib.debye_f64(w.q, w.bodies, w.ff)) < TOL
+        assert rel(got, _existing_entry(w.q, w.bodies, w.ff)) < TOL
+
+
+SCRATCH_DOUBLES = 1048544   # the array's room for partial sums
+
+
+def test_noalloc_several_j_blocks_per_item(oracle_lib):
+    """20,000 bodies and 201 q: one partial sum per block pair would need
+    157 * 158 / 2 * 201 doubles, more than the array holds, so each work item
+    sums a run of J blocks.  Checked against the existing entry on every q and
+    the FP64 oracle on every 8th q."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    torch.cuda.set_device(0)
+    w = W.make_config(2, seed=44)
+    nb = (w.n + 127) // 128
+    assert nb * (nb + 1) // 2 * len(w.q) > SCRATCH_DOUBLES     # the J runs are needed
+    assert nb * len(w.q) <= SCRATCH_DOUBLES                    # and the call is accepted
+    got = _noalloc_entry(torch, w.q, w.bodies, w.ff)
+    assert rel(got, _existing_entry(w.q, w.bodies, w.ff)) < TOL
+    sel = np.arange(0, len(w.q), 8)
+    q64 = w.q.astype(np.float64)
+    dq = (q64[-1] - q64[0]) / (len(q64) - 1)
+    ref = oracle_lib.debye_f64_uniform(q64[0], 8 * dq, len(sel), w.bodies, w.ff[sel])
+    assert rel(got[sel], ref) < TOL
 
 
 def test_noalloc_rejects_oversize_and_bad_types():
