@@ -125,11 +125,13 @@ rsx_status rsx_calc_saxs_curve_status(const float *v_q, int n_q, const rsx_body 
  * held until process exit; problems need ceil(n_bodies/128) * n_q <= 1048544
  * (larger ones are rejected with RSX_INVALID_ARG before any launch).
  * The first call on a device looks up that array's device address (with the
- * device current); make that first call before any stream capture.  Every
- * call reuses the array and leaves its contents behind; calls that overlap on
- * the GPU (several streams, threads or devices sharing a context) race on it
- * and must be serialised by the caller.  Returns after the stream finished
- * the call (the error word of the array is read back). */
+ * device current), and so does the first call after the device's context was
+ * recreated (cudaDeviceReset); make such a first call before any stream
+ * capture.  Every call reuses the array and leaves its contents behind; calls
+ * on the same device that overlap on the GPU (several streams or threads)
+ * race on it and must be serialised by the caller (each device has its own
+ * array).  Returns after the stream finished the call (the error word of the
+ * array is read back with a synchronisation of `stream`). */
 rsx_status rsx_calc_saxs_curve_device_noalloc(const float *d_q, int n_q, const rsx_body *d_bodies,
                                               int n_bodies, const float *d_factors, int n_factors,
                                               float *d_out_iq, void *stream);
@@ -142,9 +144,11 @@ typedef struct rsx_debye rsx_debye;
 
 typedef struct rsx_debye_options {
     int device;          /* CUDA ordinal; -1 = current device */
-    int q_slab;          /* q values per CTA slab: 8, 16, 32, 64 or 128; 0 = tuned / default.
-                            On uniform grids without water 64 and 128 select the
-                            wide slabs (64 or 112 q per recurrence seed). */
+    int q_slab;          /* q values per CTA slab: 8, 16, 32, 64, 128 or 192; 0 = tuned /
+                            default.  On uniform grids 64 and 128 select the wide
+                            slabs (64 to 128 q per recurrence seed), and 192 adds
+                            192-q slabs to the forward without water (2 CTAs/SM);
+                            the other kernels take at most 128. */
     int max_items;       /* cap on forward work items (scratch = items*n_q*8 B); 0 = default */
     int force_general_q; /* 1: never use the uniform-grid recurrence */
     int timing;          /* 1: record CUDA events around the pair kernel */
@@ -293,6 +297,21 @@ rsx_status rsx_sasa_fibonacci_dots(int n_dots, float *out_xyz);
 /* The 32 unit directions of create_dodeca_icosa_dots
  * (rsasa_algorithm.cpp:156-208), the reference GPU path's dot set: 32 x 3. */
 rsx_status rsx_sasa_dodeca_icosa_dots(float *out_xyz);
+
+/* The reference's dot spheres, pre-scaled for one atom radius:
+ * dot_spheres_params::create_dots / create_32_dots / create_fibonacci_dots /
+ * create_dodecahedron_dots / create_dodeca_icosa_dots
+ * (resaxslib/src/rsasa_algorithm.cpp:60-208), the same FP32 values.  Each dot
+ * is x, y, z (on the sphere of radius + probe) and w = radius.  *n_out gets
+ * the set's size; RSX_INVALID_ARG when it exceeds cap (or dot_density < 0 for
+ * the latitude set, whose size is about 4 pi r^2 density). */
+#define RSX_DOTS_LATITUDE 0      /* create_dots: rsasa_cpu_alg's set (density) */
+#define RSX_DOTS_32 1            /* create_32_dots */
+#define RSX_DOTS_FIBONACCI 2     /* create_fibonacci_dots: 64 dots */
+#define RSX_DOTS_DODECAHEDRON 3  /* create_dodecahedron_dots: 20 dots */
+#define RSX_DOTS_DODECA_ICOSA 4  /* create_dodeca_icosa_dots: 32 dots, rsasa_cl_gpu's set */
+rsx_status rsx_sasa_sphere_dots(int kind, float radius, float dot_density, float probe,
+                                float *out_xyzw, int cap, int *n_out);
 
 /* rsasa_cl_gpu::initialize(dot_spheres_cl_params) (rsasa_cl_gpu_alg.cpp:38-57):
  * atom count, unit dot set (n_dots <= 4096, finite) and probe radius fixed

@@ -20,8 +20,10 @@
 
 #include "../rsx.h"
 
+#include <algorithm>
 #include <cstring>
 #include <exception>
+#include <limits>
 #include <memory>
 #include <string>
 #include <vector>
@@ -142,6 +144,35 @@ private:
 };
 
 // i_saxs<float> (resaxslib/include/saxs_algorithm.hpp:147-183) over rsx_debye
+// A typed rsx_sasa handle over the reference's per-type dot spheres for the
+// 16 atomic radii (atomic_form_factors::calc_radii, ff_coef.hpp:164-188),
+// padded with -inf dots as rsasa_cl_gpu::create_sphere_dots pads dots_map_.
+inline rsx_sasa *create_atomic_sasa(int n_atoms, int dot_kind, float dot_density, float probe,
+                                    int device)
+{
+    float radii[16];
+    check(rsx_ff_radii(radii));
+    std::vector<std::vector<float>> sets(16);
+    int stride = 1;
+    for (int t = 0; t < 16; ++t) {
+        int n = 0;
+        const rsx_status st =
+            rsx_sasa_sphere_dots(dot_kind, radii[t], dot_density, probe, nullptr, 0, &n);
+        if (st != RSX_OK && n == 0)
+            check(st);
+        sets[t].resize(4 * (size_t)n);
+        check(rsx_sasa_sphere_dots(dot_kind, radii[t], dot_density, probe, sets[t].data(), n, &n));
+        stride = std::max(stride, n);
+    }
+    const float pad = -std::numeric_limits<float>::infinity();
+    std::vector<float> map(16 * (size_t)stride * 4, pad);
+    for (int t = 0; t < 16; ++t)
+        std::copy(sets[t].begin(), sets[t].end(), map.begin() + (size_t)t * stride * 4);
+    rsx_sasa *h = nullptr;
+    check(rsx_sasa_create_typed(n_atoms, map.data(), 16, stride, radii, probe, device, &h));
+    return h;
+}
+
 template <typename FLT_T = float> class i_saxs {
     static_assert(sizeof(FLT_T) == 4, "librsx computes in FP32 with FP64 reductions");
 
@@ -255,11 +286,12 @@ private:
     // The water term's rsasa, as the reference's GPU algorithm keeps it
     // (saxs_alg_cl_gpu_pt_wf.cpp:82-96, 333-401): with a non-zero water
     // weight every update of the bodies recomputes rsasa from all bodies with
-    // the dot-sphere SASA (32 dodecahedron/icosahedron dots per atom, probe
-    // 1.8 A, the atomic radius of each body's type), unless no_rsasa_recalc_
-    // is set and rsasa values are present.  Values a caller wrote through
-    // access_rsasa() therefore survive only with no_rsasa_recalc_ set (the
-    // reference overwrites them on the first update in any case).
+    // the reference's own OpenCL dot map (rsasa_cl_gpu_alg.cpp:60-89: the
+    // create_dodeca_icosa_dots sphere of each of the 16 atomic radii, probe
+    // 1.8 A), unless no_rsasa_recalc_ is set and rsasa values are present.
+    // Values a caller wrote through access_rsasa() therefore survive only
+    // with no_rsasa_recalc_ set (the reference overwrites them on the first
+    // update in any case).
     void update_rsasa(const std::vector<rsx_body> &bodies, bool moved)
     {
         auto &w = params_.get_implicit_water_params();
@@ -271,23 +303,14 @@ private:
             return;
         require(bodies.size() >= n, error::SAXS_INVALID_ARG,
                 "the water term's SASA needs every body");
-        if (!sasa_) {
-            float dots[32 * 3];
-            check(rsx_sasa_dodeca_icosa_dots(dots));
-            check(rsx_sasa_create((int)n, dots, 32, 1.8f, params_.device_, &sasa_));
-        }
-        float radius_of_type[16];
-        check(rsx_ff_radii(radius_of_type));
-        std::vector<float> radii(n);
-        for (size_t i = 0; i < n; ++i) {
-            const unsigned t = get_factor_index(bodies[i]);
-            require(t < 16, error::SAXS_INVALID_ARG,
+        for (size_t i = 0; i < n; ++i)
+            require(get_factor_index(bodies[i]) < 16, error::SAXS_INVALID_ARG,
                     "the water term's SASA needs an atomic type (0..15) on every body");
-            radii[i] = radius_of_type[t];
-        }
+        if (!sasa_)
+            sasa_ = create_atomic_sasa((int)n, RSX_DOTS_DODECA_ICOSA, 0.f, 1.8f, params_.device_);
         auto &rs = w.access_rsasa(); // marks the water params dirty: pushed next
         rs.resize(n);
-        check(rsx_sasa_calc(sasa_, bodies.data(), radii.data(), rs.data()));
+        check(rsx_sasa_calc_typed(sasa_, bodies.data(), rs.data()));
     }
 
     saxs_params<FLT_T> params_;
@@ -299,8 +322,20 @@ private:
 // create_saxs_ocl<float>() (saxs_algorithm.hpp:240-244) counterpart
 inline std::unique_ptr<i_saxs<float>> create_saxs_gpu() { return std::make_unique<i_saxs<float>>(); }
 
-// i_rsasa<float> (resaxslib/include/rsasa_algorithm.hpp:42-61) over rsx_sasa,
-// with one radius per body type as the reference (rsasa_cl_gpu_alg.cpp:139-151).
+// i_rsasa<float> (resaxslib/include/rsasa_algorithm.hpp:42-61) over rsx_sasa.
+// initialize(n_atoms, dot_spheres_params) builds the reference's own per-type
+// dot map for the 16 atomic radii (atomic_form_factors::calc_radii): the
+// create_dodeca_icosa_dots spheres of rsasa_cl_gpu (rsasa_cl_gpu_alg.cpp:60-89)
+// by default, or the create_dots spheres of rsasa_cpu_alg
+// (rsasa_cpu_alg.cpp:46-61) with RSX_DOTS_LATITUDE.  The other initialize()
+// takes one unit dot set and a radius per body type.
+struct dot_spheres_params {
+    float dot_density = 0.f;  // dots per A^2 (create_dots)
+    float probe_radius = 0.f;
+    dot_spheres_params() = default;
+    dot_spheres_params(float density, float probe) : dot_density(density), probe_radius(probe) {}
+};
+
 class rsasa_gpu {
 public:
     ~rsasa_gpu()
@@ -308,16 +343,21 @@ public:
         if (h_)
             rsx_sasa_destroy(h_);
     }
+    void initialize(unsigned n_atoms, const dot_spheres_params &p,
+                    int dot_kind = RSX_DOTS_DODECA_ICOSA, int device = -1)
+    {
+        release();
+        h_ = create_atomic_sasa((int)n_atoms, dot_kind, p.dot_density, p.probe_radius, device);
+        typed_ = true;
+    }
     void initialize(unsigned n_atoms, const std::vector<float> &radius_of_type, float probe_radius,
                     const std::vector<float> &unit_dots, int device = -1)
     {
-        if (h_)
-            rsx_sasa_destroy(h_);
-        h_ = nullptr;
+        release();
         radii_ = radius_of_type;
         check(rsx_sasa_create((int)n_atoms, unit_dots.data(), (int)(unit_dots.size() / 3),
                               probe_radius, device, &h_));
-        n_ = n_atoms;
+        typed_ = false;
     }
     void calc_rsasa(const std::vector<rsx_body> &atoms, std::vector<float> &rsasa)
     {
@@ -325,14 +365,18 @@ public:
             throw error(error::SAXS_ARGS_NOT_SET, "initialize() was not called");
         if (rsasa.size() < atoms.size())
             throw error(error::SAXS_INVALID_ARG, "rsasa vector too small");
-        std::vector<float> r(atoms.size());
-        for (size_t i = 0; i < atoms.size(); ++i) {
-            const unsigned t = get_factor_index(atoms[i]);
-            if (t >= radii_.size())
-                throw error(error::SAXS_INVALID_ARG, "atom type without a radius");
-            r[i] = radii_[t];
+        if (typed_) {
+            check(rsx_sasa_calc_typed(h_, atoms.data(), rsasa.data()));
+        } else {
+            std::vector<float> r(atoms.size());
+            for (size_t i = 0; i < atoms.size(); ++i) {
+                const unsigned t = get_factor_index(atoms[i]);
+                if (t >= radii_.size())
+                    throw error(error::SAXS_INVALID_ARG, "atom type without a radius");
+                r[i] = radii_[t];
+            }
+            check(rsx_sasa_calc(h_, atoms.data(), r.data(), rsasa.data()));
         }
-        check(rsx_sasa_calc(h_, atoms.data(), r.data(), rsasa.data()));
         computing_ = true;
     }
     void recalc_rsasa(const std::vector<rsx_body> &atoms, std::vector<float> &rsasa)
@@ -343,9 +387,16 @@ public:
     }
 
 private:
+    void release()
+    {
+        if (h_)
+            rsx_sasa_destroy(h_);
+        h_ = nullptr;
+        computing_ = false;
+    }
     rsx_sasa *h_ = nullptr;
-    unsigned n_ = 0;
     std::vector<float> radii_;
+    bool typed_ = false;
     bool computing_ = false;
 };
 

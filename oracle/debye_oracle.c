@@ -519,6 +519,8 @@ typedef struct {
     int next_row;
     pthread_mutex_t mu;
     double *grad;
+    const int *rows;  /* NULL: every body; else grad row r belongs to body rows[r] */
+    int n_rows;
 } grad_job;
 
 typedef struct {
@@ -528,12 +530,14 @@ typedef struct {
 static void *grad_worker(void *p)
 {
     grad_job *J = ((grad_arg *)p)->job;
+    const int limit = J->rows ? J->n_rows : J->n;
     for (;;) {
         int b;
-        int e = grab_rows(&J->mu, &J->next_row, J->n, 8, &b);
+        int e = grab_rows(&J->mu, &J->next_row, limit, J->rows ? 1 : 8, &b);
         if (b >= e)
             break;
-        for (int i = b; i < e; ++i) {
+        for (int row = b; row < e; ++row) {
+            const int i = J->rows ? J->rows[row] : row;
             const float *pi = &J->bodies[4 * i];
             double g[3] = {0.0, 0.0, 0.0};
             for (int j = 0; j < J->n; ++j) {
@@ -560,18 +564,18 @@ static void *grad_worker(void *p)
                 g[1] += G * d[1];
                 g[2] += G * d[2];
             }
-            J->grad[3 * i + 0] = g[0];
-            J->grad[3 * i + 1] = g[1];
-            J->grad[3 * i + 2] = g[2];
+            J->grad[3 * row + 0] = g[0];
+            J->grad[3 * row + 1] = g[1];
+            J->grad[3 * row + 2] = g[2];
         }
     }
     return NULL;
 }
 
-void orc_debye_grad_f64(const double *q, int n_q, const double *w_q,
-                        const float *bodies, int n_bodies, const float *ff,
-                        int n_factors, const float *rsasa, double water_weight,
-                        int water_index, double *grad, int n_threads)
+static void grad_run(const double *q, int n_q, const double *w_q, const float *bodies,
+                     int n_bodies, const float *ff, int n_factors, const float *rsasa,
+                     double water_weight, int water_index, const int *rows, int n_rows,
+                     double *grad, int n_threads)
 {
     int nt = pick_threads(n_threads);
     double *f = (double *)malloc(sizeof(double) * (size_t)n_q * n_bodies);
@@ -588,6 +592,8 @@ void orc_debye_grad_f64(const double *q, int n_q, const double *w_q,
     J.f = f;
     J.next_row = 0;
     J.grad = grad;
+    J.rows = rows;
+    J.n_rows = n_rows;
     pthread_mutex_init(&J.mu, NULL);
     pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nt);
     grad_arg *args = (grad_arg *)malloc(sizeof(grad_arg) * nt);
@@ -600,6 +606,120 @@ void orc_debye_grad_f64(const double *q, int n_q, const double *w_q,
     pthread_mutex_destroy(&J.mu);
     free(th);
     free(args);
+    free(f);
+}
+
+void orc_debye_grad_f64(const double *q, int n_q, const double *w_q,
+                        const float *bodies, int n_bodies, const float *ff,
+                        int n_factors, const float *rsasa, double water_weight,
+                        int water_index, double *grad, int n_threads)
+{
+    grad_run(q, n_q, w_q, bodies, n_bodies, ff, n_factors, rsasa, water_weight, water_index,
+             NULL, 0, grad, n_threads);
+}
+
+void orc_debye_grad_rows_f64(const double *q, int n_q, const double *w_q,
+                             const float *bodies, int n_bodies, const float *ff,
+                             int n_factors, const int *rows, int n_rows, double *grad,
+                             int n_threads)
+{
+    grad_run(q, n_q, w_q, bodies, n_bodies, ff, n_factors, NULL, 0.0, 0, rows, n_rows, grad,
+             n_threads);
+}
+
+/* Central differences of L = sum_q w_q I(q) along single coordinates: only
+ * the pairs of the moved body change, so
+ *   L(x+) - L(x-) = sum_q w_q 2 f_i(q) sum_{j != i} f_j(q)
+ *                   [sinc(q |p_j - p_i(x+)|) - sinc(q |p_j - p_i(x-)|)]
+ * (host_debye.cpp:74-108 restricted to row i), in FP64 with libm sin. */
+typedef struct {
+    const double *q, *w;
+    int n_q;
+    const float *bodies;
+    int n;
+    const double *f;
+    const int *atom, *axis;
+    const float *plus, *minus;
+    int n_coords, next;
+    pthread_mutex_t mu;
+    double *out;
+} fd_job;
+
+static void *fd_worker(void *p)
+{
+    fd_job *J = (fd_job *)p;
+    for (;;) {
+        int c;
+        pthread_mutex_lock(&J->mu);
+        c = J->next++;
+        pthread_mutex_unlock(&J->mu);
+        if (c >= J->n_coords)
+            break;
+        const int i = J->atom[c], ax = J->axis[c];
+        double pp[3], pm[3];
+        for (int a = 0; a < 3; ++a)
+            pp[a] = pm[a] = J->bodies[4 * i + a];
+        pp[ax] = J->plus[c];
+        pm[ax] = J->minus[c];
+        double dl = 0.0;
+        for (int j = 0; j < J->n; ++j) {
+            if (j == i)
+                continue;
+            const float *pj = &J->bodies[4 * j];
+            double a2 = 0.0, b2 = 0.0;
+            for (int a = 0; a < 3; ++a) {
+                const double da = pp[a] - pj[a], db = pm[a] - pj[a];
+                a2 += da * da;
+                b2 += db * db;
+            }
+            const double ra = sqrt(a2), rb = sqrt(b2);
+            double s = 0.0;
+            for (int k = 0; k < J->n_q; ++k) {
+                const double qk = J->q[k];
+                const double xa = qk * ra, xb = qk * rb;
+                const double sa = xa == 0.0 ? 1.0 : sin(xa) / xa;
+                const double sb = xb == 0.0 ? 1.0 : sin(xb) / xb;
+                s += J->w[k] * J->f[(size_t)k * J->n + i] * J->f[(size_t)k * J->n + j] * (sa - sb);
+            }
+            dl += 2.0 * s;
+        }
+        J->out[c] = dl / ((double)J->plus[c] - (double)J->minus[c]);
+    }
+    return NULL;
+}
+
+void orc_debye_fd_f64(const double *q, int n_q, const double *w_q, const float *bodies,
+                      int n_bodies, const float *ff, int n_factors, const int *atom,
+                      const int *axis, const float *plus, const float *minus, int n_coords,
+                      double *out, int n_threads)
+{
+    int nt = pick_threads(n_threads);
+    double *f = (double *)malloc(sizeof(double) * (size_t)n_q * n_bodies);
+    for (int k = 0; k < n_q; ++k)
+        for (int i = 0; i < n_bodies; ++i)
+            f[(size_t)k * n_bodies + i] = ff[(size_t)k * n_factors + body_type(bodies, i)];
+    fd_job J;
+    J.q = q;
+    J.w = w_q;
+    J.n_q = n_q;
+    J.bodies = bodies;
+    J.n = n_bodies;
+    J.f = f;
+    J.atom = atom;
+    J.axis = axis;
+    J.plus = plus;
+    J.minus = minus;
+    J.n_coords = n_coords;
+    J.next = 0;
+    J.out = out;
+    pthread_mutex_init(&J.mu, NULL);
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nt);
+    for (int t = 0; t < nt; ++t)
+        pthread_create(&th[t], NULL, fd_worker, &J);
+    for (int t = 0; t < nt; ++t)
+        pthread_join(th[t], NULL);
+    pthread_mutex_destroy(&J.mu);
+    free(th);
     free(f);
 }
 

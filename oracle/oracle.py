@@ -69,6 +69,10 @@ def lib():
         L.orc_sin_probe.restype = d
         L.orc_debye_f64_uniform.argtypes = [d, d, i, _f32p, i, _f32p, i, _f64p, i]
         L.orc_debye_grad_f64.argtypes = [_f64p, i, _f64p, _f32p, i, _f32p, i, vp, d, i, _f64p, i]
+        L.orc_debye_grad_rows_f64.argtypes = [_f64p, i, _f64p, _f32p, i, _f32p, i, _i32p, i,
+                                              _f64p, i]
+        L.orc_debye_fd_f64.argtypes = [_f64p, i, _f64p, _f32p, i, _f32p, i, _i32p, _i32p,
+                                       _f32p, _f32p, i, _f64p, i]
         L.orc_refport_host_debye.argtypes = [_f32p, i, _f32p, i, _f32p, i, _f32p]
         L.orc_refport_host_debye_mt.argtypes = [_f32p, i, _f32p, i, _f32p, i, _f32p, i]
         L.orc_refport_host_debye_mt.restype = d
@@ -191,6 +195,37 @@ def debye_grad_f64(q, w_q, bodies, ff, rsasa=None, water_weight=0.0, water_index
                              ff.shape[1], rs, float(water_weight), int(water_index),
                              grad.reshape(-1), int(threads))
     return grad
+
+
+def debye_grad_rows_f64(q, w_q, bodies, ff, rows, threads=0):
+    """FP64 gradient rows of L = sum_q w_q I(q) for the bodies ``rows``."""
+    q = _c(q, np.float64)
+    w_q = _c(w_q, np.float64)
+    bodies = _c(bodies, np.float32)
+    ff = _c(ff, np.float32)
+    rows = _c(rows, np.int32)
+    grad = np.zeros((len(rows), 3), np.float64)
+    lib().orc_debye_grad_rows_f64(q, len(q), w_q, bodies.reshape(-1), len(bodies), ff.reshape(-1),
+                                  ff.shape[1], rows, len(rows), grad.reshape(-1), int(threads))
+    return grad
+
+
+def debye_fd_f64(q, w_q, bodies, ff, coords, h=1e-4, threads=0):
+    """FP64 central differences of L = sum_q w_q I(q) along the (body, axis)
+    pairs ``coords``, with the FP32-represented steps x +/- h as divisor."""
+    q = _c(q, np.float64)
+    w_q = _c(w_q, np.float64)
+    bodies = _c(bodies, np.float32)
+    ff = _c(ff, np.float32)
+    atom = _c([c[0] for c in coords], np.int32)
+    axis = _c([c[1] for c in coords], np.int32)
+    x = bodies[atom, axis].astype(np.float64)
+    plus = _c(x + h, np.float32)
+    minus = _c(x - h, np.float32)
+    out = np.zeros(len(coords), np.float64)
+    lib().orc_debye_fd_f64(q, len(q), w_q, bodies.reshape(-1), len(bodies), ff.reshape(-1),
+                           ff.shape[1], atom, axis, plus, minus, len(coords), out, int(threads))
+    return out
 
 
 def refport_host_debye(q, bodies, ff, threads=1):

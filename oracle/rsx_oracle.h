@@ -57,6 +57,22 @@ void orc_debye_grad_f64(const double *q, int n_q, const double *w_q,
                         int n_factors, const float *rsasa, double water_weight,
                         int water_index, double *grad, int n_threads);
 
+/* The same gradient for the bodies rows[0..n_rows) only (no water):
+ * grad is [n_rows][3], row r for body rows[r]. */
+void orc_debye_grad_rows_f64(const double *q, int n_q, const double *w_q,
+                             const float *bodies, int n_bodies, const float *ff,
+                             int n_factors, const int *rows, int n_rows, double *grad,
+                             int n_threads);
+
+/* FP64 central differences of L = sum_q w_q I(q): out[c] = (L with body
+ * atom[c]'s coordinate axis[c] set to plus[c] - L with it set to minus[c]) /
+ * (plus[c] - minus[c]), from the pairs of that body only (the rest of the
+ * sum of host_debye.cpp:74-108 cancels), libm sin per term (no water). */
+void orc_debye_fd_f64(const double *q, int n_q, const double *w_q, const float *bodies,
+                      int n_bodies, const float *ff, int n_factors, const int *atom,
+                      const int *axis, const float *plus, const float *minus, int n_coords,
+                      double *out, int n_threads);
+
 /* Reference-faithful port of host_debye<double,float,cl_float4>::calc_curve
  * (host_debye.cpp:54-109): same N*N distance matrix, same loop order, same
  * mixed float/double arithmetic.  Single threaded, exactly as the reference.

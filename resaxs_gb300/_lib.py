@@ -111,6 +111,8 @@ SIGNATURES = [
     ("rsx_sasa_fibonacci_dots", _st, [_i, _f32p]),
     ("rsx_sasa_dodeca_icosa_dots", _st, [_f32p]),
     ("rsx_sasa_create", _st, [_i, _f32p, _i, ctypes.c_float, _i, ctypes.POINTER(_vp)]),
+    ("rsx_sasa_sphere_dots", _st, [_i, ctypes.c_float, ctypes.c_float, ctypes.c_float, _f32p,
+                              _i, ctypes.POINTER(_i)]),
     ("rsx_sasa_create_typed", _st, [_i, _f32p, _i, _i, _f32p, ctypes.c_float, _i,
                                ctypes.POINTER(_vp)]),
     ("rsx_sasa_counts_typed", _st, [_vp, _f32p, _u32p]),

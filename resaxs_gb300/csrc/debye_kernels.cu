@@ -42,9 +42,10 @@ __global__ void __launch_bounds__(kBlockAtoms) forward_kernel(const DebyeArgs a)
     forward_item<QS, UNIFORM, WATER>(a, blockIdx.x, a.k_base + blockIdx.y * QS);
 }
 
-// up to 64 q: <= 168 registers, 3 CTAs per SM; wider: <= 255, 2 CTAs per SM
+// up to 64 q, and plain up to 128 q: <= 168 registers, 3 CTAs per SM; wider
+// (signed above 64 q, every instantiation above 128 q): <= 255, 2 CTAs per SM
 template <int QS, int IL, bool SIGNED>
-__global__ void __launch_bounds__(kBlockAtoms, (QS <= 64 || !SIGNED) ? 3 : 2)
+__global__ void __launch_bounds__(kBlockAtoms, (QS <= 64 || (!SIGNED && QS <= 128)) ? 3 : 2)
     forward_wide_kernel(const DebyeArgs a)
 {
     forward_wide_item<QS, IL, SIGNED>(a, blockIdx.x, a.k_base + blockIdx.y * QS);
@@ -384,6 +385,17 @@ static cudaError_t wide_launch(DebyeArgs a, int k_base, int n_slabs, bool water,
 {
     a.k_base = k_base;
     const dim3 grid(a.n_items, n_slabs);
+    if constexpr (QS > 128) {
+        // no water instantiation this wide (its per-q factor rows would spill)
+        if (water)
+            return cudaErrorInvalidValue;
+        if (a.small_theta >= 2)
+            forward_wide_kernel<QS, 2, false><<<grid, kBlockAtoms, 0, st>>>(a);
+        else
+            forward_wide_kernel<QS, 2, true><<<grid, kBlockAtoms, 0, st>>>(a);
+        count_launch();
+        return cudaGetLastError();
+    }
     if (water && a.small_theta >= 2)
         forward_wide_water_kernel<QS, false><<<grid, kBlockAtoms, 0, st>>>(a);
     else if (water)
@@ -403,6 +415,8 @@ static cudaError_t wide_launch(DebyeArgs a, int k_base, int n_slabs, bool water,
 // steps, so short slabs are dear per q (the 48-q slab measured slower than
 // the 64-q one, which therefore also serves remainders of 33..48 q).
 static constexpr float kCostMain64 = 1.82f, kCostMain112 = 2.75f, kCostMain128 = 3.00f;
+// the 192-q slab (2 CTAs/SM), relative to the same scale
+static constexpr float kCostMain192 = 4.30f;
 static constexpr float kCostWidth[8] = {0.99f, 1.35f, 2.34f, 1.82f, 2.13f, 2.29f, 2.75f, 3.00f};
 
 // Width (multiple of 16, <= 128) of the cheapest slab that covers len q.
@@ -461,6 +475,11 @@ WidePlan wide_plan(int n_q, int q_slab)
         const int f128 = n_q / 128, r128 = n_q - 128 * f128;
         consider(128, f128, r128, f128 * kCostMain128 + tail_cost(r128));
     }
+    if (q_slab >= 192) {
+        const int f192 = n_q / 192, r192 = n_q - 192 * f192;
+        if (f192 > 0)
+            consider(192, f192, r192, f192 * kCostMain192 + tail_cost(r192));
+    }
     return best;
 }
 
@@ -470,7 +489,7 @@ WidePlan wide_plan(int n_q, int q_slab)
 static cudaError_t launch_forward_wide(const DebyeArgs &a, int q_slab, bool water, cudaStream_t st,
                                        const AuxStream *aux)
 {
-    const WidePlan p = wide_plan(a.n_q, q_slab);
+    const WidePlan p = wide_plan(a.n_q, water ? std::min(q_slab, 128) : q_slab);
     const bool split = aux && p.full > 0 && p.tail_len > 0;
     if (split) {
         cudaError_t e = cudaEventRecord(aux->fork, st);
@@ -483,6 +502,7 @@ static cudaError_t launch_forward_wide(const DebyeArgs &a, int q_slab, bool wate
         cudaError_t e;
         e = p.main == 64    ? wide_launch<64>(a, 0, p.full, water, st)
             : p.main == 112 ? wide_launch<112>(a, 0, p.full, water, st)
+            : p.main == 192 ? wide_launch<192>(a, 0, p.full, water, st)
                             : wide_launch<128>(a, 0, p.full, water, st);
         if (e != cudaSuccess)
             return e;

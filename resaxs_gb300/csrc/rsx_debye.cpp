@@ -271,7 +271,7 @@ bool has_water(const rsx_debye *h) { return h->water_weight != 0.f; }
 // forward): water keeps two accumulator sets in registers there.
 int slab_for(const rsx_debye *h)
 {
-    int qs = h->q_slab;
+    int qs = std::min(h->q_slab, 128); // 192 selects the wider forward slabs only
     if (has_water(h) && qs > 16)
         qs = 16;
     if (!h->uniform && qs > 32)
@@ -809,8 +809,8 @@ rsx_status rsx_debye_create(const float *q, int n_q, const float *t_factors, int
     if (opts)
         o = *opts;
     if (o.q_slab != 0 && o.q_slab != 8 && o.q_slab != 16 && o.q_slab != 32 && o.q_slab != 64 &&
-        o.q_slab != 128)
-        return fail(RSX_INVALID_ARG, "q_slab must be 0, 8, 16, 32, 64 or 128");
+        o.q_slab != 128 && o.q_slab != 192)
+        return fail(RSX_INVALID_ARG, "q_slab must be 0, 8, 16, 32, 64, 128 or 192");
     int dev = -1;
     RSX_TRY(select_device(o.device, &dev));
     DeviceGuard g(dev);

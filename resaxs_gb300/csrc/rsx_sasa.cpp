@@ -380,6 +380,102 @@ rsx_status rsx_sasa_dodeca_icosa_dots(float *out_xyz)
     return ok();
 }
 
+rsx_status rsx_sasa_sphere_dots(int kind, float radius, float dot_density, float probe,
+                                float *out_xyzw, int cap, int *n_out)
+{
+    // dot_spheres_params::create_* (rsasa_algorithm.cpp:60-208) in FLT_T =
+    // float, operation for operation: the dots are pre-scaled by
+    // ext = radius + probe and carry the radius in w.
+    if (!n_out || (!out_xyzw && cap > 0) || cap < 0)
+        return fail(RSX_INVALID_ARG, "null output");
+    *n_out = 0;
+    if (!std::isfinite(radius) || !std::isfinite(probe) || !std::isfinite(dot_density))
+        return fail(RSX_INVALID_ARG, "radius, probe and density must be finite");
+    const float pi_f = (float)3.14159265358979323846;
+    const float ext = radius + probe;
+    std::vector<float4> d;
+    auto sphere = [&](float n_sect) { // create_sphere_dots (:38-58)
+        const float n_vert_sect = 0.5f * n_sect;
+        for (unsigned i = 0; (float)i < n_vert_sect; i++) {
+            const float phi = (pi_f * (float)i) / n_vert_sect;
+            const float z = std::cos(phi) * ext;
+            const float xy = std::sin(phi);
+            const float horz_count = xy * n_sect;
+            for (unsigned j = 0; (float)j < horz_count - 1; j++) {
+                const float theta = (2 * pi_f * (float)j) / horz_count;
+                const float x = xy * std::cos(theta) * ext;
+                const float y = xy * std::sin(theta) * ext;
+                d.push_back(make_float4(x, y, z, radius));
+                if (d.size() > (size_t)1 << 20)
+                    return false;
+            }
+        }
+        return true;
+    };
+    const float phi = (1.0f + std::sqrt(5.0f)) / 2.0f;
+    switch (kind) {
+    case RSX_DOTS_LATITUDE: {
+        // create_dots (:60-65): n_sect = 2 pi r sqrt(density)
+        if (!(dot_density >= 0.f))
+            return fail(RSX_INVALID_ARG, "dot density must be >= 0");
+        const float n_sect = 2 * pi_f * radius * std::sqrt(dot_density);
+        if (!sphere(n_sect))
+            return fail(RSX_INVALID_ARG, "more than 2^20 dots");
+        break;
+    }
+    case RSX_DOTS_32:
+        sphere(10.5f); // create_32_dots (:67-71)
+        break;
+    case RSX_DOTS_FIBONACCI: { // create_fibonacci_dots (:96-116)
+        const int n = 32;
+        for (int i = -(n - 1); i <= n; ++i) {
+            const float theta = 2 * pi_f * i / phi;
+            const float sphi = static_cast<float>(i) / n;
+            const float cphi = static_cast<float>(std::sqrt((double)((n + i) * (n - i))) / n);
+            d.push_back(make_float4(cphi * std::sin(theta) * ext, cphi * std::cos(theta) * ext,
+                                    sphi * ext, radius));
+        }
+        break;
+    }
+    case RSX_DOTS_DODECAHEDRON:
+    case RSX_DOTS_DODECA_ICOSA: { // (:118-154), (:156-208)
+        const float r_phi = 1 / phi;
+        const float r_sqrt3 = 1 / std::sqrt(3.0f);
+        const float v1 = r_sqrt3 * ext, v2 = r_phi * v1, v3 = phi * v1;
+        const float dod[20][3] = {
+            {v1, v1, v1},  {v1, v1, -v1},  {v1, -v1, v1},  {v1, -v1, -v1}, {-v1, v1, v1},
+            {-v1, v1, -v1}, {-v1, -v1, v1}, {-v1, -v1, -v1}, {0, v2, v3},   {0, v2, -v3},
+            {0, -v2, v3},  {0, -v2, -v3},  {v2, v3, 0},    {v2, -v3, 0},   {-v2, v3, 0},
+            {-v2, -v3, 0}, {v3, 0, v2},    {v3, 0, -v2},   {-v3, 0, v2},   {-v3, 0, -v2}};
+        for (const auto &v : dod)
+            d.push_back(make_float4(v[0], v[1], v[2], radius));
+        if (kind == RSX_DOTS_DODECA_ICOSA) {
+            const double pi = 3.14159265358979323846;
+            const float ico = (float)((std::sqrt(5.0f) + 5) / 10 /
+                                      std::sqrt(3 - 1 / std::pow(phi * std::cos(3 * pi / 10), 2)) *
+                                      ext);
+            const float pi_c = phi * ico;
+            const float ic[12][3] = {{ico, 0, pi_c},  {ico, 0, -pi_c}, {-ico, 0, pi_c},
+                                     {-ico, 0, -pi_c}, {0, pi_c, ico},  {0, pi_c, -ico},
+                                     {0, -pi_c, ico}, {0, -pi_c, -ico}, {pi_c, ico, 0},
+                                     {pi_c, -ico, 0}, {-pi_c, ico, 0}, {-pi_c, -ico, 0}};
+            for (const auto &v : ic)
+                d.push_back(make_float4(v[0], v[1], v[2], radius));
+        }
+        break;
+    }
+    default:
+        return fail(RSX_INVALID_ARG, "unknown dot set kind");
+    }
+    *n_out = (int)d.size();
+    if ((int)d.size() > cap)
+        return fail(RSX_INVALID_ARG, "output holds " + std::to_string(cap) + " dots, the set has " +
+                                         std::to_string(d.size()));
+    if (!d.empty())
+        std::memcpy(out_xyzw, d.data(), sizeof(float4) * d.size());
+    return ok();
+}
+
 rsx_status rsx_sasa_create(int n_atoms, const float *unit_dots, int n_dots, float probe,
                            int device, rsx_sasa **out)
 {

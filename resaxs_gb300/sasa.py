@@ -13,13 +13,42 @@ from . import _lib
 from ._lib import ResaxsError, check, lib
 
 __all__ = ["DotSphereSasa", "TypedDotSphereSasa", "RsasaAlgorithm", "fibonacci_dots",
-           "dodeca_icosa_dots", "dot_map_from_sets"]
+           "dodeca_icosa_dots", "dot_map_from_sets", "sphere_dots", "reference_dot_map"]
 
 
 def fibonacci_dots(n_dots: int) -> np.ndarray:
     out = np.zeros((n_dots, 3), np.float32)
     check(lib().rsx_sasa_fibonacci_dots(int(n_dots), out.reshape(-1)))
     return out
+
+
+DOT_KINDS = {"latitude": 0, "32": 1, "fibonacci": 2, "dodecahedron": 3, "dodeca_icosa": 4}
+
+
+def sphere_dots(kind: str, radius: float, probe: float, dot_density: float = 0.0) -> np.ndarray:
+    """The reference's dot sphere for one radius ((n, 4) float32: x, y, z on
+    the sphere of radius + probe, w = radius): dot_spheres_params::create_*."""
+    cap = 8192
+    while True:
+        out = np.zeros((cap, 4), np.float32)
+        n = ctypes.c_int()
+        st = lib().rsx_sasa_sphere_dots(DOT_KINDS[kind], ctypes.c_float(radius),
+                                        ctypes.c_float(dot_density), ctypes.c_float(probe),
+                                        out.reshape(-1), cap, ctypes.byref(n))
+        if st == 0:
+            return out[: n.value].copy()
+        if n.value > cap:
+            cap = n.value
+            continue
+        check(st)
+
+
+def reference_dot_map(type_radii, kind: str, probe: float, dot_density: float = 0.0) -> np.ndarray:
+    """Per-type pre-scaled dot map ((n_types, stride, 4), -inf padding) built
+    the way the reference builds dots_map_ (rsasa_cl_gpu_alg.cpp:60-89) or
+    its per-type sets (rsasa_cpu_alg.cpp:46-61)."""
+    return dot_map_from_sets([sphere_dots(kind, float(r), probe, dot_density)
+                              for r in np.asarray(type_radii, np.float32)])
 
 
 def dodeca_icosa_dots() -> np.ndarray:
@@ -167,20 +196,39 @@ class TypedDotSphereSasa:
 
 class RsasaAlgorithm:
     """Mirror of ``i_rsasa<float>``: ``initialize(params)`` then
-    ``calc_rsasa(atoms, rsasa)`` / ``recalc_rsasa(atoms, rsasa)``.  Radii come
-    from ``radius_of_type`` (one radius per body type index in atoms[:, 3])."""
+    ``calc_rsasa(atoms, rsasa)`` / ``recalc_rsasa(atoms, rsasa)``.
+
+    ``initialize(n_atoms, dot_density=..., probe_radius=...)`` uses the
+    reference's own per-type dot spheres for the 16 atomic radii
+    (``dot_kind="dodeca_icosa"``: rsasa_cl_gpu's map, rsasa_cl_gpu_alg.cpp:60-89;
+    ``"latitude"``: rsasa_cpu_alg's create_dots sets, rsasa_cpu_alg.cpp:46-61).
+    With ``radius_of_type`` it uses one unit dot set (``unit_dots`` or
+    ``n_dots`` Fibonacci dots) and a radius per body type instead."""
 
     def __init__(self):
         self._s = None
+        self._typed = False
         self._computing = False
 
-    def initialize(self, n_atoms: int, radius_of_type, probe_radius: float = 1.4,
-                   unit_dots=None, n_dots: int = 960, device: int = -1):
-        self.radius_of_type = np.asarray(radius_of_type, np.float32)
+    def initialize(self, n_atoms: int, radius_of_type=None, probe_radius: float = 1.4,
+                   unit_dots=None, n_dots: int = 960, device: int = -1,
+                   dot_density: float = 0.0, dot_kind: str = "dodeca_icosa"):
         if self._s is not None:
             self._s.close()
-        self._s = DotSphereSasa(n_atoms, n_dots=n_dots, probe=probe_radius, unit_dots=unit_dots,
-                                device=device)
+        self._s = None
+        self._computing = False
+        if radius_of_type is None:
+            radii = np.zeros(16, np.float32)
+            check(lib().rsx_ff_radii(radii))
+            self._s = TypedDotSphereSasa(n_atoms, reference_dot_map(radii, dot_kind, probe_radius,
+                                                                    dot_density),
+                                         radii, probe_radius, device=device)
+            self._typed = True
+        else:
+            self.radius_of_type = np.asarray(radius_of_type, np.float32)
+            self._s = DotSphereSasa(n_atoms, n_dots=n_dots, probe=probe_radius,
+                                    unit_dots=unit_dots, device=device)
+            self._typed = False
 
     def _radii(self, atoms):
         types = np.ascontiguousarray(atoms, np.float32).view(np.uint32)[:, 3]
@@ -193,7 +241,10 @@ class RsasaAlgorithm:
             raise ResaxsError(_lib.RSX_ARGS_NOT_SET, "initialize() was not called")
         if rsasa is not None and len(rsasa) < len(atoms):
             raise ResaxsError(_lib.RSX_INVALID_ARG, "rsasa vector too small")
-        res = self._s.rsasa(atoms, self._radii(atoms))
+        if self._typed:
+            res = self._s.rsasa(atoms)
+        else:
+            res = self._s.rsasa(atoms, self._radii(atoms))
         self._computing = True
         if rsasa is not None:
             rsasa[: len(res)] = res

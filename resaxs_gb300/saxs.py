@@ -336,9 +336,9 @@ class SaxsAlgorithm:
         """The water term's rsasa as the reference's GPU algorithm keeps it
         (saxs_alg_cl_gpu_pt_wf.cpp:82-96, 333-401): with a non-zero water weight
         every update of the bodies recomputes rsasa from all bodies with the
-        dot-sphere SASA (32 dodecahedron/icosahedron dots, probe 1.8 A, the
-        atomic radius of each body's type), unless ``no_rsasa_recalc`` is set
-        and rsasa values are present."""
+        reference's own OpenCL dot map (the create_dodeca_icosa_dots sphere of
+        each of the 16 atomic radii, probe 1.8 A, rsasa_cl_gpu_alg.cpp:60-89),
+        unless ``no_rsasa_recalc`` is set and rsasa values are present."""
         w = self._params.get_implicit_water_params()
         if w.water_weight == 0:
             return
@@ -346,7 +346,7 @@ class SaxsAlgorithm:
         present = w.rsasa is not None and len(w.rsasa) >= n
         if present and (w.no_rsasa_recalc or not moved):
             return
-        from .sasa import DotSphereSasa, dodeca_icosa_dots
+        from .sasa import TypedDotSphereSasa, reference_dot_map
         bodies = np.ascontiguousarray(bodies, np.float32).reshape(-1, 4)
         if len(bodies) < n:
             raise ResaxsError(_lib.RSX_INVALID_ARG, "the water term's SASA needs every body")
@@ -354,13 +354,13 @@ class SaxsAlgorithm:
         if types.size and types.max() >= 16:
             raise ResaxsError(_lib.RSX_INVALID_ARG,
                               "the water term's SASA needs an atomic type (0..15) on every body")
-        radii = np.zeros(16, np.float32)
-        check(lib().rsx_ff_radii(radii))
         if self._sasa is None:
-            self._sasa = DotSphereSasa(n, unit_dots=dodeca_icosa_dots(), probe=1.8,
-                                       device=self._params.device)
+            radii = np.zeros(16, np.float32)
+            check(lib().rsx_ff_radii(radii))
+            self._sasa = TypedDotSphereSasa(n, reference_dot_map(radii, "dodeca_icosa", 1.8),
+                                            radii, 1.8, device=self._params.device)
         w.access_rsasa()
-        w.rsasa = self._sasa.rsasa(bodies[:n], radii[types])
+        w.rsasa = self._sasa.rsasa(bodies[:n])
 
     @staticmethod
     def _emit(out, values):

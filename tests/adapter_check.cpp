@@ -11,7 +11,7 @@
 //                float q[n_q], factors[n_q][n_types], bodies[n][4], rsasa[n],
 //                radius_of_type[n_types]
 //       out.bin: float curves[8][n_q], then float rsasa_out[n],
-//                water_rsasa[n], water_rsasa_moved[n]
+//                water_rsasa[n], water_rsasa_moved[n], typed_rsasa[n]
 //         0 calc_curve(bodies)
 //         1 recalc_curve after bodies [start, start+length) moved by +0.3 A in x
 //         2 after revert() to the committed state of curve 0, recalc_curve
@@ -25,6 +25,9 @@
 //         7 then recalc_curve of the +0.3 A bodies: rsasa recomputed
 //           (water_rsasa_moved)
 //       rsasa_out: calc_rsasa with 960 Fibonacci dots, probe 1.4
+//       typed_rsasa: calc_rsasa of an rsasa_gpu initialized with
+//         dot_spheres_params(5 dots/A^2, probe 1.4) and the latitude sets of
+//         the reference's CPU algorithm (one per atomic radius)
 #include "rsx/saxs_algorithm.hpp"
 
 #include <cstdint>
@@ -157,6 +160,12 @@ int run_gpu(const char *in_path, const char *out_path)
     sasa.initialize((unsigned)n, radius_of_type, 1.4f, dots, 0);
     std::vector<float> rsasa_out(n);
     sasa.calc_rsasa(bodies, rsasa_out);
+    rsx::algorithm::rsasa_gpu typed;
+    typed.initialize((unsigned)n, rsx::algorithm::dot_spheres_params(5.f, 1.4f),
+                     RSX_DOTS_LATITUDE, 0);
+    std::vector<float> typed_rsasa(n);
+    typed.calc_rsasa(bodies, typed_rsasa);
+    typed.recalc_rsasa(bodies, typed_rsasa);
 
     std::ofstream o(out_path, std::ios::binary);
     for (const auto &c : curves) {
@@ -166,7 +175,8 @@ int run_gpu(const char *in_path, const char *out_path)
         }
         o.write(reinterpret_cast<const char *>(c.data()), std::streamsize(c.size() * 4));
     }
-    const std::vector<float> *tails[] = {&rsasa_out, &water_rsasa, &water_rsasa_moved};
+    const std::vector<float> *tails[] = {&rsasa_out, &water_rsasa, &water_rsasa_moved,
+                                         &typed_rsasa};
     for (const std::vector<float> *v : tails) {
         if ((int)v->size() != n) {
             std::fprintf(stderr, "rsasa of %zu values, want %d\n", v->size(), n);

@@ -67,9 +67,9 @@ def test_adapter_curves_and_rsasa(adapter_exe, oracle_lib, tmp_path):
                        text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     raw = np.fromfile(outp, np.float32)
-    assert raw.size == 8 * n_q + 3 * n
+    assert raw.size == 8 * n_q + 4 * n
     curves = raw[:8 * n_q].reshape(8, n_q)
-    got_rsasa, water_rsasa, water_rsasa_moved = raw[8 * n_q:].reshape(3, n)
+    got_rsasa, water_rsasa, water_rsasa_moved, typed_rsasa = raw[8 * n_q:].reshape(4, n)
 
     moved, moved2 = w.bodies.copy(), w.bodies.copy()
     moved[start:start + length, 0] += np.float32(0.3)
@@ -94,19 +94,25 @@ def test_adapter_curves_and_rsasa(adapter_exe, oracle_lib, tmp_path):
     want = counts.astype(np.float32) / np.float32(960)
     assert np.array_equal(got_rsasa, want)
 
-    # the water term's own SASA: 32 dodecahedron/icosahedron dots, probe 1.8 A,
-    # the atomic radius of each body's type (saxs_alg_cl_gpu_pt_wf.cpp:82-96)
+    # the water term's own SASA: the reference's OpenCL dot map (the
+    # create_dodeca_icosa_dots sphere of each atomic radius, probe 1.8 A,
+    # saxs_alg_cl_gpu_pt_wf.cpp:82-96, rsasa_cl_gpu_alg.cpp:60-89)
     from resaxs_gb300 import _lib
-    from resaxs_gb300.sasa import dodeca_icosa_dots
+    from resaxs_gb300.sasa import reference_dot_map
     atomic_radii = np.zeros(16, np.float32)
     _lib.check(_lib.lib().rsx_ff_radii(atomic_radii))
-    ico = dodeca_icosa_dots()
+    ico = reference_dot_map(atomic_radii, "dodeca_icosa", 1.8)
     for bodies, got, curve in ((w.bodies, water_rsasa, curves[6]),
                                (moved, water_rsasa_moved, curves[7])):
-        c = oracle_lib.sasa_counts(bodies, atomic_radii[types], ico, 1.8)
+        c = oracle_lib.sasa_counts_typed(bodies, atomic_radii, ico, 1.8)
         rs = c.astype(np.float32) / np.float32(32)
         assert np.array_equal(got, rs)
         ref = oracle_lib.debye_f64(w.q, bodies, w.ff, rsasa=rs, water_weight=0.7,
                                    water_index=water_index)
         assert rel(curve, ref) < TOL
     assert rel(curves[6], ref_w) > 1e-4
+    # the reference CPU algorithm's dot sets through rsasa_gpu::initialize
+    lat = reference_dot_map(atomic_radii, "latitude", 1.4, 5.0)
+    c = oracle_lib.sasa_counts_typed(w.bodies, atomic_radii, lat, 1.4)
+    n_dots = np.isfinite(lat[:, :, 0]).sum(axis=1)[types].astype(np.float32)
+    assert np.array_equal(typed_rsasa, c.astype(np.float32) / n_dots)

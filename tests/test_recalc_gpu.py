@@ -196,16 +196,15 @@ def test_saxs_algorithm_mirror(S, oracle_lib):
 
 def test_saxs_algorithm_mirror_water_computes_its_own_rsasa(S, oracle_lib):
     """With a non-zero water weight the i_saxs mirror recomputes rsasa from the
-    bodies on each update, as the reference's GPU algorithm does (32
-    dodecahedron/icosahedron dots, probe 1.8 A, atomic radii by type); given
-    rsasa values are kept only with no_rsasa_recalc set."""
+    bodies on each update, as the reference's GPU algorithm does (its own
+    dodeca-icosa dot map, probe 1.8 A, atomic radii by type); given rsasa
+    values are kept only with no_rsasa_recalc set."""
     from resaxs_gb300 import _lib
-    from resaxs_gb300.sasa import dodeca_icosa_dots
+    from resaxs_gb300.sasa import reference_dot_map
     w = W.make_config(2, seed=29, n_override=600)
     radii = np.zeros(16, np.float32)
     _lib.check(_lib.lib().rsx_ff_radii(radii))
-    types = w.bodies.view(np.uint32)[:, 3]
-    ico = dodeca_icosa_dots()
+    ico = reference_dot_map(radii, "dodeca_icosa", 1.8)
     widx = w.ff.shape[1] - 1
 
     def expect(bodies, rs):
@@ -219,14 +218,14 @@ def test_saxs_algorithm_mirror_water_computes_its_own_rsasa(S, oracle_lib):
     p.get_implicit_water_params().set_water_weight(1.5)
     alg.initialize()
     out = alg.calc_curve(w.bodies)
-    rs = (oracle_lib.sasa_counts(w.bodies, radii[types], ico, 1.8).astype(np.float32)
+    rs = (oracle_lib.sasa_counts_typed(w.bodies, radii, ico, 1.8).astype(np.float32)
           / np.float32(32))
     assert np.array_equal(p.get_implicit_water_params().rsasa, rs)
     assert rel(out, expect(w.bodies, rs)) < TOL
     b = w.bodies.copy()
     b[100:130, :3] += np.float32(2.0)
     out = alg.recalc_curve(b, 100, 30)
-    rs_b = (oracle_lib.sasa_counts(b, radii[types], ico, 1.8).astype(np.float32)
+    rs_b = (oracle_lib.sasa_counts_typed(b, radii, ico, 1.8).astype(np.float32)
             / np.float32(32))
     assert rel(out, expect(b, rs_b)) < TOL
     given = np.random.default_rng(3).uniform(0, 1, w.n).astype(np.float32)

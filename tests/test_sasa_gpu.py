@@ -251,3 +251,23 @@ def test_typed_bad_inputs(golden_sasa):
         assert status == _lib.RSX_INVALID_ARG  # unit-form call on a typed handle
     with pytest.raises(_lib.ResaxsError):
         TypedDotSphereSasa(2, dm, -g["radii"], 1.8)
+
+
+@gpu
+@pytest.mark.parametrize("name", ["a", "c"])
+def test_rsasa_mirror_reproduces_reference_cpu_algorithm(golden_sasa, name):
+    """i_rsasa mirror initialized like the reference's rsasa_cpu_alg
+    (dot_spheres_params(5 dots/A^2, probe 1.4), the create_dots sphere of each
+    atomic radius): calc_rsasa and recalc_rsasa give the reference's rsasa bit
+    for bit."""
+    from resaxs_gb300.sasa import RsasaAlgorithm
+    g = golden_sasa
+    atoms = g[f"{name}_atoms"]
+    alg = RsasaAlgorithm()
+    alg.initialize(len(atoms), dot_density=float(g["density"]), probe_radius=float(g["probe"]),
+                   dot_kind="latitude")
+    out = np.zeros(len(atoms), np.float32)
+    alg.calc_rsasa(atoms, out)
+    assert np.array_equal(out.view(np.uint32), g[f"{name}_rsasa_ref"].view(np.uint32))
+    again = alg.recalc_rsasa(atoms)
+    assert np.array_equal(again, out)

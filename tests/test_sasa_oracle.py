@@ -106,3 +106,26 @@ def test_reference_dot_sets_shapes(golden_sasa):
             assert np.allclose(r, ext, rtol=1e-5), (kind, t)
     sizes = np.diff(g["dots_latitude_start"])
     assert np.all(sizes > 20) and np.all(np.diff(sizes[np.argsort(g["radii"])]) >= 0)
+
+
+@pytest.mark.parametrize("kind", ["latitude", "32", "fibonacci", "dodecahedron", "dodeca_icosa"])
+def test_library_sphere_dots_bitexact_with_reference(golden_sasa, kind):
+    """rsx_sasa_sphere_dots (host code, no GPU) gives the reference
+    generators' dots bit for bit for every type radius."""
+    from resaxs_gb300 import sasa
+    g = golden_sasa
+    probe = float(g[f"dots_{kind}_probe"])
+    for t, ref in enumerate(sasa_dot_sets(g, kind)):
+        got = sasa.sphere_dots(kind, float(g["radii"][t]), probe, float(g["density"]))
+        assert got.shape == ref.shape, (kind, t)
+        assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (kind, t)
+
+
+def test_library_sphere_dots_rejects_bad_input():
+    from resaxs_gb300 import _lib, sasa
+    with pytest.raises(_lib.ResaxsError):
+        sasa.sphere_dots("latitude", 1.5, 1.4, -1.0)
+    with pytest.raises(_lib.ResaxsError):
+        sasa.sphere_dots("fibonacci", float("nan"), 1.4)
+    big = sasa.sphere_dots("latitude", 1.9, 1.4, 50.0)   # grows the output buffer
+    assert len(big) > 1000
