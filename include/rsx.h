@@ -145,10 +145,11 @@ typedef struct rsx_debye rsx_debye;
 typedef struct rsx_debye_options {
     int device;          /* CUDA ordinal; -1 = current device */
     int q_slab;          /* q values per CTA slab: 8, 16, 32, 64, 128 or 192; 0 = tuned /
-                            default.  On uniform grids 64 and 128 select the wide
-                            slabs (64 to 128 q per recurrence seed), and 192 adds
-                            192-q slabs to the forward without water (2 CTAs/SM);
-                            the other kernels take at most 128. */
+                            default (192 on uniform grids of 64 q or more).  On
+                            uniform grids 64, 128 and 192 select the wide slabs
+                            (64, up to 128, or up to 192 q per recurrence seed;
+                            192-q slabs for the forward without water only, at
+                            2 CTAs/SM); the other kernels take at most 128. */
     int max_items;       /* cap on forward work items (scratch = items*n_q*8 B); 0 = default */
     int force_general_q; /* 1: never use the uniform-grid recurrence */
     int timing;          /* 1: record CUDA events around the pair kernel */

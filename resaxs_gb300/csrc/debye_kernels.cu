@@ -415,8 +415,11 @@ static cudaError_t wide_launch(DebyeArgs a, int k_base, int n_slabs, bool water,
 // steps, so short slabs are dear per q (the 48-q slab measured slower than
 // the 64-q one, which therefore also serves remainders of 33..48 q).
 static constexpr float kCostMain64 = 1.82f, kCostMain112 = 2.75f, kCostMain128 = 3.00f;
-// the 192-q slab (2 CTAs/SM), relative to the same scale
-static constexpr float kCostMain192 = 4.30f;
+// the 192-q slab (2 CTAs/SM) on the same scale: N = 200,000, 512 q took
+// 1083.7 ms as four 128-q slabs and 1001.1 ms as two 192-q slabs and a
+// 128-q tail, so a 192-q slab costs (1001.1 - 1083.7 / 4) / 2 / (1083.7 / 4)
+// = 1.347 128-q slabs
+static constexpr float kCostMain192 = 4.04f;
 static constexpr float kCostWidth[8] = {0.99f, 1.35f, 2.34f, 1.82f, 2.13f, 2.29f, 2.75f, 3.00f};
 
 // Width (multiple of 16, <= 128) of the cheapest slab that covers len q.
@@ -454,7 +457,8 @@ static cudaError_t wide_tail(const DebyeArgs &a, int k0, int width, bool water, 
 }
 
 // The cheapest of: 64-q slabs and a tail; 64-q slabs with a short remainder
-// (<= 48 q) folded into the last slab; 112-q slabs and a tail.
+// (<= 48 q) folded into the last slab; 112-q or 128-q slabs and a tail
+// (q_slab >= 128); 192-q slabs and a tail of at most 128 q (q_slab >= 192).
 WidePlan wide_plan(int n_q, int q_slab)
 {
     WidePlan best{};
@@ -476,8 +480,9 @@ WidePlan wide_plan(int n_q, int q_slab)
         consider(128, f128, r128, f128 * kCostMain128 + tail_cost(r128));
     }
     if (q_slab >= 192) {
+        // one tail slab of at most 128 q follows the 192-q slabs
         const int f192 = n_q / 192, r192 = n_q - 192 * f192;
-        if (f192 > 0)
+        if (f192 > 0 && r192 <= 128)
             consider(192, f192, r192, f192 * kCostMain192 + tail_cost(r192));
     }
     return best;

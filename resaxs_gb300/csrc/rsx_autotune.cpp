@@ -16,7 +16,10 @@
 
 namespace rsx {
 
-static bool valid_q_slab(long v) { return v == 8 || v == 16 || v == 32 || v == 64 || v == 128; }
+static bool valid_q_slab(long v)
+{
+    return v == 8 || v == 16 || v == 32 || v == 64 || v == 128 || v == 192;
+}
 
 static std::mutex g_mu;
 static std::map<std::string, int> g_cache;

@@ -542,6 +542,8 @@ rsx_status tune_slab(rsx_debye *h)
     if (h->uniform) {
         cands.push_back(64);
         cands.push_back(128);
+        if (!has_water(h) && h->n_q >= 192)
+            cands.push_back(192);
     }
     cudaEvent_t e0, e1;
     RSX_TRY_CUDA(cudaEventCreate(&e0), "event");
@@ -823,10 +825,10 @@ rsx_status rsx_debye_create(const float *q, int n_q, const float *t_factors, int
     h->q.assign(q, q + n_q);
     h->ff.assign(t_factors, t_factors + (size_t)n_q * n_factors);
     h->uniform = !o.force_general_q && detect_uniform(h->q, &h->dq);
-    // default tile: the wide slabs (112 q per seed) on uniform grids of 64 q
-    // or more, otherwise 32 / 16 / 8
+    // default tile: the wide slabs (64 to 192 q per seed, by the plan's
+    // measured costs) on uniform grids of 64 q or more, otherwise 32 / 16 / 8
     h->q_slab = o.q_slab ? o.q_slab
-                         : (h->uniform && n_q >= 64 ? 128 : (n_q >= 32 ? 32 : (n_q >= 16 ? 16 : 8)));
+                         : (h->uniform && n_q >= 64 ? 192 : (n_q >= 32 ? 32 : (n_q >= 16 ? 16 : 8)));
     h->autotune = o.autotune != 0 && o.q_slab == 0;
     h->max_items = o.max_items > 0 ? o.max_items : 16384;
     h->timing = o.timing != 0;
@@ -974,8 +976,8 @@ int rsx_debug_theta_level(int uniform, double dq, double diag)
 
 rsx_status rsx_debug_wide_plan(int n_q, int q_slab, int *out)
 {
-    if (n_q <= 0 || !out || (q_slab != 64 && q_slab != 128))
-        return fail(RSX_INVALID_ARG, "need n_q > 0, q_slab 64 or 128 and an output");
+    if (n_q <= 0 || !out || (q_slab != 64 && q_slab != 128 && q_slab != 192))
+        return fail(RSX_INVALID_ARG, "need n_q > 0, q_slab 64, 128 or 192 and an output");
     const WidePlan p = wide_plan(n_q, q_slab);
     out[0] = p.main;
     out[1] = p.full;

@@ -111,11 +111,12 @@ def test_wide_slab_plan_covers_every_q(librsx):
     wider than 112 q."""
     from resaxs_gb300 import _lib
     out = np.zeros(5, np.int32)
-    for q_slab in (64, 128):
+    mains = {64: (64,), 128: (64, 112, 128), 192: (64, 112, 128, 192)}
+    for q_slab in (64, 128, 192):
         for n_q in range(1, 700):
             _lib.check(librsx.rsx_debug_wide_plan(n_q, q_slab, out))
             main, full, k0, tail_len, tail_w = (int(x) for x in out)
-            assert main in ((64,) if q_slab == 64 else (64, 112, 128)), (n_q, out)
+            assert main in mains[q_slab], (n_q, out)
             assert k0 == full * main and k0 + tail_len == n_q, (n_q, out)
             if tail_len:
                 assert tail_w % 16 == 0 and tail_len <= tail_w <= 128, (n_q, out)
@@ -123,6 +124,10 @@ def test_wide_slab_plan_covers_every_q(librsx):
                     assert tail_w <= 112, (n_q, out)
             else:
                 assert tail_w == 0
+    # the measured costs pick the 192-q slabs for the configurations' grids
+    for n_q in (201, 256, 512):
+        _lib.check(librsx.rsx_debug_wide_plan(n_q, 192, out))
+        assert int(out[0]) == 192, (n_q, out)
     assert librsx.rsx_debug_wide_plan(0, 128, out) == _lib.RSX_INVALID_ARG
     assert librsx.rsx_debug_wide_plan(10, 32, out) == _lib.RSX_INVALID_ARG
 

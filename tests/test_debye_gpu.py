@@ -39,7 +39,7 @@ def test_forward_configs_vs_oracle(saxs, oracle_lib, idx, n):
     assert rel(out, ref) < TOL
 
 
-@pytest.mark.parametrize("q_slab", [8, 16, 32, 64, 128])
+@pytest.mark.parametrize("q_slab", [8, 16, 32, 64, 128, 192])
 def test_forward_slab_sizes(saxs, oracle_lib, q_slab):
     w = W.make_config(1, seed=12, n_override=700)
     _, out64, cfg = gpu_curve(saxs, w.q, w.ff, w.bodies, q_slab=q_slab)
@@ -47,8 +47,9 @@ def test_forward_slab_sizes(saxs, oracle_lib, q_slab):
     assert rel(out64, oracle_lib.debye_f64(w.q, w.bodies, w.ff)) < TOL
 
 
-@pytest.mark.parametrize("q_slab", [64, 128])
-@pytest.mark.parametrize("n_q", [5, 16, 33, 47, 64, 65, 80, 100, 111, 112, 113, 130, 201, 240])
+@pytest.mark.parametrize("q_slab", [64, 128, 192])
+@pytest.mark.parametrize("n_q", [5, 16, 33, 47, 64, 65, 80, 100, 111, 112, 113, 130, 192, 193,
+                                 201, 240, 300, 384, 400])
 def test_wide_slab_tails(saxs, oracle_lib, q_slab, n_q):
     # every tail width of the wide uniform path (16..112 after full slabs)
     rng = np.random.default_rng(n_q)
@@ -327,7 +328,7 @@ def test_autotuned_slab(saxs, oracle_lib):
     _lib.lib().rsx_autotune_clear()
     w = W.make_config(2, seed=18, n_override=3000)
     _, out64, cfg = gpu_curve(saxs, w.q, w.ff, w.bodies, autotune=True)
-    assert cfg["q_slab"] in (16, 32, 64, 128)
+    assert cfg["q_slab"] in (16, 32, 64, 128, 192)
     assert rel(out64, oracle_lib.debye_f64(w.q, w.bodies, w.ff)) < TOL
     _, again, cfg2 = gpu_curve(saxs, w.q, w.ff, w.bodies, autotune=True)   # cached choice
     assert cfg2["q_slab"] == cfg["q_slab"]
