@@ -153,11 +153,14 @@ typedef struct rsx_debye_options {
     int max_items;       /* cap on forward work items (scratch = items*n_q*8 B); 0 = default */
     int force_general_q; /* 1: never use the uniform-grid recurrence */
     int timing;          /* 1: record CUDA events around the pair kernel */
-    int autotune;        /* 1: time the q-slab candidates on first use and cache the winner */
+    int autotune;        /* 1: time the tile shapes (q-slab plan x pairs per step) on first
+                            use and cache the winner per problem class */
     int no_pair_tables;  /* 1: evaluate every pair*q term instead of the tabulated pair
                             functions (adjoint) and the gridded pair-distance distribution
                             (forward on non-uniform grids): the recurrence adjoint and the
                             direct-sine forward, at their pair*q cost */
+    int pairs_per_step;  /* pairs a thread steps together in the wide forward's main
+                            slabs of 128 q or more: 2 or 4; 0 = tuned / default (2) */
 } rsx_debye_options;
 
 /* Forgets every autotuned tile choice of this process (the file named by
@@ -253,6 +256,11 @@ rsx_status rsx_debye_chi2_backward(rsx_debye *h, const float *target, const floa
                                    double *chi2, float *grad_xyz);
 
 /* Tuning in effect: q-slab, work items, whether the uniform-q recurrence is used. */
+/* Tile shape of the forward (the q-slab option in effect and the pairs per
+ * step of the wide main slabs), after autotuning when it was requested.  No
+ * reference counterpart (the reference's tile is its fixed GROUP_SIZE,
+ * saxs_alg_cl_gpu_pt_wf.cpp:203-207). */
+rsx_status rsx_debye_tile_shape(rsx_debye *h, int *q_slab, int *pairs_per_step);
 rsx_status rsx_debye_config(rsx_debye *h, int *q_slab, int *n_items, int *uniform_q);
 
 /* Form-factor tables (host side, no GPU): resaxs::atomic_form_factors<float>
@@ -374,6 +382,16 @@ rsx_status rsx_batch_destroy(rsx_batch *h);
 rsx_status rsx_batch_forward(rsx_batch *h, const rsx_body *bodies, float *out_iq);
 /* Per-member targets and sigmas (n_members x n_q each) of the chi^2 loss. */
 rsx_status rsx_batch_set_targets(rsx_batch *h, const float *targets, const float *sigma);
+/* Replaces the factor table (n_q x n_factors, the handle's n_factors), as
+ * rsx_debye_set_factors does for one structure. */
+rsx_status rsx_batch_set_factors(rsx_batch *h, const float *t_factors, int n_factors);
+/* Implicit water for every member (f~_i = f_t(i) + weight * rsasa_i * f_water),
+ * as rsx_debye_set_water does for one structure: rsasa holds one value per
+ * body in the concatenated caller order of rsx_batch_forward (NULL keeps the
+ * values already set); weight 0 turns the term off.  Forward only:
+ * rsx_batch_forward_chi2_backward returns RSX_NOT_SUPPORTED while the weight
+ * is non-zero. */
+rsx_status rsx_batch_set_water(rsx_batch *h, float weight, int water_index, const float *rsasa);
 /* Forward, chi^2_m = sum_q ((I_m - t_m)/sigma_m)^2 and dchi^2_m/dx for every
  * body of every member, in one pass (out_iq, chi2, grad_xyz may be NULL). */
 rsx_status rsx_batch_forward_chi2_backward(rsx_batch *h, const rsx_body *bodies, float *out_iq,

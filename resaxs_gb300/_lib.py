@@ -48,7 +48,8 @@ class ResaxsError(RuntimeError):
 class DebyeOptions(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("q_slab", ctypes.c_int), ("max_items", ctypes.c_int),
                 ("force_general_q", ctypes.c_int), ("timing", ctypes.c_int),
-                ("autotune", ctypes.c_int), ("no_pair_tables", ctypes.c_int)]
+                ("autotune", ctypes.c_int), ("no_pair_tables", ctypes.c_int),
+                ("pairs_per_step", ctypes.c_int)]
 
 
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
@@ -99,6 +100,7 @@ SIGNATURES = [
     ("rsx_debye_backward_f64", _st, [_vp, _f32p, _f64p]),
     ("rsx_debye_chi2_backward", _st, [_vp, _f32p, _f32p, ctypes.POINTER(ctypes.c_double),
                                       _vp]),
+    ("rsx_debye_tile_shape", _st, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
     ("rsx_debye_config", _st, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i),
                                ctypes.POINTER(_i)]),
     ("rsx_ff_type_count", _i, []),
@@ -127,6 +129,8 @@ SIGNATURES = [
     ("rsx_batch_destroy", _st, [_vp]),
     ("rsx_batch_forward", _st, [_vp, _f32p, _f32p]),
     ("rsx_batch_set_targets", _st, [_vp, _f32p, _f32p]),
+    ("rsx_batch_set_factors", _st, [_vp, _f32p, _i]),
+    ("rsx_batch_set_water", _st, [_vp, ctypes.c_float, _i, _vp]),
     ("rsx_batch_forward_chi2_backward", _st, [_vp, _f32p, _vp, _vp, _vp]),
     ("rsx_batch_timing", _st, [_vp, ctypes.POINTER(ctypes.c_float)]),
     ("rsx_batch_config", _st, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i),

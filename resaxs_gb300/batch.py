@@ -15,7 +15,8 @@ __all__ = ["DebyeBatch"]
 
 class DebyeBatch:
     def __init__(self, q, factors, member_sizes, *, device: int = -1, q_slab: int = 0,
-                 autotune: bool = False, force_general_q: bool = False, pair_tables: bool = True):
+                 autotune: bool = False, force_general_q: bool = False, pair_tables: bool = True,
+                 pairs_per_step: int = 0):
         self.q = np.ascontiguousarray(q, np.float32)
         factors = np.ascontiguousarray(factors, np.float32)
         self.sizes = np.ascontiguousarray(member_sizes, np.int32)
@@ -30,6 +31,7 @@ class DebyeBatch:
         opts.autotune = int(autotune)
         opts.force_general_q = int(force_general_q)
         opts.no_pair_tables = int(not pair_tables)
+        opts.pairs_per_step = int(pairs_per_step)
         h = ctypes.c_void_p()
         check(lib().rsx_batch_create(self.q, self.n_q, factors.reshape(-1), factors.shape[1],
                                      self.sizes, self.n_members, ctypes.byref(opts),
@@ -69,6 +71,28 @@ class DebyeBatch:
         out = np.zeros((self.n_members, self.n_q), np.float32)
         check(lib().rsx_batch_forward(self._h, b.reshape(-1), out.reshape(-1)))
         return out
+
+    def set_factors(self, factors):
+        f = np.ascontiguousarray(factors, np.float32)
+        # the C call reads n_q rows of n_factors values
+        if f.ndim != 2 or f.shape[0] != self.n_q:
+            raise ResaxsError(_lib.RSX_INVALID_ARG, "factor table must be [n_q][n_factors]")
+        check(lib().rsx_batch_set_factors(self._h, f.reshape(-1), f.shape[1]))
+
+    def set_water(self, weight: float, water_index: int, rsasa=None):
+        """Implicit water for every member; rsasa: one value per body, members
+        concatenated (None keeps the values already set)."""
+        ptr = None
+        if rsasa is not None:
+            if not isinstance(rsasa, np.ndarray):
+                rsasa = np.concatenate([np.asarray(r, np.float32).reshape(-1) for r in rsasa])
+            keep = np.ascontiguousarray(rsasa, np.float32).reshape(-1)
+            # the C call reads one value per body
+            if keep.size != self.n_total:
+                raise ResaxsError(_lib.RSX_INVALID_ARG, "rsasa needs one value per body")
+            self._rsasa_keep = keep
+            ptr = keep.ctypes.data
+        check(lib().rsx_batch_set_water(self._h, float(weight), int(water_index), ptr))
 
     def set_targets(self, targets, sigma):
         t = np.ascontiguousarray(targets, np.float32).reshape(-1)

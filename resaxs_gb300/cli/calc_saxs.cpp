@@ -299,11 +299,14 @@ struct Fit {
     std::vector<float> intensity;
 };
 
-// One librsx handle per model; the factor table follows the expansion factor
-// (generated with the mean radius of the first model, as the reference's
-// atomic_ff_params does) and the water weight enters with per-model rsasa
-// from the dot-sphere SASA (32 dodecahedron/icosahedron dots, probe 1.8 A,
-// radii per atom type: saxs_alg_cl_gpu_pt_wf.cpp:82-96).
+// All models in one librsx batch handle: each grid point of the fit is one
+// graph-captured persistent pass over the whole ensemble (the reference runs
+// one i_saxs::calc_curve per model).  The factor table follows the expansion
+// factor (generated with the mean radius of the first model, as the
+// reference's atomic_ff_params does) and the water weight enters with
+// per-model rsasa from the dot-sphere SASA on the reference GPU algorithm's
+// own dot map (create_dodeca_icosa_dots per atomic radius, probe 1.8 A:
+// saxs_alg_cl_gpu_pt_wf.cpp:82-96, rsasa_cl_gpu_alg.cpp:60-89).
 class Evaluator {
 public:
     Evaluator(const std::vector<std::vector<rsx_body>> &models, const std::vector<float> &q,
@@ -313,46 +316,45 @@ public:
         check(rsx_ff_avg_radius(models_[0].data(), (int)models_[0].size(), &avg_radius_));
         table_.resize(q_.size() * 16);
         check(rsx_ff_atomic_table(q_.data(), (int)q_.size(), avg_radius_, 1.0f, table_.data()));
+        std::vector<int> sizes;
+        for (const auto &m : models_) {
+            sizes.push_back((int)m.size());
+            bodies_.insert(bodies_.end(), m.begin(), m.end());
+        }
         rsx_debye_options o;
         rsx_debye_default_options(&o);
         o.device = device_;
-        for (const auto &m : models_) {
-            rsx_debye *h = nullptr;
-            check(rsx_debye_create(q_.data(), (int)q_.size(), table_.data(), 16, (int)m.size(), &o, &h));
-            handles_.push_back(h);
-        }
+        check(rsx_batch_create(q_.data(), (int)q_.size(), table_.data(), 16, sizes.data(),
+                               (int)sizes.size(), &o, &batch_));
+        curves_.resize(models_.size() * q_.size());
     }
-    ~Evaluator()
-    {
-        for (auto h : handles_)
-            rsx_debye_destroy(h);
-    }
+    ~Evaluator() { rsx_batch_destroy(batch_); }
 
-    // avg_ensemble (calc_saxs.hpp:611-624)
+    // avg_ensemble (calc_saxs.hpp:611-624): the mean of the models' curves,
+    // summed in model order
     std::vector<float> average(float exp_factor, float water_weight)
     {
         ++calls;
         if (exp_factor != cur_ef_) {
             check(rsx_ff_atomic_table(q_.data(), (int)q_.size(), avg_radius_, exp_factor,
                                       table_.data()));
-            for (auto h : handles_)
-                check(rsx_debye_set_factors(h, table_.data(), 16));
+            check(rsx_batch_set_factors(batch_, table_.data(), 16));
             cur_ef_ = exp_factor;
         }
         if (water_weight != cur_ww_) {
-            if (water_weight != 0 && rsasa_.empty())
+            const float *rs = nullptr;
+            if (water_weight != 0 && rsasa_.empty()) {
                 compute_rsasa();
-            for (size_t m = 0; m < handles_.size(); ++m)
-                check(rsx_debye_set_water(handles_[m], water_weight, rsx_ff_water_index(),
-                                          water_weight != 0 ? rsasa_[m].data() : nullptr));
+                rs = rsasa_.data();
+            }
+            check(rsx_batch_set_water(batch_, water_weight, rsx_ff_water_index(), rs));
             cur_ww_ = water_weight;
         }
-        std::vector<float> avg(q_.size(), 0.f), iq(q_.size());
-        for (size_t m = 0; m < handles_.size(); ++m) {
-            check(rsx_debye_calc(handles_[m], models_[m].data(), iq.data()));
-            for (size_t k = 0; k < iq.size(); ++k)
-                avg[k] += iq[k];
-        }
+        check(rsx_batch_forward(batch_, bodies_.data(), curves_.data()));
+        std::vector<float> avg(q_.size(), 0.f);
+        for (size_t m = 0; m < models_.size(); ++m)
+            for (size_t k = 0; k < q_.size(); ++k)
+                avg[k] += curves_[m * q_.size() + k];
         for (auto &v : avg)
             v /= models_.size();
         return avg;
@@ -361,24 +363,37 @@ public:
     unsigned calls = 0;
 
 private:
+    // rsasa of every model, concatenated in model order
     void compute_rsasa()
     {
-        float radii[16], dots[96];
+        float radii[16];
         check(rsx_ff_radii(radii));
-        check(rsx_sasa_dodeca_icosa_dots(dots));
+        std::vector<std::vector<float>> sets(16);
+        int stride = 1;
+        for (int t = 0; t < 16; ++t) {
+            int n = 0;
+            rsx_status st = rsx_sasa_sphere_dots(RSX_DOTS_DODECA_ICOSA, radii[t], 0.f, 1.8f,
+                                                 nullptr, 0, &n);
+            if (st != RSX_OK && n == 0)
+                check(st);
+            sets[t].resize(4 * (size_t)n);
+            check(rsx_sasa_sphere_dots(RSX_DOTS_DODECA_ICOSA, radii[t], 0.f, 1.8f,
+                                       sets[t].data(), n, &n));
+            stride = std::max(stride, n);
+        }
+        std::vector<float> map(16 * (size_t)stride * 4, -std::numeric_limits<float>::infinity());
+        for (int t = 0; t < 16; ++t)
+            std::copy(sets[t].begin(), sets[t].end(), map.begin() + (size_t)t * stride * 4);
+        rsasa_.resize(bodies_.size());
+        size_t off = 0;
         for (const auto &m : models_) {
             rsx_sasa *s = nullptr;
-            check(rsx_sasa_create((int)m.size(), dots, 32, 1.8f, device_, &s));
-            std::vector<float> r(m.size()), out(m.size());
-            for (size_t i = 0; i < m.size(); ++i) {
-                unsigned t;
-                std::memcpy(&t, &m[i].w, 4);
-                r[i] = radii[t];
-            }
-            const rsx_status st = rsx_sasa_calc(s, m.data(), r.data(), out.data());
+            check(rsx_sasa_create_typed((int)m.size(), map.data(), 16, stride, radii, 1.8f,
+                                        device_, &s));
+            const rsx_status st = rsx_sasa_calc_typed(s, m.data(), rsasa_.data() + off);
             rsx_sasa_destroy(s);
             check(st);
-            rsasa_.push_back(std::move(out));
+            off += m.size();
         }
     }
 
@@ -387,8 +402,10 @@ private:
     int device_;
     float avg_radius_ = 0;
     std::vector<float> table_;
-    std::vector<rsx_debye *> handles_;
-    std::vector<std::vector<float>> rsasa_;
+    std::vector<rsx_body> bodies_;
+    std::vector<float> curves_;
+    rsx_batch *batch_ = nullptr;
+    std::vector<float> rsasa_;
     float cur_ef_ = 1.0f, cur_ww_ = 0.0f;
 };
 

@@ -16,7 +16,7 @@
 
 namespace rsx {
 
-template <int QS, bool UNIFORM>
+template <int QS, bool UNIFORM, bool WATER = false>
 __global__ void __launch_bounds__(kBlockAtoms)
     batch_forward_kernel(const DebyeArgs a, const int *work_order, int n_units, int n_slabs,
                          int k_base, int *counter)
@@ -31,13 +31,35 @@ __global__ void __launch_bounds__(kBlockAtoms)
         if (w >= n_units)
             break;
         const int item = work_order[w / n_slabs];
-        forward_item<QS, UNIFORM, false>(a, item, k_base + (w % n_slabs) * QS);
+        forward_item<QS, UNIFORM, WATER>(a, item, k_base + (w % n_slabs) * QS);
     }
 }
 
-// Wide uniform slabs (no water), as forward_wide_kernel.
-template <int QS, int IL, bool SIGNED = true>
+// Wide uniform slabs with the implicit water term, as forward_wide_water_kernel.
+template <int QS, bool SIGNED>
 __global__ void __launch_bounds__(kBlockAtoms, (QS <= 64 || !SIGNED) ? 3 : 2)
+    batch_wide_water_kernel(const DebyeArgs a, const int *work_order, int n_units, int n_slabs,
+                            int k_base, int *counter)
+{
+    __shared__ int s_w;
+    for (;;) {
+        if (threadIdx.x == 0)
+            s_w = atomicAdd(counter, 1);
+        __syncthreads();
+        const int w = s_w;
+        __syncthreads();
+        if (w >= n_units)
+            break;
+        const int item = work_order[w / n_slabs];
+        forward_wide_water_item<QS, SIGNED>(a, item, k_base + (w % n_slabs) * QS);
+    }
+}
+
+// Wide uniform slabs (no water), as forward_wide_kernel (same register
+// classes: 3 CTAs per SM for two plain pairs per step up to 128 q).
+template <int QS, int IL, bool SIGNED = true>
+__global__ void __launch_bounds__(kBlockAtoms,
+                                  (IL == 2 && (QS <= 64 || (!SIGNED && QS <= 128))) ? 3 : 2)
     batch_wide_kernel(const DebyeArgs a, const int *work_order, int n_units, int n_slabs,
                       int k_base, int *counter)
 {
@@ -97,9 +119,18 @@ __global__ void __launch_bounds__(256) batch_assemble_kernel(const BatchAssemble
     double self = 0.0, sumf = 0.0;
     const float *ff = a.ff + (size_t)k * a.n_types;
     const int *cnt = a.type_count + (size_t)m * a.n_types;
+    // f~_i = f_t + w rsasa_i f_w: sum f~^2 = sum f_t^2 + 2 w f_w sum_t f_t S_t +
+    // (w f_w)^2 sum rsasa^2, sum f~ = sum f_t + w f_w sum rsasa (assemble_kernel)
+    const double fw = a.has_water ? (double)(a.water_weight * ff[a.water_index]) : 0.0;
     for (int t = 0; t < a.n_types; ++t) {
         self += cnt[t] * (double)ff[t] * ff[t];
         sumf += cnt[t] * (double)ff[t];
+        if (a.has_water)
+            self += 2.0 * fw * ff[t] * a.rsasa_sum[(size_t)m * a.n_types + t];
+    }
+    if (a.has_water) {
+        self += fw * fw * a.rsasa_sq[m];
+        sumf += fw * a.rsasa_tot[m];
     }
     const double iq = (q != 0.0) ? self + 2.0 * cross / q : sumf * sumf;
     a.iq64[(size_t)m * a.n_q + k] = iq;
@@ -132,22 +163,35 @@ __global__ void __launch_bounds__(256) batch_loss_kernel(const BatchLossArgs a)
     }
 }
 
-template <int QS, bool U>
+template <int QS, bool U, bool W = false>
 static cudaError_t fwd_launch(const DebyeArgs &a, const int *order, int n_items, int n_slabs,
                               int k_base, int *counter, int grid, cudaStream_t st)
 {
-    batch_forward_kernel<QS, U><<<grid, kBlockAtoms, 0, st>>>(a, order, n_items * n_slabs,
-                                                              n_slabs, k_base, counter);
+    batch_forward_kernel<QS, U, W><<<grid, kBlockAtoms, 0, st>>>(a, order, n_items * n_slabs,
+                                                                 n_slabs, k_base, counter);
     count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_batch_forward(const DebyeArgs &a, const int *work_order, int n_work_items,
                                  int q_slab, int n_slabs, int k_base, bool uniform,
-                                 int *counter, int grid, cudaStream_t st)
+                                 int *counter, int grid, cudaStream_t st, bool water)
 {
     if (n_work_items == 0 || n_slabs == 0)
         return cudaSuccess;
+    if (water) { // two accumulator sets per thread: 8 or 16 q per slab
+        if (q_slab == 8)
+            return uniform ? fwd_launch<8, true, true>(a, work_order, n_work_items, n_slabs,
+                                                       k_base, counter, grid, st)
+                           : fwd_launch<8, false, true>(a, work_order, n_work_items, n_slabs,
+                                                        k_base, counter, grid, st);
+        if (q_slab == 16)
+            return uniform ? fwd_launch<16, true, true>(a, work_order, n_work_items, n_slabs,
+                                                        k_base, counter, grid, st)
+                           : fwd_launch<16, false, true>(a, work_order, n_work_items, n_slabs,
+                                                         k_base, counter, grid, st);
+        return cudaErrorInvalidValue;
+    }
 #define RSX_BF(QS)                                                                         \
     return uniform ? fwd_launch<QS, true>(a, work_order, n_work_items, n_slabs, k_base,    \
                                           counter, grid, st)                               \
@@ -170,12 +214,37 @@ template <class K>
 static int occupancy_grid(K kfn, size_t smem, int sms);
 
 template <int QS>
+static cudaError_t wide_batch_water_launch(const DebyeArgs &a, const int *order, int n_items,
+                                           int n_slabs, int k_base, int *counter, int sms,
+                                           cudaStream_t st)
+{
+    if constexpr (QS > 128) {
+        return cudaErrorInvalidValue; // the water slabs stop at 128 q
+    } else {
+        auto kfn = a.small_theta >= 2 ? batch_wide_water_kernel<QS, false>
+                                      : batch_wide_water_kernel<QS, true>;
+        const int grid = std::min(occupancy_grid(kfn, 0, sms), n_items * n_slabs);
+        kfn<<<grid, kBlockAtoms, 0, st>>>(a, order, n_items * n_slabs, n_slabs, k_base, counter);
+        count_launch();
+        return cudaGetLastError();
+    }
+}
+
+template <int QS>
 static cudaError_t wide_batch_launch(const DebyeArgs &a, const int *order, int n_items,
                                      int n_slabs, int k_base, int *counter, int sms,
-                                     cudaStream_t st)
+                                     cudaStream_t st, bool main = false, bool water = false)
 {
-    // instantiations as in the single-structure launcher
+    if (water)
+        return wide_batch_water_launch<QS>(a, order, n_items, n_slabs, k_base, counter, sms, st);
+    // instantiations as in the single-structure launcher (four pairs per step
+    // in the main slabs of 128 q and more when the tuned tile shape says so)
     auto kfn = a.small_theta >= 2 ? batch_wide_kernel<QS, 2, false> : batch_wide_kernel<QS, 2, true>;
+    if constexpr (QS >= 128) {
+        if (main && a.pairs4)
+            kfn = a.small_theta >= 2 ? batch_wide_kernel<QS, 4, false>
+                                     : batch_wide_kernel<QS, 4, true>;
+    }
     const int grid = std::min(occupancy_grid(kfn, 0, sms), n_items * n_slabs);
     kfn<<<grid, kBlockAtoms, 0, st>>>(a, order, n_items * n_slabs, n_slabs, k_base, counter);
     count_launch();
@@ -184,26 +253,29 @@ static cudaError_t wide_batch_launch(const DebyeArgs &a, const int *order, int n
 
 cudaError_t launch_batch_forward_wide(const DebyeArgs &a, const int *work_order,
                                       int n_work_items, int q_slab, int *counters, int sms,
-                                      cudaStream_t st)
+                                      cudaStream_t st, bool water)
 {
     if (n_work_items == 0)
         return cudaSuccess;
-    const WidePlan p = wide_plan(a.n_q, q_slab);
+    const WidePlan p = wide_plan(a.n_q, water ? std::min(q_slab, 128) : q_slab);
     if (p.full > 0) {
         cudaError_t e;
         e = p.main == 64    ? wide_batch_launch<64>(a, work_order, n_work_items, p.full, 0,
-                                                    counters, sms, st)
+                                                    counters, sms, st, false, water)
             : p.main == 112 ? wide_batch_launch<112>(a, work_order, n_work_items, p.full, 0,
-                                                     counters, sms, st)
+                                                     counters, sms, st, false, water)
+            : p.main == 192 ? wide_batch_launch<192>(a, work_order, n_work_items, p.full, 0,
+                                                     counters, sms, st, true, water)
                             : wide_batch_launch<128>(a, work_order, n_work_items, p.full, 0,
-                                                     counters, sms, st);
+                                                     counters, sms, st, true, water);
         if (e != cudaSuccess)
             return e;
     }
     if (p.tail_len == 0)
         return cudaSuccess;
 #define RSX_BW(QS)                                                                         \
-    return wide_batch_launch<QS>(a, work_order, n_work_items, 1, p.tail_k0, counters + 1, sms, st)
+    return wide_batch_launch<QS>(a, work_order, n_work_items, 1, p.tail_k0, counters + 1, sms, \
+                                 st, false, water)
     switch (p.tail_w / 16) {
     case 1:
         RSX_BW(16);
@@ -325,8 +397,14 @@ static int occupancy_grid(K kfn, size_t smem, int sms)
     return per_sm * sms;
 }
 
-int batch_forward_grid(int q_slab, bool uniform, int sms)
+int batch_forward_grid(int q_slab, bool uniform, int sms, bool water)
 {
+    if (water && q_slab <= 8)
+        return uniform ? occupancy_grid(batch_forward_kernel<8, true, true>, 0, sms)
+                       : occupancy_grid(batch_forward_kernel<8, false, true>, 0, sms);
+    if (water)
+        return uniform ? occupancy_grid(batch_forward_kernel<16, true, true>, 0, sms)
+                       : occupancy_grid(batch_forward_kernel<16, false, true>, 0, sms);
     switch (q_slab) {
     case 8:
         return uniform ? occupancy_grid(batch_forward_kernel<8, true>, 0, sms)

@@ -42,10 +42,12 @@ __global__ void __launch_bounds__(kBlockAtoms) forward_kernel(const DebyeArgs a)
     forward_item<QS, UNIFORM, WATER>(a, blockIdx.x, a.k_base + blockIdx.y * QS);
 }
 
-// up to 64 q, and plain up to 128 q: <= 168 registers, 3 CTAs per SM; wider
-// (signed above 64 q, every instantiation above 128 q): <= 255, 2 CTAs per SM
+// two pairs per step up to 64 q, and plain up to 128 q: <= 168 registers,
+// 3 CTAs per SM; the rest (signed above 64 q, every instantiation above 128 q,
+// four pairs per step): <= 255, 2 CTAs per SM
 template <int QS, int IL, bool SIGNED>
-__global__ void __launch_bounds__(kBlockAtoms, (QS <= 64 || (!SIGNED && QS <= 128)) ? 3 : 2)
+__global__ void __launch_bounds__(kBlockAtoms,
+                                  (IL == 2 && (QS <= 64 || (!SIGNED && QS <= 128))) ? 3 : 2)
     forward_wide_kernel(const DebyeArgs a)
 {
     forward_wide_item<QS, IL, SIGNED>(a, blockIdx.x, a.k_base + blockIdx.y * QS);
@@ -67,6 +69,12 @@ __global__ void __launch_bounds__(256) assemble_kernel(const AssembleArgs a)
 {
     __shared__ double s_w[8];
     const int k = blockIdx.x;
+    if (k >= a.n_q) { // the moved bodies' new positions (incremental mode)
+        const int m = (k - a.n_q) * blockDim.x + threadIdx.x;
+        if (m < a.apply_k)
+            a.apply_pos[a.apply_idx[m]] = a.apply_new[m];
+        return;
+    }
     double s = 0.0;
     const double *row = a.partial + (size_t)k * a.n_parts;
     for (int x = threadIdx.x; x < a.n_parts; x += blockDim.x)
@@ -229,20 +237,11 @@ __global__ void __launch_bounds__(kBlockAtoms) delta_kernel(const DeltaArgs a)
     }
 }
 
-// After a delta step: the moved bodies take their new positions.
-__global__ void apply_moves_kernel(float4 *pos, const float4 *moved_new, const int *moved_idx,
-                                   int k)
-{
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m < k)
-        pos[moved_idx[m]] = moved_new[m];
-}
-
 // Incremental delta on a uniform grid with wide slabs: as delta_kernel, but
 // QS up to 112 q per seed pair, FP32 per-tile sums reduce-scattered into FP64
 // lane accumulators (forward_wide_item's scheme).  The two chains of a pair
 // (new position, old position seeded with -1/r) run interleaved.
-template <int QS>
+template <int QS, bool SMALL>
 __global__ void __launch_bounds__(kBlockAtoms, QS <= 64 ? 3 : 2) delta_wide_kernel(const DeltaArgs a,
                                                                                   int k_base)
 {
@@ -296,9 +295,12 @@ __global__ void __launch_bounds__(kBlockAtoms, QS <= 64 ? 3 : 2) delta_wide_kern
             float rn, rninv, ro, roinv, dx, dy, dz;
             pair_r(py_new, s_new[jj], rn, rninv, dx, dy, dz);
             pair_r(py_old, s_old[jj], ro, roinv, dx, dy, dz);
-            const WideSeed pn = wide_seed(q0, dq, rn, use ? mult * rninv : 0.f);
-            const WideSeed po = wide_seed(q0, dq, ro, use ? -mult * roinv : 0.f);
-            wide_pair2<QS, QP / 2>(pn, po, S);
+            const WideSeed pn = wide_seed(q0, dq, rn, use ? mult * rninv : 0.f, SMALL);
+            const WideSeed po = wide_seed(q0, dq, ro, use ? -mult * roinv : 0.f, SMALL);
+            if constexpr (SMALL)
+                wide_pair2_body<QS, QP / 2, false>(pn, po, S);
+            else
+                wide_pair2<QS, QP / 2>(pn, po, S);
         }
 #pragma unroll
         for (int c = 0; c < NR; ++c) {
@@ -381,10 +383,22 @@ static cudaError_t forward_dispatch(const DebyeArgs &a, int qs, int k_base, int 
 // latency (6 % faster than 2 CTAs with 4 pairs per step at 201 q); the signed
 // ones keep 2 CTAs/SM above 64 q.  Both step 2 pairs at a time.
 template <int QS>
-static cudaError_t wide_launch(DebyeArgs a, int k_base, int n_slabs, bool water, cudaStream_t st)
+static cudaError_t wide_launch(DebyeArgs a, int k_base, int n_slabs, bool water, cudaStream_t st,
+                               bool main = false)
 {
     a.k_base = k_base;
     const dim3 grid(a.n_items, n_slabs);
+    if constexpr (QS >= 128) {
+        // the tuned tile shape: four pairs per step in the main slabs
+        if (main && a.pairs4 && !water) {
+            if (a.small_theta >= 2)
+                forward_wide_kernel<QS, 4, false><<<grid, kBlockAtoms, 0, st>>>(a);
+            else
+                forward_wide_kernel<QS, 4, true><<<grid, kBlockAtoms, 0, st>>>(a);
+            count_launch();
+            return cudaGetLastError();
+        }
+    }
     if constexpr (QS > 128) {
         // no water instantiation this wide (its per-q factor rows would spill)
         if (water)
@@ -395,17 +409,18 @@ static cudaError_t wide_launch(DebyeArgs a, int k_base, int n_slabs, bool water,
             forward_wide_kernel<QS, 2, true><<<grid, kBlockAtoms, 0, st>>>(a);
         count_launch();
         return cudaGetLastError();
+    } else {
+        if (water && a.small_theta >= 2)
+            forward_wide_water_kernel<QS, false><<<grid, kBlockAtoms, 0, st>>>(a);
+        else if (water)
+            forward_wide_water_kernel<QS, true><<<grid, kBlockAtoms, 0, st>>>(a);
+        else if (a.small_theta >= 2)
+            forward_wide_kernel<QS, 2, false><<<grid, kBlockAtoms, 0, st>>>(a);
+        else
+            forward_wide_kernel<QS, 2, true><<<grid, kBlockAtoms, 0, st>>>(a);
+        count_launch();
+        return cudaGetLastError();
     }
-    if (water && a.small_theta >= 2)
-        forward_wide_water_kernel<QS, false><<<grid, kBlockAtoms, 0, st>>>(a);
-    else if (water)
-        forward_wide_water_kernel<QS, true><<<grid, kBlockAtoms, 0, st>>>(a);
-    else if (a.small_theta >= 2)
-        forward_wide_kernel<QS, 2, false><<<grid, kBlockAtoms, 0, st>>>(a);
-    else
-        forward_wide_kernel<QS, 2, true><<<grid, kBlockAtoms, 0, st>>>(a);
-    count_launch();
-    return cudaGetLastError();
 }
 
 // Relative cost of one slab per pair on GB300 (CUDA-event times of single
@@ -507,8 +522,8 @@ static cudaError_t launch_forward_wide(const DebyeArgs &a, int q_slab, bool wate
         cudaError_t e;
         e = p.main == 64    ? wide_launch<64>(a, 0, p.full, water, st)
             : p.main == 112 ? wide_launch<112>(a, 0, p.full, water, st)
-            : p.main == 192 ? wide_launch<192>(a, 0, p.full, water, st)
-                            : wide_launch<128>(a, 0, p.full, water, st);
+            : p.main == 192 ? wide_launch<192>(a, 0, p.full, water, st, true)
+                            : wide_launch<128>(a, 0, p.full, water, st, true);
         if (e != cudaSuccess)
             return e;
     }
@@ -552,7 +567,7 @@ cudaError_t launch_forward(const DebyeArgs &a, int q_slab, bool uniform, bool wa
 
 cudaError_t launch_assemble(const AssembleArgs &a, cudaStream_t st)
 {
-    assemble_kernel<<<a.n_q, 256, 0, st>>>(a);
+    assemble_kernel<<<a.n_q + (a.apply_k + 255) / 256, 256, 0, st>>>(a);
     count_launch();
     return cudaGetLastError();
 }
@@ -569,12 +584,17 @@ static cudaError_t delta_qs(const DeltaArgs &a, bool uniform, cudaStream_t st)
     return cudaGetLastError();
 }
 
+// SMALL (small_theta level 2: |theta| < pi/4 for every pair before and after
+// the move): the seeds skip the reduction of theta and the signed steps.
 template <int QS>
 static cudaError_t delta_wide_launch(const DeltaArgs &a, int k_base, int n_slabs,
                                      cudaStream_t st)
 {
-    delta_wide_kernel<QS><<<dim3(a.n_blocks, n_slabs, delta_groups(a)), kBlockAtoms, 0, st>>>(
-        a, k_base);
+    const dim3 grid(a.n_blocks, n_slabs, delta_groups(a));
+    if (a.small_theta >= 2)
+        delta_wide_kernel<QS, true><<<grid, kBlockAtoms, 0, st>>>(a, k_base);
+    else
+        delta_wide_kernel<QS, false><<<grid, kBlockAtoms, 0, st>>>(a, k_base);
     count_launch();
     return cudaGetLastError();
 }
@@ -601,18 +621,21 @@ static cudaError_t delta_wide_tail(const DeltaArgs &a, int k0, int width, cudaSt
         return delta_wide_launch<96>(a, k0, 1, st);
     case 7:
         return delta_wide_launch<112>(a, k0, 1, st);
-    default: // a 64-q plan never needs a wider remainder slab
+    case 8:
+        return delta_wide_launch<128>(a, k0, 1, st);
+    default: // remainder slabs are at most 128 q wide
         return cudaErrorInvalidValue;
     }
 }
 
-// Uniform grids and q_slab 64 / 128: the forward's wide slab plan restricted
-// to 64-q main slabs (the two chains of a pair already interleave).  As in
-// the forward, the remainder slab goes to the aux stream when there is one,
-// so that its CTAs fill the last wave of the main launch.
+// Uniform grids and q_slab 64 / 128: the forward's wide slab plan up to
+// 128-q main slabs (fewer seeds per pair than 64-q slabs; 0.069 to 0.065 ms
+// per step with the small-theta seeds at k = 50 of 20,000 bodies, 201 q).
+// As in the forward, the remainder slab goes to the aux stream when there is
+// one, so that its CTAs fill the last wave of the main launch.
 static cudaError_t launch_delta_wide(const DeltaArgs &a, cudaStream_t st, const AuxStream *aux)
 {
-    const WidePlan p = wide_plan(a.n_q, 64);
+    const WidePlan p = wide_plan(a.n_q, 128);
     const bool split = aux && p.full > 0 && p.tail_len > 0;
     if (split) {
         cudaError_t e = cudaEventRecord(aux->fork, st);
@@ -622,8 +645,9 @@ static cudaError_t launch_delta_wide(const DeltaArgs &a, cudaStream_t st, const 
             return e;
     }
     if (p.full > 0) {
-        cudaError_t e = p.main == 64 ? delta_wide_launch<64>(a, 0, p.full, st)
-                                     : delta_wide_launch<112>(a, 0, p.full, st);
+        cudaError_t e = p.main == 64    ? delta_wide_launch<64>(a, 0, p.full, st)
+                        : p.main == 112 ? delta_wide_launch<112>(a, 0, p.full, st)
+                                        : delta_wide_launch<128>(a, 0, p.full, st);
         if (e != cudaSuccess)
             return e;
     }
@@ -661,16 +685,6 @@ cudaError_t launch_delta(const DeltaArgs &a, int q_slab, bool uniform, cudaStrea
     default:
         return cudaErrorInvalidValue;
     }
-}
-
-cudaError_t launch_apply_moves(float4 *pos, const float4 *moved_new, const int *moved_idx,
-                               int k, cudaStream_t st)
-{
-    if (k == 0)
-        return cudaSuccess;
-    apply_moves_kernel<<<(k + 255) / 256, 256, 0, st>>>(pos, moved_new, moved_idx, k);
-    count_launch();
-    return cudaGetLastError();
 }
 
 cudaError_t launch_f64_to_f32(const double *src, float *dst, int n, cudaStream_t st)

@@ -1,5 +1,7 @@
-// Autotuning cache for librsx: the winning tile shape (q-slab) of a problem
-// class, chosen by timing the candidates on the device on first use.
+// Autotuning cache for librsx: the winning tile shape of a problem class
+// (the q-slab plan, and for the wide forward the pairs a thread steps
+// together), chosen by timing the candidates on the device on first use.
+// Stored as q_slab + 1000 * (pairs_per_step == 4).
 //
 // Key: device name | kind | log2 size bucket | n_q | n_types | uniform | water.
 // The cache lives in the process; when RSX_AUTOTUNE_CACHE names a file it is
@@ -18,7 +20,8 @@ namespace rsx {
 
 static bool valid_q_slab(long v)
 {
-    return v == 8 || v == 16 || v == 32 || v == 64 || v == 128 || v == 192;
+    return v == 8 || v == 16 || v == 32 || v == 64 || v == 128 || v == 192 || v == 1128 ||
+           v == 1192;
 }
 
 static std::mutex g_mu;
@@ -39,8 +42,8 @@ static void load_file_locked()
         const auto sp = line.rfind(' ');
         if (sp == std::string::npos)
             continue;
-        // the file is outside the library's control: keep only q-slab sizes
-        // that rsx_debye_create accepts, so an edited or damaged line can
+        // the file is outside the library's control: keep only tile shapes
+        // that librsx has kernels for, so an edited or damaged line can
         // never select a kernel shape that does not exist
         char *end = nullptr;
         const long v = std::strtol(line.c_str() + sp + 1, &end, 10);

@@ -37,7 +37,18 @@ struct rsx_batch {
     float dq = 0.f;
     int small_theta = 0; // theta_level() the captured graphs were built with
     int q_slab = 64;
+    int pairs_per_step = 2; // wide main slabs of 128 q and more: 2 or 4
     bool autotune = false, tuned = false;
+    int sms = 152;
+
+    // implicit water (forward only): weight 0 leaves it out; rsasa is kept in
+    // caller order and staged per sorted slot with per-member sums
+    float water_weight = 0.f;
+    int water_index = 0;
+    std::vector<float> rsasa;
+    bool water_dirty = false;
+    float *d_rsasa = nullptr;       // [n_total] per sorted slot
+    double *d_water_sums = nullptr; // [M][T] by type, [M] of rsasa^2, [M] of rsasa
 
     // layout (rebuilt when any body type changes)
     bool have_layout = false;
@@ -120,7 +131,7 @@ rsx_status batch_release(rsx_batch *h)
     free_layout_buffers(h);
     void *dev[] = {h->d_pos,    h->d_ff,     h->d_q,      h->d_iq64,    h->d_iq32,
                    h->d_target, h->d_sigma, h->d_lambda, h->d_chi2,    h->d_grad,
-                   h->d_counter, h->d_adj_tab, h->d_adj_geom};
+                   h->d_counter, h->d_adj_tab, h->d_adj_geom, h->d_rsasa, h->d_water_sums};
     for (void *x : dev)
         dev_free(x);
     void *pin[] = {h->h_pos, h->h_iq, h->h_chi2, h->h_grad, h->h_adj_geom};
@@ -257,8 +268,50 @@ rsx_status build_batch_layout(rsx_batch *h, const rsx_body *bodies)
                "counts"));
     RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "batch layout");
     h->have_layout = true;
+    h->water_dirty = true; // new slot order
     drop_graphs(h);
     return RSX_OK;
+}
+
+bool has_water(const rsx_batch *h) { return h->water_weight != 0.f; }
+
+// rsasa per sorted slot and, per member, its sums by type, of squares and in
+// total (summed in caller order, as the single-structure handle does).
+rsx_status upload_water(rsx_batch *h)
+{
+    const int T = h->n_types, M = h->n_members;
+    std::vector<float> sorted((size_t)std::max(h->n_total, 1), 0.f);
+    std::vector<double> sums((size_t)M * T + 2 * (size_t)M, 0.0);
+    for (int m = 0; m < M; ++m) {
+        const int end = h->offsets[m] + h->sizes[m];
+        for (int i = h->offsets[m]; i < end; ++i) {
+            const double r = h->rsasa[i];
+            sums[(size_t)m * T + h->types[i]] += r;
+            sums[(size_t)M * T + m] += r * r;
+            sums[(size_t)M * T + M + m] += r;
+        }
+    }
+    for (int s = 0; s < h->n_total; ++s)
+        sorted[s] = h->rsasa[h->perm[s]];
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->d_rsasa, sorted.data(), sizeof(float) * sorted.size(),
+                                 cudaMemcpyHostToDevice, h->st),
+                 "upload rsasa");
+    if (!sums.empty())
+        RSX_TRY_CUDA(cudaMemcpyAsync(h->d_water_sums, sums.data(), sizeof(double) * sums.size(),
+                                     cudaMemcpyHostToDevice, h->st),
+                     "upload rsasa sums");
+    RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "upload water");
+    h->water_dirty = false;
+    return RSX_OK;
+}
+
+// The q slab the forward kernels run with: water keeps two accumulator sets
+// per thread, so its slabs stop at 16 q (128 q on the wide uniform path).
+int water_slab(const rsx_batch *h, int q_slab)
+{
+    if (!has_water(h) || (h->uniform && q_slab >= 64))
+        return q_slab;
+    return q_slab >= 16 ? 16 : 8;
 }
 
 DebyeArgs batch_args(rsx_batch *h, bool adjoint)
@@ -276,8 +329,14 @@ DebyeArgs batch_args(rsx_batch *h, bool adjoint)
     a.n_items = (int)(adjoint ? h->adj_items.size() : h->items.size());
     a.dq = h->dq;
     a.small_theta = h->small_theta;
+    a.pairs4 = h->pairs_per_step == 4 ? 1 : 0;
     a.lambda = h->d_lambda;
     a.grad = h->d_grad;
+    if (!adjoint && has_water(h)) {
+        a.rsasa = h->d_rsasa;
+        a.water_weight = h->water_weight;
+        a.water_index = h->water_index;
+    }
     return a;
 }
 
@@ -291,25 +350,24 @@ rsx_status enqueue_pass(rsx_batch *h, bool with_adjoint, int q_slab)
     RSX_TRY_CUDA(cudaMemsetAsync(h->d_counter, 0, sizeof(int) * 4, h->st), "counters");
     const DebyeArgs a = batch_args(h, false);
     const int n_items = (int)h->items.size();
+    const bool water = has_water(h);
     const bool wide = h->uniform && q_slab >= 64;
-    if (wide) {
-        int sms = 152;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
-        RSX_TRY_CUDA(launch_batch_forward_wide(a, h->d_order, n_items, q_slab, h->d_counter, sms,
-                                               h->st),
+    if (wide)
+        RSX_TRY_CUDA(launch_batch_forward_wide(a, h->d_order, n_items, q_slab, h->d_counter,
+                                               h->sms, h->st, water),
                      "batch forward");
-    }
-    const int full = wide ? 0 : h->n_q / q_slab, rest = wide ? 0 : h->n_q - full * q_slab;
+    const int slab = water_slab(h, q_slab);
+    const int full = wide ? 0 : h->n_q / slab, rest = wide ? 0 : h->n_q - full * slab;
     if (full > 0)
-        RSX_TRY_CUDA(launch_batch_forward(a, h->d_order, n_items, q_slab, full, 0, h->uniform,
-                                          h->d_counter + 0, h->fwd_grid, h->st),
+        RSX_TRY_CUDA(launch_batch_forward(a, h->d_order, n_items, slab, full, 0, h->uniform,
+                                          h->d_counter + 0, h->fwd_grid, h->st, water),
                      "batch forward");
     if (rest > 0) {
         const int tail = rest <= 8 ? 8 : (rest <= 16 ? 16 : 32);
         const int n_tail = (rest + tail - 1) / tail;
-        const int grid = batch_forward_grid(tail, h->uniform, h->fwd_grid / std::max(1, batch_forward_grid(q_slab, h->uniform, 1)));
-        RSX_TRY_CUDA(launch_batch_forward(a, h->d_order, n_items, tail, n_tail, full * q_slab,
-                                          h->uniform, h->d_counter + 1, grid, h->st),
+        const int grid = batch_forward_grid(tail, h->uniform, h->sms, water);
+        RSX_TRY_CUDA(launch_batch_forward(a, h->d_order, n_items, tail, n_tail, full * slab,
+                                          h->uniform, h->d_counter + 1, grid, h->st, water),
                      "batch forward tail");
     }
     BatchAssembleArgs b{};
@@ -324,6 +382,15 @@ rsx_status enqueue_pass(rsx_batch *h, bool with_adjoint, int q_slab)
     b.n_members = h->n_members;
     b.iq64 = h->d_iq64;
     b.iq32 = h->d_iq32;
+    if (water) {
+        const size_t MT = (size_t)h->n_members * h->n_types;
+        b.rsasa_sum = h->d_water_sums;
+        b.rsasa_sq = h->d_water_sums + MT;
+        b.rsasa_tot = h->d_water_sums + MT + h->n_members;
+        b.water_weight = h->water_weight;
+        b.water_index = h->water_index;
+        b.has_water = 1;
+    }
     RSX_TRY_CUDA(launch_batch_assemble(b, h->st), "batch assemble");
     if (with_adjoint) {
         BatchLossArgs l{};
@@ -371,10 +438,11 @@ rsx_status enqueue_pass(rsx_batch *h, bool with_adjoint, int q_slab)
 
 rsx_status capture(rsx_batch *h, bool with_adjoint, cudaGraphExec_t *out)
 {
-    h->fwd_grid = batch_forward_grid(h->q_slab, h->uniform, 1);
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
-    h->fwd_grid *= sms;
+    h->sms = sms;
+    h->fwd_grid = batch_forward_grid(water_slab(h, h->q_slab), h->uniform, sms,
+                                     has_water(h) && !(h->uniform && h->q_slab >= 64));
     h->adj_grid = batch_adjoint_grid(h->q_slab, h->uniform, h->n_q, sms);
     h->adj_table_grid = batch_adjoint_table_grid(sms);
     RSX_TRY_CUDA(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal),
@@ -484,16 +552,25 @@ rsx_status run_graph(rsx_batch *h, cudaGraphExec_t g)
     return RSX_OK;
 }
 
-// Times one forward pass with each candidate q-slab and keeps the fastest.
+// Times one forward pass with each candidate tile shape (q-slab plan, and
+// for the wide slabs of 128 q and more the pairs stepped together; encoded as
+// q_slab + 1000 * (pairs_per_step == 4)) and keeps the fastest.
 rsx_status tune(rsx_batch *h)
 {
-    const int candidates[] = {32, 64, 128};
+    const int candidates[] = {32, 64, 128, 1128, 192, 1192};
     float best = 1e30f;
-    int best_qs = h->q_slab;
-    for (int qs : candidates) {
+    int best_qs = h->q_slab, best_pp = h->pairs_per_step;
+    for (int c : candidates) {
+        const int qs = c % 1000;
         if (qs >= 64 && !h->uniform)
             continue;
+        if (qs == 192 && h->n_q < 192)
+            continue;
+        // the water kernels step two pairs and stop at 128 q per slab
+        if (has_water(h) && (c >= 1000 || qs == 192))
+            continue;
         h->q_slab = qs;
+        h->pairs_per_step = c >= 1000 ? 4 : 2;
         cudaGraphExec_t g = nullptr;
         RSX_TRY(capture(h, false, &g));
         rsx_status s = run_graph(h, g); // warm
@@ -504,9 +581,11 @@ rsx_status tune(rsx_batch *h)
         if (h->last_ms < best) {
             best = h->last_ms;
             best_qs = qs;
+            best_pp = h->pairs_per_step;
         }
     }
     h->q_slab = best_qs;
+    h->pairs_per_step = best_pp;
     h->tuned = true;
     return RSX_OK;
 }
@@ -532,8 +611,10 @@ rsx_status rsx_batch_create(const float *q, int n_q, const float *t_factors, int
     if (opts)
         o = *opts;
     if (o.q_slab != 0 && o.q_slab != 8 && o.q_slab != 16 && o.q_slab != 32 && o.q_slab != 64 &&
-        o.q_slab != 128)
-        return fail(RSX_INVALID_ARG, "q_slab must be 0, 8, 16, 32, 64 or 128");
+        o.q_slab != 128 && o.q_slab != 192)
+        return fail(RSX_INVALID_ARG, "q_slab must be 0, 8, 16, 32, 64, 128 or 192");
+    if (o.pairs_per_step != 0 && o.pairs_per_step != 2 && o.pairs_per_step != 4)
+        return fail(RSX_INVALID_ARG, "pairs_per_step must be 0, 2 or 4");
     long long total = 0;
     for (int m = 0; m < n_members; ++m) {
         if (member_sizes[m] < 0)
@@ -570,10 +651,11 @@ rsx_status rsx_batch_create(const float *q, int n_q, const float *t_factors, int
             h->uniform = std::fabs((double)q[k] - (q0 + k * step)) <= 4e-7 * std::fabs((double)q[k]) + 1e-30;
         h->dq = (float)step;
     }
-    h->q_slab = o.q_slab ? o.q_slab : (h->uniform && n_q >= 64 ? 128 : 32);
+    h->q_slab = o.q_slab ? o.q_slab : (h->uniform && n_q >= 64 ? 192 : 32);
     if (!h->uniform && h->q_slab > 32)
         h->q_slab = 32;
-    h->autotune = o.autotune != 0 && o.q_slab == 0;
+    h->pairs_per_step = o.pairs_per_step ? o.pairs_per_step : 2;
+    h->autotune = o.autotune != 0 && o.q_slab == 0 && o.pairs_per_step == 0;
     h->pair_tables = o.no_pair_tables == 0;
     auto bail = [&](rsx_status s) {
         batch_release(h);
@@ -639,6 +721,8 @@ rsx_status rsx_batch_forward(rsx_batch *h, const rsx_body *bodies, float *out_iq
         return fail(RSX_INVALID_ARG, "null bodies / output");
     RSX_TRY_CUDA(cudaSetDevice(h->device), "cudaSetDevice");
     RSX_TRY(stage_bodies(h, bodies));
+    if (has_water(h) && h->water_dirty)
+        RSX_TRY(upload_water(h));
     if (h->autotune && !h->tuned) {
         drop_graphs(h);
         RSX_TRY(tune(h));
@@ -679,6 +763,8 @@ rsx_status rsx_batch_forward_chi2_backward(rsx_batch *h, const rsx_body *bodies,
         return fail(RSX_ALG_NOT_INITIALIZED, "null rsx_batch handle");
     if (!h->have_targets)
         return fail(RSX_ARGS_NOT_SET, "rsx_batch_set_targets was not called");
+    if (has_water(h))
+        return fail(RSX_NOT_SUPPORTED, "the batched adjoint has no implicit water term");
     if ((!bodies && h->n_total > 0))
         return fail(RSX_INVALID_ARG, "null bodies");
     RSX_TRY_CUDA(cudaSetDevice(h->device), "cudaSetDevice");
@@ -697,6 +783,56 @@ rsx_status rsx_batch_forward_chi2_backward(rsx_batch *h, const rsx_body *bodies,
             grad_xyz[3 * c + 1] = (float)h->h_grad[3 * s + 1];
             grad_xyz[3 * c + 2] = (float)h->h_grad[3 * s + 2];
         }
+    return ok();
+}
+
+rsx_status rsx_batch_set_factors(rsx_batch *h, const float *t_factors, int n_factors)
+{
+    if (!h)
+        return fail(RSX_ALG_NOT_INITIALIZED, "null rsx_batch handle");
+    if (!t_factors || n_factors != h->n_types)
+        return fail(RSX_INVALID_ARG, "factor table must have the handle's n_factors columns");
+    RSX_TRY_CUDA(cudaSetDevice(h->device), "cudaSetDevice");
+    h->ff.assign(t_factors, t_factors + (size_t)h->n_q * n_factors);
+    // the captured graphs read the table from d_ff
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->d_ff, h->ff.data(), sizeof(float) * h->ff.size(),
+                                 cudaMemcpyHostToDevice, h->st),
+                 "factors");
+    RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "factors");
+    return ok();
+}
+
+rsx_status rsx_batch_set_water(rsx_batch *h, float weight, int water_index, const float *rsasa)
+{
+    if (!h)
+        return fail(RSX_ALG_NOT_INITIALIZED, "null rsx_batch handle");
+    if (water_index < 0 || water_index >= h->n_types)
+        return fail(RSX_INVALID_ARG, "water_index outside the factor table");
+    if (!std::isfinite(weight))
+        return fail(RSX_INVALID_ARG, "water weight must be finite");
+    if (weight != 0.f && !rsasa && h->rsasa.empty())
+        return fail(RSX_INVALID_ARG, "a non-zero water weight needs rsasa");
+    RSX_TRY_CUDA(cudaSetDevice(h->device), "cudaSetDevice");
+    if (weight != 0.f && !h->d_rsasa) {
+        const size_t M = (size_t)std::max(h->n_members, 1);
+        RSX_TRY(dev_alloc((void **)&h->d_rsasa, sizeof(float) * std::max(h->n_total, 1),
+                          "rsasa"));
+        RSX_TRY(dev_alloc((void **)&h->d_water_sums,
+                          sizeof(double) * (M * h->n_types + 2 * M), "rsasa sums"));
+    }
+    if (rsasa) {
+        for (int i = 0; i < h->n_total; ++i)
+            if (!std::isfinite(rsasa[i]))
+                return fail(RSX_INVALID_ARG, "rsasa must be finite");
+        h->rsasa.assign(rsasa, rsasa + h->n_total);
+        h->water_dirty = true;
+    }
+    // weight and water column are arguments of the captured kernels
+    // (a tile shape tuned without water runs capped at 128 q and two pairs)
+    if (weight != h->water_weight || water_index != h->water_index)
+        drop_graphs(h);
+    h->water_weight = weight;
+    h->water_index = water_index;
     return ok();
 }
 

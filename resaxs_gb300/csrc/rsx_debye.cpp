@@ -162,6 +162,7 @@ struct rsx_debye {
     float dq = 0.f;
     float lo[3] = {0.f, 0.f, 0.f}, hi[3] = {0.f, 0.f, 0.f}; // extent of the device bodies
     int q_slab = 32;
+    int pairs_per_step = 2; // wide forward main slabs of 128 q and more: 2 or 4
     int max_items = 16384;
     bool autotune = false, tuned = false;
     bool pair_tables = true; // tabulated adjoint, gridded non-uniform forward
@@ -413,6 +414,7 @@ DebyeArgs debye_args(rsx_debye *h)
     a.n_items = (int)h->L.items.size();
     a.dq = h->dq;
     a.small_theta = small_theta(h);
+    a.pairs4 = h->pairs_per_step == 4 ? 1 : 0;
     a.water_weight = h->water_weight;
     a.water_index = h->water_index;
     return a;
@@ -525,9 +527,11 @@ rsx_status read_curve(rsx_debye *h, float *out_iq)
     return RSX_OK;
 }
 
-// Picks the q-slab of the forward kernel for this problem class: the cached
-// winner, or the fastest candidate timed here (two timed runs each, after a
-// warm-up) on the bodies just uploaded.
+// Picks the tile shape of the forward for this problem class -- the q-slab
+// plan and, for the wide slabs of 128 q and more, the pairs a thread steps
+// together -- as the cached winner, or the fastest candidate timed here (two
+// timed runs each, after a warm-up) on the bodies just uploaded.  The cache
+// holds q_slab + 1000 * (pairs_per_step == 4).
 rsx_status tune_slab(rsx_debye *h)
 {
     h->tuned = true;
@@ -535,15 +539,21 @@ rsx_status tune_slab(rsx_debye *h)
                                          h->uniform, has_water(h));
     int qs = 0;
     if (autotune_lookup(key, &qs)) {
-        h->q_slab = qs;
+        h->q_slab = qs % 1000;
+        h->pairs_per_step = qs >= 1000 ? 4 : 2;
         return RSX_OK;
     }
     std::vector<int> cands = {16, 32};
     if (h->uniform) {
         cands.push_back(64);
         cands.push_back(128);
-        if (!has_water(h) && h->n_q >= 192)
-            cands.push_back(192);
+        if (!has_water(h)) {
+            cands.push_back(1128);
+            if (h->n_q >= 192) {
+                cands.push_back(192);
+                cands.push_back(1192);
+            }
+        }
     }
     cudaEvent_t e0, e1;
     RSX_TRY_CUDA(cudaEventCreate(&e0), "event");
@@ -554,7 +564,8 @@ rsx_status tune_slab(rsx_debye *h)
     const bool timing = h->timing;
     h->timing = false;
     for (int c : cands) {
-        h->q_slab = c;
+        h->q_slab = c % 1000;
+        h->pairs_per_step = c >= 1000 ? 4 : 2;
         float t_min = 1e30f;
         for (int rep = 0; rep < 3 && st == RSX_OK; ++rep) {
             cudaEventRecord(e0, h->st);
@@ -577,7 +588,8 @@ rsx_status tune_slab(rsx_debye *h)
     h->timing = timing;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    h->q_slab = best_qs;
+    h->q_slab = best_qs % 1000;
+    h->pairs_per_step = best_qs >= 1000 ? 4 : 2;
     if (st == RSX_OK)
         autotune_store(key, best_qs);
     return st;
@@ -705,16 +717,21 @@ rsx_status delta_update(rsx_debye *h, const rsx_body *moved, const unsigned *idx
     a.n_mtiles = (int)tiles.size();
     a.max_groups = kDeltaGroups;
     a.dq = h->dq;
+    // the extent already holds the moved bodies' new positions (recalc_common
+    // grows it first), so the level covers the pairs before and after the move
+    a.small_theta = small_theta(h);
     int *d_idx = reinterpret_cast<int *>(h->d_moved + off_idx);
     if (h->timing)
         RSX_TRY_CUDA(cudaEventRecord(h->ev_k0, h->st), "event");
     RSX_LAUNCH(launch_delta(a, slab_for(h), h->uniform, h->st, &h->aux), "delta kernel");
     if (h->timing)
         RSX_TRY_CUDA(cudaEventRecord(h->ev_k1, h->st), "event");
-    RSX_LAUNCH(launch_assemble(assemble_args(h, delta_parts(a, slab_for(h), h->uniform), 1),
-                               h->st),
-               "assemble delta");
-    RSX_LAUNCH(launch_apply_moves(h->d_pos, a.moved_new, d_idx, (int)k, h->st), "apply moves");
+    AssembleArgs as = assemble_args(h, delta_parts(a, slab_for(h), h->uniform), 1);
+    as.apply_pos = h->d_pos;
+    as.apply_new = a.moved_new;
+    as.apply_idx = d_idx;
+    as.apply_k = (int)k;
+    RSX_LAUNCH(launch_assemble(as, h->st), "assemble delta and apply moves");
     return RSX_OK;
 }
 
@@ -745,8 +762,8 @@ rsx_status recalc_common(rsx_debye *h, const rsx_body *moved, const unsigned *id
             next[idx[m]] = moved[m];
         RSX_TRY(full_calc(h, next.data()));
     } else if (k > 0) {
+        grow_extent(h, moved, k); // an upper bound of every pair distance, old and new
         RSX_TRY(delta_update(h, moved, idx, k));
-        grow_extent(h, moved, k);
         for (unsigned m = 0; m < k; ++m)
             h->cur[idx[m]] = moved[m];
     }
@@ -813,6 +830,8 @@ rsx_status rsx_debye_create(const float *q, int n_q, const float *t_factors, int
     if (o.q_slab != 0 && o.q_slab != 8 && o.q_slab != 16 && o.q_slab != 32 && o.q_slab != 64 &&
         o.q_slab != 128 && o.q_slab != 192)
         return fail(RSX_INVALID_ARG, "q_slab must be 0, 8, 16, 32, 64, 128 or 192");
+    if (o.pairs_per_step != 0 && o.pairs_per_step != 2 && o.pairs_per_step != 4)
+        return fail(RSX_INVALID_ARG, "pairs_per_step must be 0, 2 or 4");
     int dev = -1;
     RSX_TRY(select_device(o.device, &dev));
     DeviceGuard g(dev);
@@ -829,7 +848,8 @@ rsx_status rsx_debye_create(const float *q, int n_q, const float *t_factors, int
     // measured costs) on uniform grids of 64 q or more, otherwise 32 / 16 / 8
     h->q_slab = o.q_slab ? o.q_slab
                          : (h->uniform && n_q >= 64 ? 192 : (n_q >= 32 ? 32 : (n_q >= 16 ? 16 : 8)));
-    h->autotune = o.autotune != 0 && o.q_slab == 0;
+    h->pairs_per_step = o.pairs_per_step ? o.pairs_per_step : 2;
+    h->autotune = o.autotune != 0 && o.q_slab == 0 && o.pairs_per_step == 0;
     h->max_items = o.max_items > 0 ? o.max_items : 16384;
     h->timing = o.timing != 0;
     h->pair_tables = o.no_pair_tables == 0;
@@ -1266,6 +1286,17 @@ rsx_status rsx_debye_chi2_backward(rsx_debye *h, const float *target, const floa
         *chi2 = c2;
     if (grad_xyz)
         RSX_TRY(rsx_debye_backward(h, lam.data(), grad_xyz));
+    return ok();
+}
+
+rsx_status rsx_debye_tile_shape(rsx_debye *h, int *q_slab, int *pairs_per_step)
+{
+    if (!h)
+        return fail(RSX_ALG_NOT_INITIALIZED, "null rsx_debye handle");
+    if (q_slab)
+        *q_slab = forward_slab(h);
+    if (pairs_per_step)
+        *pairs_per_step = h->pairs_per_step;
     return ok();
 }
 

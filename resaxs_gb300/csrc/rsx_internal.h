@@ -49,6 +49,7 @@ struct DebyeArgs {
     int k_base;              // first q index of the launch (set by the launcher)
     float dq;                // uniform q step (rotation path)
     int small_theta;         // theta_level() of the launch's bodies
+    int pairs4;              // 1: the wide main slabs step 4 pairs at a time (else 2)
     float water_weight;      // w (water path)
     int water_index;         // column of the water factor
     // adjoint
@@ -82,6 +83,12 @@ struct AssembleArgs {
     double *iq64;            // [n_q] result (or accumulation target)
     float *iq32;             // [n_q] FP32 copy of iq64
     int accumulate;          // 1: iq64 += 2*cross/q (incremental mode, no self terms)
+    // incremental mode: the moved bodies take their new positions in the same
+    // launch (extra CTAs past the n_q assembling ones), pos[idx[m]] = new[m]
+    float4 *apply_pos;
+    const float4 *apply_new;
+    const int *apply_idx;
+    int apply_k;
 };
 
 // Moved-set description for the incremental kernel.
@@ -96,6 +103,7 @@ struct DeltaArgs {
     int n, k, n_q, n_types, n_blocks, n_mtiles;
     int max_groups;          // cap on the moved-list groups (partial holds n_blocks * groups rows)
     float dq;
+    int small_theta;         // theta_level() of the bodies before and after the move
 };
 
 constexpr int kDeltaGroups = 8; // moved-list groups of the wide delta kernel
@@ -144,8 +152,6 @@ cudaError_t launch_delta(const DeltaArgs &a, int q_slab, bool uniform, cudaStrea
 // partial sums per q that launch_delta writes (the assembly's n_parts)
 int delta_parts(const DeltaArgs &a, int q_slab, bool uniform);
 int delta_groups(const DeltaArgs &a);
-cudaError_t launch_apply_moves(float4 *pos, const float4 *moved_new, const int *moved_idx,
-                               int k, cudaStream_t st);
 cudaError_t launch_f64_to_f32(const double *src, float *dst, int n, cudaStream_t st);
 cudaError_t launch_adjoint(const DebyeArgs &a, int q_slab, bool uniform, bool water,
                            cudaStream_t st);

@@ -42,7 +42,7 @@ class Debye:
 
     def __init__(self, q, factors, n_bodies: int, *, device: int = -1, q_slab: int = 0,
                  max_items: int = 0, force_general_q: bool = False, timing: bool = False,
-                 autotune: bool = False, pair_tables: bool = True):
+                 autotune: bool = False, pair_tables: bool = True, pairs_per_step: int = 0):
         self.q = _f32(q)
         factors = _f32(factors)
         if factors.ndim != 2 or factors.shape[0] != len(self.q):
@@ -59,6 +59,7 @@ class Debye:
         opts.timing = int(timing)
         opts.autotune = int(autotune)
         opts.no_pair_tables = int(not pair_tables)
+        opts.pairs_per_step = int(pairs_per_step)
         h = ctypes.c_void_p()
         check(lib().rsx_debye_create(self.q, self.n_q, factors.reshape(-1), self.n_factors,
                                      self.n, ctypes.byref(opts), ctypes.byref(h)))
@@ -185,9 +186,11 @@ class Debye:
         return c2.value, g
 
     def config(self):
-        qs, ni, un = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        qs, ni, un, pp = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         check(lib().rsx_debye_config(self._h, ctypes.byref(qs), ctypes.byref(ni), ctypes.byref(un)))
-        return {"q_slab": qs.value, "n_items": ni.value, "uniform_q": bool(un.value)}
+        check(lib().rsx_debye_tile_shape(self._h, None, ctypes.byref(pp)))
+        return {"q_slab": qs.value, "n_items": ni.value, "uniform_q": bool(un.value),
+                "pairs_per_step": pp.value}
 
 
 # ---------------------------------------------------------------------------

@@ -173,3 +173,105 @@ def test_batch_errors():
                 call()
             assert e.value.code == _lib.RSX_INVALID_ARG
         assert np.all(np.isfinite(b.forward(good)))
+
+
+@pytest.mark.parametrize("q_slab,pairs", [(128, 4), (192, 2), (192, 4)])
+def test_batch_tile_shapes(oracle_lib, ensemble, q_slab, pairs):
+    """Every tile shape the batch tuner chooses from gives the oracle's curves."""
+    from resaxs_gb300.batch import DebyeBatch
+    q, ff, members = ensemble
+    with DebyeBatch(q, ff, [len(m) for m in members], q_slab=q_slab,
+                    pairs_per_step=pairs) as b:
+        out = b.forward(members)
+    for m, body in enumerate(members):
+        if len(body) > 0:
+            assert rel(out[m], oracle_lib.debye_f64(q, body, ff)) < TOL, m
+
+
+def test_batch_autotuned_tile_shape(oracle_lib, ensemble):
+    from resaxs_gb300.batch import DebyeBatch
+    q, ff, members = ensemble
+    with DebyeBatch(q, ff, [len(m) for m in members], autotune=True) as b:
+        out = b.forward(members)
+        cfg = b.config()
+    assert cfg["q_slab"] in (32, 64, 128, 192)
+    for m, body in enumerate(members):
+        if len(body) > 0:
+            assert rel(out[m], oracle_lib.debye_f64(q, body, ff)) < TOL, m
+
+
+@pytest.mark.parametrize("q_slab,general,ww", [(0, False, 0.8), (16, False, -1.5), (32, False, 2.0),
+                                               (64, False, 0.8), (128, False, 3.0),
+                                               (192, False, 0.8), (0, True, 0.8), (8, True, -1.5)])
+def test_batch_water(oracle_lib, ensemble, q_slab, general, ww):
+    """The implicit water term in the batched forward (f~_i = f_t + w rsasa_i
+    f_w): every member against the FP64 oracle with its own rsasa; new rsasa at
+    the same weight reaches the next replay; weight 0 gives the dry curves."""
+    from resaxs_gb300.batch import DebyeBatch
+    q, ff, members = ensemble
+    sizes = [len(m) for m in members]
+    rng = np.random.default_rng(q_slab + 7 * general)
+    rs = rng.uniform(0, 1, sum(sizes)).astype(np.float32)
+    rs2 = rng.uniform(0, 1, sum(sizes)).astype(np.float32)
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    with DebyeBatch(q, ff, sizes, q_slab=q_slab, force_general_q=general) as b:
+        dry = b.forward(members)
+        for r in (rs, rs2):
+            b.set_water(ww, 4, r)
+            out = b.forward(members)
+            for m, body in enumerate(members):
+                if len(body) == 0:
+                    assert np.all(out[m] == 0)
+                    continue
+                ref = oracle_lib.debye_f64(q, body, ff, rsasa=r[off[m]:off[m + 1]],
+                                           water_weight=ww, water_index=4)
+                assert rel(out[m], ref) < TOL, (m, rel(out[m], ref))
+        b.set_water(0.0, 4)
+        assert np.array_equal(b.forward(members), dry)
+
+
+def test_batch_water_autotuned_and_factors(oracle_lib, ensemble):
+    """A tuned handle with water, then a new factor table (as an expansion
+    factor changes it) under the same water weight."""
+    from resaxs_gb300.batch import DebyeBatch
+    q, ff, members = ensemble
+    sizes = [len(m) for m in members]
+    rs = np.random.default_rng(11).uniform(0, 1, sum(sizes)).astype(np.float32)
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    ff2 = (ff * np.float32(1.07)).astype(np.float32)
+    with DebyeBatch(q, ff, sizes, autotune=True) as b:
+        b.set_water(1.3, 2, rs)
+        for table in (ff, ff2):
+            b.set_factors(table)
+            out = b.forward(members)
+            assert b.config()["q_slab"] in (32, 64, 128)
+            for m, body in enumerate(members):
+                if len(body) > 0:
+                    ref = oracle_lib.debye_f64(q, body, table, rsasa=rs[off[m]:off[m + 1]],
+                                               water_weight=1.3, water_index=2)
+                    assert rel(out[m], ref) < TOL, m
+
+
+def test_batch_water_errors(ensemble):
+    from resaxs_gb300 import _lib
+    from resaxs_gb300.batch import DebyeBatch
+    q, ff, members = ensemble
+    sizes = [len(m) for m in members]
+    with DebyeBatch(q, ff, sizes) as b:
+        for call in (lambda: b.set_water(0.5, 1),                       # no rsasa yet
+                     lambda: b.set_water(0.5, 5, np.zeros(sum(sizes))),   # column 5 of 5
+                     lambda: b.set_water(np.inf, 1, np.zeros(sum(sizes))),
+                     lambda: b.set_water(0.5, 1, np.zeros(sum(sizes) - 1)),
+                     lambda: b.set_factors(ff[:, :4])):
+            with pytest.raises(_lib.ResaxsError) as e:
+                call()
+            assert e.value.code == _lib.RSX_INVALID_ARG
+        b.set_water(0.5, 1, np.zeros(sum(sizes), np.float32))
+        b.set_targets(np.ones((len(sizes), len(q)), np.float32),
+                      np.ones((len(sizes), len(q)), np.float32))
+        with pytest.raises(_lib.ResaxsError) as e:
+            b.forward_chi2_backward(members)
+        assert e.value.code == _lib.RSX_NOT_SUPPORTED
+        b.set_water(0.0, 1)
+        _, chi2, _ = b.forward_chi2_backward(members)
+        assert np.all(np.isfinite(chi2))

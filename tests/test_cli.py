@@ -144,17 +144,19 @@ def _oracle_curve(oracle_lib, q, models, ef, ww, rsasa=None):
 
 
 def _oracle_rsasa(oracle_lib, models):
-    from resaxs_gb300 import _lib, sasa
-    from resaxs_gb300 import workloads as W
+    """rsasa of each model as the CLI computes it: the reference GPU
+    algorithm's dot map (create_dodeca_icosa_dots per atomic radius, probe
+    1.8 A, 32 dots per type)."""
+    from resaxs_gb300 import _lib
+    from resaxs_gb300.sasa import reference_dot_map
     L = _lib.lib()
     radii16 = np.zeros(16, np.float32)
     _lib.check(L.rsx_ff_radii(radii16))
-    dots = sasa.dodeca_icosa_dots()
+    ico = reference_dot_map(radii16, "dodeca_icosa", 1.8)
     out = []
     for b in models:
-        r = radii16[W.body_types(b)]
-        cnt = oracle_lib.sasa_counts(b, r, dots, 1.8)
-        out.append((cnt / float(len(dots))).astype(np.float32))
+        cnt = oracle_lib.sasa_counts_typed(b, radii16, ico, 1.8)
+        out.append((cnt.astype(np.float32) / np.float32(32)))
     return out
 
 
@@ -176,6 +178,29 @@ def test_cli_fixed_parameters_curve(cli, tmp_path, oracle_lib):
     assert params["expansion factor"] == 1
     np.testing.assert_allclose(qq, np.round(q.astype(np.float64), 6), atol=1e-6)
     # 1e-5 relative, plus the 6 decimals the output format keeps
+    np.testing.assert_allclose(iq, ref, rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.gpu
+def test_cli_fixed_water_and_expansion(cli, tmp_path, oracle_lib):
+    """Fixed water weight and expansion factor: the ensemble average (one
+    batched pass over the models) with the oracle's rsasa on the reference
+    dot map."""
+    pdb = os.path.join(GOLD, "synthetic_a.pdb")
+    bodies, sizes = _read_pdb(pdb)
+    models = np.split(bodies, np.cumsum(sizes)[:-1])
+    assert len(models) > 1
+    q = np.linspace(0.0, 0.5, 101).astype(np.float32)
+    rsasa = _oracle_rsasa(oracle_lib, models)
+    ref = 1.5 * _oracle_curve(oracle_lib, q, models, 1.03, 1.2, rsasa)
+    prof = tmp_path / "p.dat"
+    _write_profile(prof, q, ref)
+    r = _run(cli, ["-s", "1.5", "-w", "1.2", "-e", "1.03", "-f", str(prof), "-o", "out.dat",
+                   pdb], tmp_path)
+    assert r.returncode == 0, r.stderr
+    params, qq, iq = _read_output(tmp_path / "out.dat")
+    assert params["water weight"] == pytest.approx(1.2) and params["expansion factor"] == \
+        pytest.approx(1.03)
     np.testing.assert_allclose(iq, ref, rtol=1e-5, atol=1e-6)
 
 

@@ -323,12 +323,43 @@ def test_full_size_config2_q_subset_vs_oracle(saxs, oracle_lib):
     assert rel(out64[sel], ref) < TOL
 
 
+@pytest.mark.parametrize("q_slab,n_q", [(128, 300), (192, 512), (192, 450)])
+def test_four_pairs_per_step(saxs, oracle_lib, q_slab, n_q):
+    """The second tile dimension: four pairs stepped together in the wide
+    main slabs (128 q and more); the tail slab keeps two."""
+    rng = np.random.default_rng(n_q)
+    w = W.make_config(4, seed=23, n_override=700)
+    q = W.q_grid(n_q, 1.0)
+    ff = W.exp_form_factors(q, W.Z8, rng.uniform(0.3, 2.5, 8))
+    with saxs.Debye(q, ff, w.n, q_slab=q_slab, pairs_per_step=4) as d:
+        d.calc(w.bodies)
+        out64 = d.curve_f64()
+        cfg = d.config()
+    assert cfg["pairs_per_step"] == 4 and cfg["q_slab"] == q_slab
+    assert rel(out64, oracle_lib.debye_f64(q, w.bodies, ff)) < TOL
+    # a spread structure takes the signed instantiation
+    b = w.bodies.copy()
+    b[0, :3] += np.float32(500.0)
+    with saxs.Debye(q, ff, w.n, q_slab=q_slab, pairs_per_step=4) as d:
+        d.calc(b)
+        out64 = d.curve_f64()
+    assert rel(out64, oracle_lib.debye_f64(q, b, ff)) < TOL
+
+
+def test_tile_shape_options_rejected(saxs):
+    from resaxs_gb300 import _lib
+    w = W.make_config(1, seed=5, n_override=50)
+    with pytest.raises(_lib.ResaxsError):
+        saxs.Debye(w.q, w.ff, w.n, pairs_per_step=3)
+
+
 def test_autotuned_slab(saxs, oracle_lib):
     from resaxs_gb300 import _lib
     _lib.lib().rsx_autotune_clear()
     w = W.make_config(2, seed=18, n_override=3000)
     _, out64, cfg = gpu_curve(saxs, w.q, w.ff, w.bodies, autotune=True)
     assert cfg["q_slab"] in (16, 32, 64, 128, 192)
+    assert cfg["pairs_per_step"] in (2, 4)
     assert rel(out64, oracle_lib.debye_f64(w.q, w.bodies, w.ff)) < TOL
     _, again, cfg2 = gpu_curve(saxs, w.q, w.ff, w.bodies, autotune=True)   # cached choice
     assert cfg2["q_slab"] == cfg["q_slab"]

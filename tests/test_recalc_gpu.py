@@ -22,12 +22,13 @@ def S():
 
 
 @pytest.mark.parametrize("q_slab,n_q", [(0, 201), (32, 201), (16, 201), (128, 101),
-                                         (128, 256), (64, 150), (64, 40)])
+                                         (128, 256), (64, 150), (64, 40), (0, 113),
+                                         (0, 384), (0, 450), (0, 97)])
 def test_recalc_indices_matches_full_recompute(S, oracle_lib, q_slab, n_q):
     """Config-2 style moves (k random bodies, Gaussian sigma 0.5 A) at a size the
     oracle recomputes quickly; every step is checked.  The slab sizes and q
-    counts cover the wide delta slabs (64-q main slabs, every tail shape) and
-    the 16 / 32-q kernel."""
+    counts cover the wide delta slabs (main slabs of 64 to 128 q, remainder
+    slabs up to 128 q wide) and the 16 / 32-q kernel."""
     w = W.make_config(2, seed=21, n_override=1200)
     q = W.q_grid(n_q, 0.5)
     ff = W.exp_form_factors(q, W.Z5, np.random.default_rng(n_q).uniform(0.5, 2.0, 5))
