@@ -31,6 +31,35 @@ __device__ __forceinline__ void warp_reduce_scatter(float (&v)[QS], int lane)
     }
 }
 
+// Warp-wide sums of 32 q values through shared memory: lane L stores its value
+// of q index k at buf[k][L] (row stride kSumStride floats), then sums row L
+// (the 32 lanes' values of q index L) with FP32x2 adds.  32 stores, 8 vector
+// loads and 16 adds, against 31 shuffles, 31 adds and 62 selects for the
+// shuffle reduce-scatter; both are bank-conflict free.  buf: 32 * kSumStride
+// floats owned by the warp.
+constexpr int kSumStride = 36;
+
+template <typename F>
+__device__ __forceinline__ float warp_sum_rows(F &&value_of, float *buf, int lane)
+{
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < 32; ++k)
+        buf[k * kSumStride + lane] = value_of(k);
+    __syncwarp();
+    const float4 *row = reinterpret_cast<const float4 *>(buf + lane * kSumStride);
+    float4 v = row[0];
+    float2 s0 = make_float2(v.x, v.y), s1 = make_float2(v.z, v.w);
+#pragma unroll
+    for (int j = 1; j < 8; ++j) {
+        v = row[j];
+        s0 = __fadd2_rn(s0, make_float2(v.x, v.y));
+        s1 = __fadd2_rn(s1, make_float2(v.z, v.w));
+    }
+    s0 = __fadd2_rn(s0, s1);
+    return s0.x + s0.y;
+}
+
 __device__ __forceinline__ void kahan_add(float &acc, float &comp, float x)
 {
     const float y = x - comp;
@@ -258,9 +287,11 @@ __device__ __forceinline__ float2 splat2(float x) { return make_float2(x, x); }
 // (q_{2m}, q_{2m+1}).  SIGNED adds the odd steps with the pairs' signs;
 // warps whose pairs all have sign +1 (compact structures: all of them) take
 // the plain adds.
+// The chains' states after the QS q are left in a.s, a.d and b.s, b.d, so a
+// following slab can continue them without a new seed (QS / 2 must then be
+// even for the signs of the odd steps to line up).
 template <int QS, int QH, bool SIGNED>
-__device__ __forceinline__ void wide_pair2_body(const WideSeed &a, const WideSeed &b,
-                                                float2 (&S)[QH])
+__device__ __forceinline__ void wide_pair2_carry(WideSeed &a, WideSeed &b, float2 (&S)[QH])
 {
     float2 sa = a.s, da = a.d, sb = b.s, db = b.d;
     const float2 la = splat2(a.l), lb = splat2(b.l);
@@ -275,6 +306,18 @@ __device__ __forceinline__ void wide_pair2_body(const WideSeed &a, const WideSee
         sa = __fadd2_rn(sa, da);
         sb = __fadd2_rn(sb, db);
     }
+    a.s = sa;
+    a.d = da;
+    b.s = sb;
+    b.d = db;
+}
+
+template <int QS, int QH, bool SIGNED>
+__device__ __forceinline__ void wide_pair2_body(const WideSeed &a, const WideSeed &b,
+                                                float2 (&S)[QH])
+{
+    WideSeed x = a, y = b;
+    wide_pair2_carry<QS, QH, SIGNED>(x, y, S);
 }
 
 template <int QS, int QH>

@@ -11,9 +11,10 @@
 //  * A CTA covers a slab of consecutive q values.  On a uniform q grid the
 //    per-pair values sin(q_k r)/r come from Reinsch's two-term recurrence
 //    (3 FP32 ops per pair*q with the accumulation), seeded per pair and slab
-//    from the range-reduced FP32 sin/cos of rsx_math.cuh; the wide kernels
-//    (forward_wide_kernel, delta_wide_kernel) run 64..128 q per seed following
-//    the slab plan of wide_plan(), with the even and odd q of a slab as two
+//    from the range-reduced FP32 sin/cos of rsx_math.cuh; the wide forward
+//    kernels run 64..192 q per seed following the slab plan of wide_plan(),
+//    and the delta kernel (delta_chain_kernel) runs a chain of two slabs of up
+//    to 112 q on one seed, with the even and odd q of a slab as two
 //    sequences of step 2 theta packed in float2 lanes, so that each FP32x2
 //    instruction advances both.  Non-uniform grids and water use
 //    forward_kernel / delta_kernel (8..32 q per slab, sin/cos per pair*q).
@@ -237,25 +238,57 @@ __global__ void __launch_bounds__(kBlockAtoms) delta_kernel(const DeltaArgs a)
     }
 }
 
-// Incremental delta on a uniform grid with wide slabs: as delta_kernel, but
-// QS up to 112 q per seed pair, FP32 per-tile sums reduce-scattered into FP64
-// lane accumulators (forward_wide_item's scheme).  The two chains of a pair
-// (new position, old position seeded with -1/r) run interleaved.
-template <int QS, bool SMALL>
-__global__ void __launch_bounds__(kBlockAtoms, QS <= 64 ? 3 : 2) delta_wide_kernel(const DeltaArgs a,
-                                                                                  int k_base)
+// sg (+1 or -1) rides in the sign bit of lam, which is -4 x^2 (sign bit set,
+// -0.0 included): a clear sign bit stands for sg = -1.
+__device__ __forceinline__ float pack_lam_sign(float l, float sg) { return sg > 0.f ? l : -l; }
+__device__ __forceinline__ void unpack_lam_sign(float x, float &l, float &sg)
 {
-    constexpr int QP = WideSlab<QS>::QP, NR = WideSlab<QS>::NR;
-    __shared__ float4 s_new[kBlockAtoms], s_old[kBlockAtoms];
-    __shared__ int s_idx[kBlockAtoms], s_slot[kBlockAtoms];
-    __shared__ float s_fx[QP];
-    __shared__ double s_red[kBlockAtoms / 32][QP];
+    sg = signbit(x) ? 1.f : -1.f;
+    l = -fabsf(x);
+}
+
+// Incremental delta on a uniform grid.  A CTA takes one static block and one
+// group of moved tiles over a chain of two slabs, [k0, k0 + Q1) and
+// [k0 + Q1, k0 + Q1 + Q2) (Q2 = 0: one slab), so each pair chain (new and
+// old position of the moved body) is seeded once per Q1 + Q2 q: its
+// recurrence state after the first slab (s, d of both chains, lam with the
+// sign) waits in shared memory while the first slab's sums are reduced, then
+// runs on through the second.  Per tile the warp sums the FP32 pair sums of
+// its threads through shared memory (warp_sum_rows), lane L receiving q index
+// 32c + L, applies the tile's factor f_x(q) to the sum and adds it to FP64
+// lane accumulators; the two chains of a pair (new position, old position
+// seeded with -1/r) run interleaved.  Tiles hold at most kDeltaTile moved
+// bodies of one type.  Dynamic shared memory: delta_chain_smem(Q2) bytes.
+__host__ __device__ constexpr size_t delta_chain_smem(int q2)
+{
+    return (q2 > 0 ? sizeof(float2) * kDeltaTile * 5 * kBlockAtoms : 0) +
+           sizeof(float) * (kBlockAtoms / 32) * 32 * kSumStride;
+}
+
+template <int Q1, int Q2, bool SMALL>
+__global__ void __launch_bounds__(kBlockAtoms, 3) delta_chain_kernel(const DeltaArgs a,
+                                                                    int k_base)
+{
+    static_assert(Q1 % 16 == 0 && Q2 % 16 == 0 && Q1 <= 112 && Q2 <= 112, "chain slabs");
+    constexpr int QP1 = WideSlab<Q1>::QP, NR1 = WideSlab<Q1>::NR;
+    constexpr int QP2 = Q2 > 0 ? WideSlab<Q2>::QP : 0, NR2 = QP2 / 32;
+    constexpr int T = kDeltaTile;
+    constexpr size_t kStateBytes = Q2 > 0 ? sizeof(float2) * T * 5 * kBlockAtoms : 0;
+    static_assert(sizeof(double) * (kBlockAtoms / 32) * (QP1 + QP2) <= delta_chain_smem(Q2),
+                  "final sums fit the dynamic buffer");
+    __shared__ float4 s_new[T], s_old[T];
+    __shared__ int s_idx[T], s_slot[kBlockAtoms];
+    __shared__ float s_fx[QP1 + QP2];
+    // dynamic: chain states between the slabs ([body][5][thread]) and the
+    // warps' summation buffers; after the tiles, the final cross-warp sums
+    extern __shared__ __align__(16) unsigned char dsm[];
+    float2 *u_st = reinterpret_cast<float2 *>(dsm);
+    double(*u_red)[QP1 + QP2] = reinterpret_cast<double(*)[QP1 + QP2]>(dsm);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    float *sum_buf = reinterpret_cast<float *>(dsm + kStateBytes) + warp * 32 * kSumStride;
     const BlockDesc by = a.blocks[blockIdx.x];
-    const int k0 = k_base + blockIdx.y * QS;
-    // moved tiles z, z + G, ... of this CTA (G = gridDim.z groups split the
-    // moved list, so a few static blocks still give enough CTAs)
+    const int k0 = k_base + blockIdx.y * (Q1 + Q2);
     const int group = blockIdx.z, n_groups = gridDim.z;
     const int y = by.start + tid;
     const bool valid = tid < by.len;
@@ -268,62 +301,116 @@ __global__ void __launch_bounds__(kBlockAtoms, QS <= 64 ? 3 : 2) delta_wide_kern
     const float q0 = a.q[k0];
     const float dq = a.dq;
 
-    double acc[NR];
+    double acc1[NR1], acc2[NR2 > 0 ? NR2 : 1];
 #pragma unroll
-    for (int c = 0; c < NR; ++c)
-        acc[c] = 0.0;
-    for (int mt = group; mt < a.n_mtiles; mt += n_groups) {
+    for (int c = 0; c < NR1; ++c)
+        acc1[c] = 0.0;
+#pragma unroll
+    for (int c = 0; c < NR2; ++c)
+        acc2[c] = 0.0;
+    for (int r = 0;; ++r) {
+        // snake order over the rounds keeps the groups' totals close (tiles
+        // come longest first)
+        const int mt = r * n_groups + ((r & 1) ? n_groups - 1 - group : group);
+        if (mt >= a.n_mtiles)
+            break;
         const BlockDesc tile = a.mtiles[mt];
+        const int len = min(tile.len, T);
         __syncthreads();
-        if (tid < tile.len) {
+        if (tid < len) {
             const int m = tile.start + tid;
             const int idx = a.moved_idx[m];
             s_new[tid] = a.moved_new[m];
             s_old[tid] = a.pos_old[idx];
             s_idx[tid] = idx;
         }
-        for (int k = tid; k < QP; k += kBlockAtoms)
-            s_fx[k] = (k < QS && k0 + k < a.n_q) ? a.ff[(size_t)(k0 + k) * a.n_types + tile.type]
-                                                 : 0.f;
-        __syncthreads();
-        float2 S[QP / 2];
-#pragma unroll
-        for (int m = 0; m < QP / 2; ++m)
-            S[m] = make_float2(0.f, 0.f);
-        for (int jj = 0; jj < tile.len; ++jj) {
-            const bool use = valid && s_idx[jj] != y;
-            float rn, rninv, ro, roinv, dx, dy, dz;
-            pair_r(py_new, s_new[jj], rn, rninv, dx, dy, dz);
-            pair_r(py_old, s_old[jj], ro, roinv, dx, dy, dz);
-            const WideSeed pn = wide_seed(q0, dq, rn, use ? mult * rninv : 0.f, SMALL);
-            const WideSeed po = wide_seed(q0, dq, ro, use ? -mult * roinv : 0.f, SMALL);
-            if constexpr (SMALL)
-                wide_pair2_body<QS, QP / 2, false>(pn, po, S);
-            else
-                wide_pair2<QS, QP / 2>(pn, po, S);
+        for (int k = tid; k < QP1 + QP2; k += kBlockAtoms) {
+            const bool first = k < QP1;
+            const int kl = first ? k : k - QP1;
+            const int kk = first ? k0 + kl : k0 + Q1 + kl;
+            const bool in = (first ? kl < Q1 : kl < Q2) && kk < a.n_q;
+            s_fx[k] = in ? a.ff[(size_t)kk * a.n_types + tile.type] : 0.f;
         }
+        __syncthreads();
+        {
+            float2 S[QP1 / 2];
 #pragma unroll
-        for (int c = 0; c < NR; ++c) {
-            float v[32];
+            for (int m = 0; m < QP1 / 2; ++m)
+                S[m] = make_float2(0.f, 0.f);
+            for (int jj = 0; jj < len; ++jj) {
+                const bool use = valid && s_idx[jj] != y;
+                float rn, rninv, ro, roinv, dx, dy, dz;
+                pair_r(py_new, s_new[jj], rn, rninv, dx, dy, dz);
+                pair_r(py_old, s_old[jj], ro, roinv, dx, dy, dz);
+                WideSeed pn = wide_seed(q0, dq, rn, use ? mult * rninv : 0.f, SMALL);
+                WideSeed po = wide_seed(q0, dq, ro, use ? -mult * roinv : 0.f, SMALL);
+                if (SMALL || !__any_sync(0xffffffffu, pn.sg < 0.f || po.sg < 0.f))
+                    wide_pair2_carry<Q1, QP1 / 2, false>(pn, po, S);
+                else
+                    wide_pair2_carry<Q1, QP1 / 2, true>(pn, po, S);
+                if constexpr (Q2 > 0) {
+                    float2 *st = &u_st[(size_t)jj * 5 * kBlockAtoms + tid];
+                    st[0] = pn.s;
+                    st[kBlockAtoms] = pn.d;
+                    st[2 * kBlockAtoms] = po.s;
+                    st[3 * kBlockAtoms] = po.d;
+                    st[4 * kBlockAtoms] =
+                        make_float2(pack_lam_sign(pn.l, pn.sg), pack_lam_sign(po.l, po.sg));
+                }
+            }
 #pragma unroll
-            for (int k = 0; k < 32; ++k)
-                v[k] = s_fx[32 * c + k] * pair_at(S, 32 * c + k);
-            warp_reduce_scatter<32>(v, lane);
-            acc[c] += (double)v[0];
+            for (int c = 0; c < NR1; ++c) {
+                const float v = warp_sum_rows([&](int k) { return pair_at(S, 32 * c + k); },
+                                              sum_buf, lane);
+                acc1[c] += (double)(s_fx[32 * c + lane] * v);
+            }
+        }
+        if constexpr (Q2 > 0) {
+            float2 S[QP2 / 2];
+#pragma unroll
+            for (int m = 0; m < QP2 / 2; ++m)
+                S[m] = make_float2(0.f, 0.f);
+            for (int jj = 0; jj < len; ++jj) {
+                const float2 *st = &u_st[(size_t)jj * 5 * kBlockAtoms + tid];
+                WideSeed pn, po;
+                pn.s = st[0];
+                pn.d = st[kBlockAtoms];
+                po.s = st[2 * kBlockAtoms];
+                po.d = st[3 * kBlockAtoms];
+                const float2 ls = st[4 * kBlockAtoms];
+                unpack_lam_sign(ls.x, pn.l, pn.sg);
+                unpack_lam_sign(ls.y, po.l, po.sg);
+                if (SMALL || !__any_sync(0xffffffffu, pn.sg < 0.f || po.sg < 0.f))
+                    wide_pair2_carry<Q2, QP2 / 2, false>(pn, po, S);
+                else
+                    wide_pair2_carry<Q2, QP2 / 2, true>(pn, po, S);
+            }
+#pragma unroll
+            for (int c = 0; c < NR2; ++c) {
+                const float v = warp_sum_rows([&](int k) { return pair_at(S, 32 * c + k); },
+                                              sum_buf, lane);
+                acc2[c] += (double)(s_fx[QP1 + 32 * c + lane] * v);
+            }
         }
     }
+    __syncthreads(); // states and summation buffers are no longer read: u_red takes their place
 #pragma unroll
-    for (int c = 0; c < NR; ++c)
-        s_red[warp][32 * c + lane] = acc[c];
+    for (int c = 0; c < NR1; ++c)
+        u_red[warp][32 * c + lane] = acc1[c];
+#pragma unroll
+    for (int c = 0; c < NR2; ++c)
+        u_red[warp][QP1 + 32 * c + lane] = acc2[c];
     __syncthreads();
-    for (int k = tid; k < QS; k += kBlockAtoms) {
-        const int kk = k0 + k;
-        if (kk >= a.n_q)
+    for (int k = tid; k < QP1 + QP2; k += kBlockAtoms) {
+        const bool first = k < QP1;
+        const int kl = first ? k : k - QP1;
+        const int kk = first ? k0 + kl : k0 + Q1 + kl;
+        if ((first ? kl >= Q1 : kl >= Q2) || kk >= a.n_q)
             continue;
         double s = 0.0;
 #pragma unroll
         for (int w = 0; w < kBlockAtoms / 32; ++w)
-            s += s_red[w][k];
+            s += u_red[w][k];
         a.partial[(size_t)kk * a.n_blocks * n_groups + (size_t)group * a.n_blocks + blockIdx.x] =
             s * (double)a.ff[(size_t)kk * a.n_types + by.type];
     }
@@ -586,15 +673,21 @@ static cudaError_t delta_qs(const DeltaArgs &a, bool uniform, cudaStream_t st)
 
 // SMALL (small_theta level 2: |theta| < pi/4 for every pair before and after
 // the move): the seeds skip the reduction of theta and the signed steps.
-template <int QS>
-static cudaError_t delta_wide_launch(const DeltaArgs &a, int k_base, int n_slabs,
-                                     cudaStream_t st)
+template <int Q1, int Q2>
+static cudaError_t delta_chain_launch(const DeltaArgs &a, int k_base, int n_chains,
+                                      cudaStream_t st)
 {
-    const dim3 grid(a.n_blocks, n_slabs, delta_groups(a));
-    if (a.small_theta >= 2)
-        delta_wide_kernel<QS, true><<<grid, kBlockAtoms, 0, st>>>(a, k_base);
-    else
-        delta_wide_kernel<QS, false><<<grid, kBlockAtoms, 0, st>>>(a, k_base);
+    const dim3 grid(a.n_blocks, n_chains, delta_groups(a));
+    constexpr size_t smem = delta_chain_smem(Q2);
+    auto kfn = a.small_theta >= 2 ? delta_chain_kernel<Q1, Q2, true>
+                                  : delta_chain_kernel<Q1, Q2, false>;
+    if (smem > 48 * 1024) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess)
+            return e;
+    }
+    kfn<<<grid, kBlockAtoms, smem, st>>>(a, k_base);
     count_launch();
     return cudaGetLastError();
 }
@@ -604,39 +697,40 @@ int delta_groups(const DeltaArgs &a)
     return std::max(1, std::min(std::min(kDeltaGroups, a.n_mtiles), a.max_groups));
 }
 
-static cudaError_t delta_wide_tail(const DeltaArgs &a, int k0, int width, cudaStream_t st)
+// One chain over the last `width` q (a multiple of 16, at most 224) from k0.
+static cudaError_t delta_chain_rest(const DeltaArgs &a, int k0, int width, cudaStream_t st)
 {
     switch (width / 16) {
-    case 1:
-        return delta_wide_launch<16>(a, k0, 1, st);
-    case 2:
-        return delta_wide_launch<32>(a, k0, 1, st);
-    case 3:
-        return delta_wide_launch<48>(a, k0, 1, st);
-    case 4:
-        return delta_wide_launch<64>(a, k0, 1, st);
-    case 5:
-        return delta_wide_launch<80>(a, k0, 1, st);
-    case 6:
-        return delta_wide_launch<96>(a, k0, 1, st);
-    case 7:
-        return delta_wide_launch<112>(a, k0, 1, st);
-    case 8:
-        return delta_wide_launch<128>(a, k0, 1, st);
-    default: // remainder slabs are at most 128 q wide
+    case 1: return delta_chain_launch<16, 0>(a, k0, 1, st);
+    case 2: return delta_chain_launch<32, 0>(a, k0, 1, st);
+    case 3: return delta_chain_launch<48, 0>(a, k0, 1, st);
+    case 4: return delta_chain_launch<64, 0>(a, k0, 1, st);
+    case 5: return delta_chain_launch<80, 0>(a, k0, 1, st);
+    case 6: return delta_chain_launch<96, 0>(a, k0, 1, st);
+    case 7: return delta_chain_launch<112, 0>(a, k0, 1, st);
+    case 8: return delta_chain_launch<112, 16>(a, k0, 1, st);
+    case 9: return delta_chain_launch<112, 32>(a, k0, 1, st);
+    case 10: return delta_chain_launch<112, 48>(a, k0, 1, st);
+    case 11: return delta_chain_launch<112, 64>(a, k0, 1, st);
+    case 12: return delta_chain_launch<112, 80>(a, k0, 1, st);
+    case 13: return delta_chain_launch<112, 96>(a, k0, 1, st);
+    case 14: return delta_chain_launch<112, 112>(a, k0, 1, st);
+    default:
         return cudaErrorInvalidValue;
     }
 }
 
-// Uniform grids and q_slab 64 / 128: the forward's wide slab plan up to
-// 128-q main slabs (fewer seeds per pair than 64-q slabs; 0.069 to 0.065 ms
-// per step with the small-theta seeds at k = 50 of 20,000 bodies, 201 q).
-// As in the forward, the remainder slab goes to the aux stream when there is
-// one, so that its CTAs fill the last wave of the main launch.
+// Uniform grids: chains of 224 q (two 112-q slabs, one seed per pair chain)
+// from q 0, then one chain over the rest rounded up to 16 q (n_q = 201: a
+// single 112 + 96 chain, one launch).  With full chains and a rest, the rest
+// goes to the aux stream when there is one, so that its CTAs fill the last
+// wave of the main launch.
 static cudaError_t launch_delta_wide(const DeltaArgs &a, cudaStream_t st, const AuxStream *aux)
 {
-    const WidePlan p = wide_plan(a.n_q, 128);
-    const bool split = aux && p.full > 0 && p.tail_len > 0;
+    constexpr int kSpan = 224;
+    const int full = a.n_q / kSpan, rest = a.n_q - full * kSpan;
+    const int rest_w = (rest + 15) / 16 * 16;
+    const bool split = aux && full > 0 && rest > 0;
     if (split) {
         cudaError_t e = cudaEventRecord(aux->fork, st);
         if (e == cudaSuccess)
@@ -644,18 +738,16 @@ static cudaError_t launch_delta_wide(const DeltaArgs &a, cudaStream_t st, const 
         if (e != cudaSuccess)
             return e;
     }
-    if (p.full > 0) {
-        cudaError_t e = p.main == 64    ? delta_wide_launch<64>(a, 0, p.full, st)
-                        : p.main == 112 ? delta_wide_launch<112>(a, 0, p.full, st)
-                                        : delta_wide_launch<128>(a, 0, p.full, st);
+    if (full > 0) {
+        const cudaError_t e = delta_chain_launch<112, 112>(a, 0, full, st);
         if (e != cudaSuccess)
             return e;
     }
-    if (p.tail_len == 0)
+    if (rest == 0)
         return cudaSuccess;
     if (!split)
-        return delta_wide_tail(a, p.tail_k0, p.tail_w, st);
-    cudaError_t e = delta_wide_tail(a, p.tail_k0, p.tail_w, aux->stream);
+        return delta_chain_rest(a, full * kSpan, rest_w, st);
+    cudaError_t e = delta_chain_rest(a, full * kSpan, rest_w, aux->stream);
     // joined even after a failed launch, so that `st` never runs ahead of
     // work queued on the aux stream
     const cudaError_t ej = cudaEventRecord(aux->join, aux->stream);

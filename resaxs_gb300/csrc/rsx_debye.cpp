@@ -655,12 +655,15 @@ rsx_status delta_update(rsx_debye *h, const rsx_body *moved, const unsigned *idx
         for (unsigned m = 0; m < k; ++m)
             order[fill[type_of(moved[m])]++] = (int)m;
     }
-    // Each type's run is cut into near-equal tiles of at most max(8, k / G)
-    // bodies (G = kDeltaGroups moved-list groups of the wide kernel), longest
-    // first, so that the groups get similar shares of a small moved list.
+    // Each type's run is cut into near-equal tiles, longest first: at most
+    // kDeltaTile bodies for the wide kernel (its chain states between the two
+    // slabs are kept per tile body), else at most max(8, k / G) (G =
+    // kDeltaGroups), so that the groups get similar shares of a small list.
     std::vector<BlockDesc> tiles;
-    const int cap = std::min(kBlockAtoms,
-                             std::max(8, (int)((k + kDeltaGroups - 1) / kDeltaGroups)));
+    const bool wide = h->uniform && slab_for(h) >= 64;
+    const int cap = wide ? kDeltaTile
+                         : std::min(kBlockAtoms,
+                                    std::max(8, (int)((k + kDeltaGroups - 1) / kDeltaGroups)));
     for (int t = 0; t < h->n_types; ++t) {
         const int c = cnt[t + 1] - cnt[t];
         if (c == 0)

@@ -107,6 +107,7 @@ struct DeltaArgs {
 };
 
 constexpr int kDeltaGroups = 8; // moved-list groups of the wide delta kernel
+constexpr int kDeltaTile = 8;   // moved bodies per tile of the wide delta kernel
 
 // launchers (debye_kernels.cu, adjoint_kernels.cu); all asynchronous on `st`
 // Slab plan of the wide uniform forward: `full` slabs of `main` q from q 0,
