@@ -681,7 +681,7 @@ static cudaError_t delta_chain_launch(const DeltaArgs &a, int k_base, int n_chai
     constexpr size_t smem = delta_chain_smem(Q2);
     auto kfn = a.small_theta >= 2 ? delta_chain_kernel<Q1, Q2, true>
                                   : delta_chain_kernel<Q1, Q2, false>;
-    if (smem > 48 * 1024) {
+    if (smem > 32 * 1024) { // with the static arrays past the 48 KB default
         const cudaError_t e =
             cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess)

@@ -299,9 +299,9 @@ rsx_status update_layout(rsx_debye *h, const rsx_body *bodies, bool same)
     RSX_TRY(ensure(&h->d_blocks, h->blocks_cap, h->L.blocks.size(), "blocks"));
     RSX_TRY(ensure(&h->d_items, h->items_cap, h->L.items.size(), "items"));
     RSX_TRY(ensure(&h->d_adj_items, h->adj_cap, h->L.adj_items.size(), "adjoint items"));
+    // (an incremental step grows it to its own need in delta_update)
     const size_t need = h->L.items.size() * (size_t)h->n_q;
-    const size_t need_delta = h->L.blocks.size() * (size_t)kDeltaGroups * h->n_q;
-    RSX_TRY(ensure(&h->d_partial, h->partial_cap, std::max(need, need_delta), "partial sums"));
+    RSX_TRY(ensure(&h->d_partial, h->partial_cap, need, "partial sums"));
     RSX_TRY_CUDA(cudaMemcpyAsync(h->d_blocks, h->L.blocks.data(),
                                  sizeof(BlockDesc) * h->L.blocks.size(), cudaMemcpyHostToDevice,
                                  h->st),
@@ -657,13 +657,11 @@ rsx_status delta_update(rsx_debye *h, const rsx_body *moved, const unsigned *idx
     }
     // Each type's run is cut into near-equal tiles, longest first: at most
     // kDeltaTile bodies for the wide kernel (its chain states between the two
-    // slabs are kept per tile body), else at most max(8, k / G) (G =
-    // kDeltaGroups), so that the groups get similar shares of a small list.
+    // slabs are kept per tile body; the tiles are split over up to
+    // kDeltaGroups CTA groups), else at most max(8, k / 8).
     std::vector<BlockDesc> tiles;
     const bool wide = h->uniform && slab_for(h) >= 64;
-    const int cap = wide ? kDeltaTile
-                         : std::min(kBlockAtoms,
-                                    std::max(8, (int)((k + kDeltaGroups - 1) / kDeltaGroups)));
+    const int cap = wide ? kDeltaTile : std::min(kBlockAtoms, std::max(8, (int)((k + 7) / 8)));
     for (int t = 0; t < h->n_types; ++t) {
         const int c = cnt[t + 1] - cnt[t];
         if (c == 0)
@@ -711,7 +709,6 @@ rsx_status delta_update(rsx_debye *h, const rsx_body *moved, const unsigned *idx
     a.mtiles = reinterpret_cast<const BlockDesc *>(h->d_moved + off_tiles);
     a.ff = h->d_ff;
     a.q = h->d_q;
-    a.partial = h->d_partial;
     a.n = h->n;
     a.k = (int)k;
     a.n_q = h->n_q;
@@ -720,6 +717,10 @@ rsx_status delta_update(rsx_debye *h, const rsx_body *moved, const unsigned *idx
     a.n_mtiles = (int)tiles.size();
     a.max_groups = kDeltaGroups;
     a.dq = h->dq;
+    // one partial row per static block and moved-list group
+    RSX_TRY(ensure(&h->d_partial, h->partial_cap,
+                   (size_t)delta_parts(a, slab_for(h), h->uniform) * h->n_q, "partial sums"));
+    a.partial = h->d_partial;
     // the extent already holds the moved bodies' new positions (recalc_common
     // grows it first), so the level covers the pairs before and after the move
     a.small_theta = small_theta(h);

@@ -106,7 +106,7 @@ struct DeltaArgs {
     int small_theta;         // theta_level() of the bodies before and after the move
 };
 
-constexpr int kDeltaGroups = 8; // moved-list groups of the wide delta kernel
+constexpr int kDeltaGroups = 16; // moved-list groups of the wide delta kernel (at most)
 constexpr int kDeltaTile = 8;   // moved bodies per tile of the wide delta kernel
 
 // launchers (debye_kernels.cu, adjoint_kernels.cu); all asynchronous on `st`
