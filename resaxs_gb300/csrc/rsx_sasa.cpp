@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <numeric>
 #include <vector>
 
@@ -208,32 +209,54 @@ rsx_status run(rsx_sasa *h, const rsx_body *atoms, const float *radii)
     const int n = h->n;
     // the staging buffer may still feed the previous call's copy
     RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "sasa staging");
-    float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0}, amax = 0.f, rmax = 0.f, dmax = 0.f;
-    std::vector<char> present(h->typed ? h->n_types : 0, 0);
+    // One branch-free pass: checks, bounding box and the largest coordinate
+    // (a NaN fails every comparison, so it never enters the box and clears
+    // `ok`); a second pass names the first bad atom only when there is one.
+    const float big = std::numeric_limits<float>::max();
+    auto mx = [](float a, float b) { return a > b ? a : b; };
+    auto mn = [](float a, float b) { return a < b ? a : b; };
+    float lo[3] = {big, big, big}, hi[3] = {-big, -big, -big}, amax = 0.f, rmax = 0.f, dmax = 0.f;
+    std::vector<char> present(h->typed ? h->n_types : 1, 0);
+    const unsigned nt = h->typed ? (unsigned)h->n_types : 1u;
+    unsigned ok = 1;
     for (int i = 0; i < n; ++i) {
-        const float p[3] = {atoms[i].x, atoms[i].y, atoms[i].z};
-        if (!std::isfinite(p[0]) || !std::isfinite(p[1]) || !std::isfinite(p[2]))
-            return fail(RSX_INVALID_ARG, "atom " + std::to_string(i) + " has a non-finite position");
+        const float x = atoms[i].x, y = atoms[i].y, z = atoms[i].z;
+        const float ax = std::fabs(x), ay = std::fabs(y), az = std::fabs(z);
+        ok &= (ax <= big) & (ay <= big) & (az <= big);
         if (h->typed) {
             unsigned t;
             std::memcpy(&t, &atoms[i].w, 4);
-            if (t >= (unsigned)h->n_types)
+            ok &= t < nt;
+            present[t < nt ? t : 0] = 1;
+        } else {
+            const float r = radii[i];
+            ok &= (r >= 0.f) & (r <= big);
+            rmax = mx(rmax, r);
+        }
+        amax = mx(amax, mx(ax, mx(ay, az)));
+        lo[0] = mn(lo[0], x);
+        hi[0] = mx(hi[0], x);
+        lo[1] = mn(lo[1], y);
+        hi[1] = mx(hi[1], y);
+        lo[2] = mn(lo[2], z);
+        hi[2] = mx(hi[2], z);
+    }
+    if (!ok) {
+        for (int i = 0; i < n; ++i) {
+            if (!std::isfinite(atoms[i].x) || !std::isfinite(atoms[i].y) ||
+                !std::isfinite(atoms[i].z))
+                return fail(RSX_INVALID_ARG, "atom " + std::to_string(i) + " has a non-finite position");
+            unsigned t;
+            std::memcpy(&t, &atoms[i].w, 4);
+            if (h->typed && t >= nt)
                 return fail(RSX_INVALID_ARG, "atom " + std::to_string(i) + " has type " +
                                                  std::to_string(t) + " outside the dot map");
-            present[t] = 1;
-        } else {
-            if (!(radii[i] >= 0.f) || !std::isfinite(radii[i]))
+            if (!h->typed && (!(radii[i] >= 0.f) || !std::isfinite(radii[i])))
                 return fail(RSX_INVALID_ARG, "atom " + std::to_string(i) + " has an invalid radius");
-            rmax = std::max(rmax, radii[i]);
-        }
-        for (int c = 0; c < 3; ++c) {
-            if (i == 0 || p[c] < lo[c])
-                lo[c] = p[c];
-            if (i == 0 || p[c] > hi[c])
-                hi[c] = p[c];
-            amax = std::max(amax, std::fabs(p[c]));
         }
     }
+    if (n == 0)
+        lo[0] = lo[1] = lo[2] = hi[0] = hi[1] = hi[2] = 0.f;
     if (h->typed) {
         for (int t = 0; t < h->n_types; ++t)
             if (present[t]) {
