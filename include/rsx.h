@@ -126,11 +126,10 @@ rsx_status rsx_calc_saxs_curve_status(const float *v_q, int n_q, const rsx_body 
  * (larger ones are rejected with RSX_INVALID_ARG before any launch).
  * The first call on a device looks up that array's device address (with the
  * device current), and so does the first call after the device's context was
- * recreated (cudaDeviceReset); make such a first call before any stream
- * capture.  Every call reuses the array and leaves its contents behind; calls
- * on the same device that overlap on the GPU (several streams or threads)
- * race on it and must be serialised by the caller (each device has its own
- * array).  Returns after the stream finished the call (the error word of the
+ * recreated (cudaDeviceReset).  Every call reuses the array and leaves its
+ * contents behind; calls on the same device that overlap on the GPU (several
+ * streams or threads) race on it and must be serialised by the caller (each
+ * device has its own array).  Returns after the stream finished the call (the error word of the
  * array is read back with a synchronisation of `stream`). */
 rsx_status rsx_calc_saxs_curve_device_noalloc(const float *d_q, int n_q, const rsx_body *d_bodies,
                                               int n_bodies, const float *d_factors, int n_factors,
@@ -323,8 +322,11 @@ rsx_status rsx_sasa_sphere_dots(int kind, float radius, float dot_density, float
                                 float *out_xyzw, int cap, int *n_out);
 
 /* rsasa_cl_gpu::initialize(dot_spheres_cl_params) (rsasa_cl_gpu_alg.cpp:38-57):
- * atom count, unit dot set (n_dots <= 4096, finite) and probe radius fixed
- * per handle.  Dot k of atom i sits at p_i + unit_k * (r_i + P). */
+ * atom count (at most 2^28), unit dot set (n_dots <= 4096, finite) and probe
+ * radius fixed per handle.  Dot k of atom i sits at p_i + unit_k * (r_i + P).
+ * A call checks the atoms (finite positions; radii >= 0 and finite, or types
+ * inside the dot map) on the GPU with the bounding box and reports the first
+ * bad atom with RSX_INVALID_ARG. */
 rsx_status rsx_sasa_create(int n_atoms, const float *unit_dots, int n_dots, float probe,
                            int device, rsx_sasa **out);
 /* The reference's own dot layout: rsasa_cl_gpu::create_sphere_dots

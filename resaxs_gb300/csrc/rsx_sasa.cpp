@@ -40,8 +40,9 @@ struct rsx_sasa {
     float4 *d_atoms = nullptr;
     int *d_cell_of = nullptr, *d_rank_of = nullptr, *d_orig = nullptr, *d_type_of = nullptr;
     int *d_cell_sorted = nullptr;
-    int *d_cell_count = nullptr, *d_cell_start = nullptr;
-    size_t cells_cap = 0;
+    int *d_cell_count = nullptr, *d_cell_start = nullptr; // [4 n + 4097] each
+    int cells_cap = 0;
+    SasaGeom *d_geom = nullptr, *h_geom = nullptr;
     unsigned *d_counts = nullptr, *h_counts = nullptr;
     unsigned long long *d_tests = nullptr, *h_tests = nullptr;
     float last_ms = 0.f;
@@ -61,10 +62,11 @@ rsx_status sasa_release(rsx_sasa *h)
                     (void *)h->d_dot_reach, (void *)h->d_type_radius, (void *)h->d_in,
                     (void *)h->d_atoms, (void *)h->d_cell_of, (void *)h->d_rank_of,
                     (void *)h->d_orig, (void *)h->d_type_of, (void *)h->d_cell_sorted,
-                    (void *)h->d_cell_count,
-                    (void *)h->d_cell_start, (void *)h->d_counts, (void *)h->d_tests})
+                    (void *)h->d_cell_count, (void *)h->d_cell_start, (void *)h->d_counts,
+                    (void *)h->d_tests, (void *)h->d_geom})
         dev_free(p);
     host_free_pinned(h->h_in);
+    host_free_pinned(h->h_geom);
     host_free_pinned(h->h_counts);
     host_free_pinned(h->h_tests);
     if (h->e0)
@@ -194,6 +196,16 @@ rsx_status new_handle(int n_atoms, float probe, int device, rsx_sasa **out)
         s = host_alloc_pinned((void **)&h->h_counts, sizeof(unsigned) * n1, "pinned counts");
     if (s == RSX_OK)
         s = host_alloc_pinned((void **)&h->h_tests, sizeof(unsigned long long), "pinned tests");
+    // the cell grid has at most 4 n + 4096 cells (sasa_plan_kernel)
+    h->cells_cap = 4 * (int)n1 + 4097;
+    if (s == RSX_OK)
+        s = dev_alloc((void **)&h->d_cell_count, sizeof(int) * (size_t)h->cells_cap, "sasa cells");
+    if (s == RSX_OK)
+        s = dev_alloc((void **)&h->d_cell_start, sizeof(int) * (size_t)h->cells_cap, "sasa cells");
+    if (s == RSX_OK)
+        s = dev_alloc((void **)&h->d_geom, sizeof(SasaGeom), "sasa geometry");
+    if (s == RSX_OK)
+        s = host_alloc_pinned((void **)&h->h_geom, sizeof(SasaGeom), "pinned sasa geometry");
     if (s != RSX_OK) {
         sasa_release(h);
         return s;
@@ -209,95 +221,15 @@ rsx_status run(rsx_sasa *h, const rsx_body *atoms, const float *radii)
     const int n = h->n;
     // the staging buffer may still feed the previous call's copy
     RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "sasa staging");
-    // One branch-free pass: checks, bounding box and the largest coordinate
-    // (a NaN fails every comparison, so it never enters the box and clears
-    // `ok`); a second pass names the first bad atom only when there is one.
-    const float big = std::numeric_limits<float>::max();
-    auto mx = [](float a, float b) { return a > b ? a : b; };
-    auto mn = [](float a, float b) { return a < b ? a : b; };
-    float lo[3] = {big, big, big}, hi[3] = {-big, -big, -big}, amax = 0.f, rmax = 0.f, dmax = 0.f;
-    std::vector<char> present(h->typed ? h->n_types : 1, 0);
-    const unsigned nt = h->typed ? (unsigned)h->n_types : 1u;
-    unsigned ok = 1;
-    for (int i = 0; i < n; ++i) {
-        const float x = atoms[i].x, y = atoms[i].y, z = atoms[i].z;
-        const float ax = std::fabs(x), ay = std::fabs(y), az = std::fabs(z);
-        ok &= (ax <= big) & (ay <= big) & (az <= big);
-        if (h->typed) {
-            unsigned t;
-            std::memcpy(&t, &atoms[i].w, 4);
-            ok &= t < nt;
-            present[t < nt ? t : 0] = 1;
-        } else {
-            const float r = radii[i];
-            ok &= (r >= 0.f) & (r <= big);
-            rmax = mx(rmax, r);
-        }
-        amax = mx(amax, mx(ax, mx(ay, az)));
-        lo[0] = mn(lo[0], x);
-        hi[0] = mx(hi[0], x);
-        lo[1] = mn(lo[1], y);
-        hi[1] = mx(hi[1], y);
-        lo[2] = mn(lo[2], z);
-        hi[2] = mx(hi[2], z);
-    }
-    if (!ok) {
-        for (int i = 0; i < n; ++i) {
-            if (!std::isfinite(atoms[i].x) || !std::isfinite(atoms[i].y) ||
-                !std::isfinite(atoms[i].z))
-                return fail(RSX_INVALID_ARG, "atom " + std::to_string(i) + " has a non-finite position");
-            unsigned t;
-            std::memcpy(&t, &atoms[i].w, 4);
-            if (h->typed && t >= nt)
-                return fail(RSX_INVALID_ARG, "atom " + std::to_string(i) + " has type " +
-                                                 std::to_string(t) + " outside the dot map");
-            if (!h->typed && (!(radii[i] >= 0.f) || !std::isfinite(radii[i])))
-                return fail(RSX_INVALID_ARG, "atom " + std::to_string(i) + " has an invalid radius");
-        }
-    }
-    if (n == 0)
-        lo[0] = lo[1] = lo[2] = hi[0] = hi[1] = hi[2] = 0.f;
-    if (h->typed) {
-        for (int t = 0; t < h->n_types; ++t)
-            if (present[t]) {
-                rmax = std::max(rmax, h->type_radius[t]);
-                dmax = std::max(dmax, h->dot_reach[t]);
-            }
-    } else {
-        dmax = (rmax + h->probe) * h->unit_reach;
-    }
-    // an occluder of a dot of atom i lies within |d| + P + r_b of it; the
-    // kernel's reach adds `margin` for the rounding of the dot's position
-    const float margin = 0.01f + 8e-6f * amax;
-    double cell = ((double)dmax * 1.000001 + h->probe + rmax + margin) * 1.001 + 1e-3;
-    int dims[3];
-    for (;;) {
-        double total = 1.0;
-        for (int c = 0; c < 3; ++c) {
-            dims[c] = (int)std::floor(((double)hi[c] - lo[c]) / cell) + 1;
-            total *= dims[c];
-        }
-        if (total <= 4.0 * n + 4096.0)
-            break;
-        cell *= 1.5; // sparse, wide boxes: fewer, larger cells (still exact)
-    }
-    const size_t n_cells = (size_t)dims[0] * dims[1] * dims[2];
-    if (n_cells + 1 > h->cells_cap) {
-        dev_free(h->d_cell_count);
-        dev_free(h->d_cell_start);
-        h->d_cell_count = h->d_cell_start = nullptr;
-        h->cells_cap = 0;
-        const size_t cap = n_cells + n_cells / 4 + 1024;
-        RSX_TRY(dev_alloc((void **)&h->d_cell_count, sizeof(int) * cap, "sasa cells"));
-        RSX_TRY(dev_alloc((void **)&h->d_cell_start, sizeof(int) * cap, "sasa cells"));
-        h->cells_cap = cap;
-    }
     std::memcpy(h->h_in, atoms, sizeof(float4) * (size_t)n);
     size_t bytes = sizeof(float4) * (size_t)n;
     if (!h->typed) {
         std::memcpy(h->h_in + bytes, radii, sizeof(float) * (size_t)n);
         bytes += sizeof(float) * (size_t)n;
     }
+    // The checks, the bounding box and the cell grid are formed on the GPU
+    // (sasa_geom_kernel, sasa_plan_kernel); the host reads the verdict with
+    // the counts and names the first bad atom only when there is one.
     SasaCellArgs c{};
     c.atoms_in = reinterpret_cast<const float4 *>(h->d_in);
     c.radii_in = h->typed ? nullptr : reinterpret_cast<const float *>(h->d_in + sizeof(float4) * n);
@@ -310,8 +242,13 @@ rsx_status run(rsx_sasa *h, const rsx_body *atoms, const float *radii)
     c.orig_index = h->d_orig;
     c.type_of = h->d_type_of;
     c.cell_sorted = h->d_cell_sorted;
+    c.geom = h->d_geom;
+    c.dot_reach = h->d_dot_reach;
+    c.unit_reach = h->unit_reach;
+    c.probe = h->probe;
     c.n_atoms = n;
-    c.n_cells = (int)n_cells;
+    c.n_types = h->typed ? h->n_types : 1;
+    c.cells_cap = h->cells_cap;
     SasaArgs a{};
     a.atoms = h->d_atoms;
     a.orig_index = h->d_orig;
@@ -326,14 +263,9 @@ rsx_status run(rsx_sasa *h, const rsx_body *atoms, const float *radii)
     a.typed = h->typed ? 1 : 0;
     a.counts = h->d_counts;
     a.tests = h->d_tests;
+    a.geom = h->d_geom;
     a.n_atoms = n;
     a.probe = h->probe;
-    a.margin = margin;
-    for (int k = 0; k < 3; ++k) {
-        c.dims[k] = a.dims[k] = dims[k];
-        c.lo[k] = a.lo[k] = lo[k];
-    }
-    c.inv_cell = a.inv_cell = 1.0 / cell;
     RSX_TRY_CUDA(cudaMemcpyAsync(h->d_in, h->h_in, bytes, cudaMemcpyHostToDevice, h->st),
                  "upload atoms");
     RSX_TRY_CUDA(cudaMemsetAsync(h->d_tests, 0, sizeof(unsigned long long), h->st), "zero tests");
@@ -347,7 +279,25 @@ rsx_status run(rsx_sasa *h, const rsx_body *atoms, const float *radii)
     RSX_TRY_CUDA(cudaMemcpyAsync(h->h_tests, h->d_tests, sizeof(unsigned long long),
                                  cudaMemcpyDeviceToHost, h->st),
                  "read tests");
+    RSX_TRY_CUDA(cudaMemcpyAsync(h->h_geom, h->d_geom, sizeof(SasaGeom), cudaMemcpyDeviceToHost,
+                                 h->st),
+                 "read sasa geometry");
     RSX_TRY_CUDA(cudaStreamSynchronize(h->st), "sasa");
+    if (h->h_geom->bad) {
+        for (int i = 0; i < n; ++i) {
+            if (!std::isfinite(atoms[i].x) || !std::isfinite(atoms[i].y) ||
+                !std::isfinite(atoms[i].z))
+                return fail(RSX_INVALID_ARG, "atom " + std::to_string(i) + " has a non-finite position");
+            unsigned t;
+            std::memcpy(&t, &atoms[i].w, 4);
+            if (h->typed && t >= (unsigned)h->n_types)
+                return fail(RSX_INVALID_ARG, "atom " + std::to_string(i) + " has type " +
+                                                 std::to_string(t) + " outside the dot map");
+            if (!h->typed && (!(radii[i] >= 0.f) || !std::isfinite(radii[i])))
+                return fail(RSX_INVALID_ARG, "atom " + std::to_string(i) + " has an invalid radius");
+        }
+        return fail(RSX_INVALID_ARG, "invalid atoms");
+    }
     cudaEventElapsedTime(&h->last_ms, h->e0, h->e1);
     h->last_tests = *h->h_tests;
     return RSX_OK;
@@ -505,9 +455,10 @@ rsx_status rsx_sasa_create(int n_atoms, const float *unit_dots, int n_dots, floa
     if (!out)
         return fail(RSX_INVALID_ARG, "out handle pointer is null");
     *out = nullptr;
-    if (n_atoms < 0 || !unit_dots || n_dots <= 0 || n_dots > 32 * kSasaMaxGroups ||
-        !(probe >= 0.f) || !std::isfinite(probe))
-        return fail(RSX_INVALID_ARG, "need n_atoms >= 0, 1..4096 unit dots and probe >= 0");
+    if (n_atoms < 0 || n_atoms > kSasaMaxAtoms || !unit_dots || n_dots <= 0 ||
+        n_dots > 32 * kSasaMaxGroups || !(probe >= 0.f) || !std::isfinite(probe))
+        return fail(RSX_INVALID_ARG,
+                    "need 0 <= n_atoms <= 2^28, 1..4096 unit dots and probe >= 0");
     std::vector<float4> set((size_t)n_dots);
     for (int k = 0; k < n_dots; ++k) {
         set[k] = make_float4(unit_dots[3 * k], unit_dots[3 * k + 1], unit_dots[3 * k + 2], 0.f);
@@ -540,10 +491,11 @@ rsx_status rsx_sasa_create_typed(int n_atoms, const float *dot_map, int n_types,
     if (!out)
         return fail(RSX_INVALID_ARG, "out handle pointer is null");
     *out = nullptr;
-    if (n_atoms < 0 || !dot_map || !type_radii || n_types <= 0 || n_types > kSasaMaxTypes ||
-        stride <= 0 || stride > 32 * kSasaMaxGroups || !(probe >= 0.f) || !std::isfinite(probe))
-        return fail(RSX_INVALID_ARG,
-                    "need n_atoms >= 0, 1..256 types, 1..4096 dots per type and probe >= 0");
+    if (n_atoms < 0 || n_atoms > kSasaMaxAtoms || !dot_map || !type_radii || n_types <= 0 ||
+        n_types > kSasaMaxTypes || stride <= 0 || stride > 32 * kSasaMaxGroups ||
+        !(probe >= 0.f) || !std::isfinite(probe))
+        return fail(RSX_INVALID_ARG, "need 0 <= n_atoms <= 2^28, 1..256 types, 1..4096 dots per "
+                                     "type and probe >= 0");
     for (int t = 0; t < n_types; ++t)
         if (!(type_radii[t] >= 0.f) || !std::isfinite(type_radii[t]))
             return fail(RSX_INVALID_ARG, "type " + std::to_string(t) + " has an invalid radius");

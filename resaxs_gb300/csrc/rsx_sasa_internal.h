@@ -7,6 +7,25 @@ namespace rsx {
 // Upper bounds of the kernels' tables.
 constexpr int kSasaMaxGroups = 128;   // 32-dot groups per atom: <= 4096 dots
 constexpr int kSasaMaxTypes = 256;    // dot tables of the typed (per-type) form
+constexpr int kSasaMaxAtoms = 1 << 28; // the cell arrays hold 4 n + 4097 ints
+
+// Geometry of one call, formed on the GPU from the atoms (sasa_geom_kernel,
+// sasa_plan_kernel; zero on entry) and read by the cell-list and occlusion
+// kernels, which do nothing when `bad` is set.
+struct SasaGeom {
+    unsigned lo_key[3];  // complemented ordered keys of the box minima
+    unsigned hi_key[3];  // ordered keys of the box maxima
+    unsigned amax_key;   // bits of the largest |coordinate|
+    unsigned rmax_key;   // bits of the largest radius (unit form)
+    unsigned present[kSasaMaxTypes / 32]; // types present (typed form)
+    unsigned bad;        // a non-finite position, a bad radius or type
+    // the cell grid (sasa_plan_kernel)
+    int dims[3];
+    int n_cells;
+    float lo[3];
+    float margin;
+    double inv_cell;
+};
 
 // Cell list built on the GPU from the atoms in caller order.
 struct SasaCellArgs {
@@ -21,10 +40,11 @@ struct SasaCellArgs {
     int *orig_index;          // [n_atoms] caller index of each cell-ordered atom
     int *type_of;             // [n_atoms] type of each cell-ordered atom (typed form)
     int *cell_sorted;         // [n_atoms] cell of each cell-ordered atom
-    int n_atoms, n_cells;
-    int dims[3];
-    float lo[3];
-    double inv_cell;
+    SasaGeom *geom;
+    const float *dot_reach;   // [n_types] largest |d| of each type's table (typed form)
+    float unit_reach, probe;  // unit form: reach of a dot is (r + P) * unit_reach
+    int n_atoms, n_types;
+    int cells_cap;            // cell_count / cell_start hold cells_cap entries (>= 4 n + 4097)
 };
 
 // Occlusion pass over the cell-ordered atoms: one warp per atom.
@@ -46,13 +66,13 @@ struct SasaArgs {
     int typed;
     unsigned *counts;         // [n_atoms] accessible dots, caller order
     unsigned long long *tests; // optional: occlusion tests to the first occluder
+    const SasaGeom *geom;     // cell grid and rounding margin of the call
     int n_atoms;
-    int dims[3];
-    float lo[3];
-    double inv_cell;
-    float probe, margin;
+    float probe;
 };
 
+// Geometry (checks, bounding box, cell grid) and the cell list; c.geom,
+// c.cell_count are cleared here first.
 cudaError_t launch_sasa_cells(const SasaCellArgs &c, cudaStream_t st);
 cudaError_t launch_sasa(const SasaArgs &a, cudaStream_t st);
 

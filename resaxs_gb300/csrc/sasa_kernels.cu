@@ -60,27 +60,168 @@ __device__ __forceinline__ void cell_coords(float x, float y, float z, const flo
     }
 }
 
+// ---- geometry of the call ---------------------------------------------------
+
+// Ordered keys of floats: key(a) < key(b) iff a < b (for non-NaN values), so
+// atomicMax / atomicMin on the keys reduce floats.
+__device__ __forceinline__ unsigned float_key(float f)
+{
+    const unsigned b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float key_float(unsigned k)
+{
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+// Checks of every atom (finite position; radius >= 0 and finite, or type
+// below n_types) and the reductions the grid needs: bounding box, largest
+// |coordinate|, largest radius (unit form) and the types present (typed
+// form).  geom is zero on entry; box minima are kept as complemented keys.
+__global__ void __launch_bounds__(256) sasa_geom_kernel(const SasaCellArgs c)
+{
+    __shared__ unsigned s_present[kSasaMaxTypes / 32];
+    const int tid = threadIdx.x, lane = tid & 31;
+    if (tid < kSasaMaxTypes / 32)
+        s_present[tid] = 0u;
+    __syncthreads();
+    unsigned lo_k[3] = {0u, 0u, 0u}, hi_k[3] = {0u, 0u, 0u}, amax_k = 0u, rmax_k = 0u, bad = 0u;
+    for (int i = blockIdx.x * blockDim.x + tid; i < c.n_atoms; i += gridDim.x * blockDim.x) {
+        const float4 p = c.atoms_in[i];
+        const float v[3] = {p.x, p.y, p.z};
+        float am = 0.f;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float av = fabsf(v[a]);
+            if (!(av <= 3.402823466e38f)) {
+                bad = 1u;
+                continue;
+            }
+            lo_k[a] = max(lo_k[a], ~float_key(v[a]));
+            hi_k[a] = max(hi_k[a], float_key(v[a]));
+            am = fmaxf(am, av);
+        }
+        amax_k = max(amax_k, __float_as_uint(am));
+        if (c.radii_in) {
+            const float r = c.radii_in[i];
+            if (!(r >= 0.f && r <= 3.402823466e38f))
+                bad = 1u;
+            else
+                rmax_k = max(rmax_k, __float_as_uint(r));
+        } else {
+            const unsigned t = __float_as_uint(p.w);
+            if (t >= (unsigned)c.n_types)
+                bad = 1u;
+            else
+                atomicOr(&s_present[t >> 5], 1u << (t & 31));
+        }
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            lo_k[a] = max(lo_k[a], __shfl_xor_sync(kFull, lo_k[a], o));
+            hi_k[a] = max(hi_k[a], __shfl_xor_sync(kFull, hi_k[a], o));
+        }
+        amax_k = max(amax_k, __shfl_xor_sync(kFull, amax_k, o));
+        rmax_k = max(rmax_k, __shfl_xor_sync(kFull, rmax_k, o));
+        bad |= __shfl_xor_sync(kFull, bad, o);
+    }
+    SasaGeom *g = c.geom;
+    if (lane == 0) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            atomicMax(&g->lo_key[a], lo_k[a]);
+            atomicMax(&g->hi_key[a], hi_k[a]);
+        }
+        atomicMax(&g->amax_key, amax_k);
+        atomicMax(&g->rmax_key, rmax_k);
+        if (bad)
+            atomicOr(&g->bad, 1u);
+    }
+    __syncthreads();
+    if (tid < kSasaMaxTypes / 32 && s_present[tid])
+        atomicOr(&g->present[tid], s_present[tid]);
+}
+
+// The cell grid from the reductions (one thread): a cell is at least as wide
+// as the largest reach |d| + P + r_b (plus a margin for the rounding of the
+// dot position), widened by 1.5 until the grid has at most 4 n + 4096 cells.
+__global__ void sasa_plan_kernel(const SasaCellArgs c)
+{
+    if (threadIdx.x != 0)
+        return;
+    SasaGeom *g = c.geom;
+    if (g->bad)
+        return;
+    float lo[3], hi[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = key_float(~g->lo_key[a]);
+        hi[a] = key_float(g->hi_key[a]);
+    }
+    const float amax = __uint_as_float(g->amax_key);
+    float rmax = __uint_as_float(g->rmax_key), dmax = 0.f;
+    if (!c.radii_in) {
+        rmax = 0.f;
+        for (int t = 0; t < c.n_types; ++t)
+            if ((g->present[t >> 5] >> (t & 31)) & 1u) {
+                rmax = fmaxf(rmax, c.type_radius[t]);
+                dmax = fmaxf(dmax, c.dot_reach[t]);
+            }
+    } else {
+        dmax = (rmax + c.probe) * c.unit_reach;
+    }
+    const float margin = 0.01f + 8e-6f * amax;
+    double cell = ((double)dmax * 1.000001 + c.probe + rmax + margin) * 1.001 + 1e-3;
+    double d[3];
+    for (;;) {
+        double total = 1.0;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            d[a] = floor(((double)hi[a] - (double)lo[a]) / cell) + 1.0;
+            total *= d[a];
+        }
+        if (total <= 4.0 * c.n_atoms + 4096.0)
+            break;
+        cell *= 1.5; // sparse, wide boxes: fewer, larger cells (still exact)
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        g->lo[a] = lo[a];
+        g->dims[a] = (int)d[a];
+    }
+    g->n_cells = (int)d[0] * (int)d[1] * (int)d[2];
+    g->margin = margin;
+    g->inv_cell = 1.0 / cell;
+}
+
 // ---- cell list --------------------------------------------------------------
 
 __global__ void sasa_bin_kernel(const SasaCellArgs c)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c.n_atoms)
+    const SasaGeom *g = c.geom;
+    if (i >= c.n_atoms || g->bad)
         return;
     const float4 p = c.atoms_in[i];
     int k[3];
-    cell_coords(p.x, p.y, p.z, c.lo, c.inv_cell, c.dims, k);
-    const int cid = (k[0] * c.dims[1] + k[1]) * c.dims[2] + k[2];
+    cell_coords(p.x, p.y, p.z, g->lo, g->inv_cell, g->dims, k);
+    const int cid = (k[0] * g->dims[1] + k[1]) * g->dims[2] + k[2];
     c.cell_of[i] = cid;
     c.rank_of[i] = atomicAdd(&c.cell_count[cid], 1);
 }
 
 // Exclusive prefix sum of the cell counts by one CTA (cells number at most
 // 4 n + 4096), 4 cells per thread per tile.
-__global__ void __launch_bounds__(1024) sasa_scan_kernel(const int *count, int *start, int n)
+__global__ void __launch_bounds__(1024) sasa_scan_kernel(const int *count, int *start,
+                                                          const SasaGeom *g)
 {
     __shared__ int s_warp[32];
     __shared__ int s_carry;
+    if (g->bad)
+        return; // the whole CTA leaves before its first barrier
+    const int n = g->n_cells;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0)
         s_carry = 0;
@@ -134,10 +275,11 @@ __global__ void __launch_bounds__(1024) sasa_scan_kernel(const int *count, int *
 __global__ void sasa_scatter_kernel(const SasaCellArgs c)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c.n_atoms)
+    if (i >= c.n_atoms || c.geom->bad)
         return;
     const float4 p = c.atoms_in[i];
     const int s = c.cell_start[c.cell_of[i]] + c.rank_of[i];
+    // (types were checked by sasa_geom_kernel: a bad one stops the call)
     float r;
     if (c.radii_in) {
         r = c.radii_in[i];
@@ -155,14 +297,20 @@ cudaError_t launch_sasa_cells(const SasaCellArgs &c, cudaStream_t st)
 {
     if (c.n_atoms == 0)
         return cudaSuccess;
-    cudaError_t e = cudaMemsetAsync(c.cell_count, 0, sizeof(int) * (size_t)(c.n_cells + 1), st);
+    if ((long long)c.cells_cap < 4LL * c.n_atoms + 4097)
+        return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(c.geom, 0, sizeof(SasaGeom), st);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(c.cell_count, 0, sizeof(int) * (size_t)c.cells_cap, st);
     if (e != cudaSuccess)
         return e;
     const int blocks = (c.n_atoms + 255) / 256;
+    sasa_geom_kernel<<<std::min(blocks, 1024), 256, 0, st>>>(c);
+    sasa_plan_kernel<<<1, 32, 0, st>>>(c);
     sasa_bin_kernel<<<blocks, 256, 0, st>>>(c);
-    sasa_scan_kernel<<<1, 1024, 0, st>>>(c.cell_count, c.cell_start, c.n_cells);
+    sasa_scan_kernel<<<1, 1024, 0, st>>>(c.cell_count, c.cell_start, c.geom);
     sasa_scatter_kernel<<<blocks, 256, 0, st>>>(c);
-    count_launch(3);
+    count_launch(5);
     return cudaGetLastError();
 }
 
@@ -350,8 +498,10 @@ __global__ void __launch_bounds__(kSasaWarps * 32, 8) sasa_kernel(const SasaArgs
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i = blockIdx.x * kSasaWarps + warp; // cell order
-    if (i >= a.n_atoms)
+    const SasaGeom *geom = a.geom;
+    if (i >= a.n_atoms || geom->bad)
         return; // the whole warp leaves; no CTA-wide barrier follows
+    const int dims[3] = {geom->dims[0], geom->dims[1], geom->dims[2]};
     float4 *list = s_list[warp];
     unsigned char *band = s_band[warp];
     unsigned *open = s_open[warp];
@@ -362,7 +512,7 @@ __global__ void __launch_bounds__(kSasaWarps * 32, 8) sasa_kernel(const SasaArgs
     const float ext = __fadd_rn(p.w, a.probe);
     // an occluder b of a dot of this atom lies within |d| + P + r_b of it
     const float dot_reach = a.typed ? a.dot_reach[t] : ext * a.unit_reach;
-    const float reach = dot_reach * 1.000001f + a.probe + a.margin;
+    const float reach = dot_reach * 1.000001f + a.probe + geom->margin;
     for (int g = lane; g < ng; g += 32)
         open[g] = kFull; // narrowed to the valid dots by the first test_list
     __syncwarp();
@@ -372,11 +522,11 @@ __global__ void __launch_bounds__(kSasaWarps * 32, 8) sasa_kernel(const SasaArgs
     int cc[3];
     {
         const int cid = a.cell_id[i]; // (x * dims1 + y) * dims2 + z
-        cc[2] = cid % a.dims[2];
-        cc[1] = (cid / a.dims[2]) % a.dims[1];
-        cc[0] = cid / (a.dims[2] * a.dims[1]);
+        cc[2] = cid % dims[2];
+        cc[1] = (cid / dims[2]) % dims[1];
+        cc[0] = cid / (dims[2] * dims[1]);
     }
-    const int z0 = max(cc[2] - 1, 0), z1 = min(cc[2] + 1, a.dims[2] - 1);
+    const int z0 = max(cc[2] - 1, 0), z1 = min(cc[2] + 1, dims[2] - 1);
     int row = 0, pos = 0, n_list = 0;
     bool walk_done = false;
     unsigned long long tests = 0;
@@ -387,8 +537,8 @@ __global__ void __launch_bounds__(kSasaWarps * 32, 8) sasa_kernel(const SasaArgs
             int beg = 0, end = 0;
             while (row < 9) {
                 const int x = cc[0] + row / 3 - 1, y = cc[1] + row % 3 - 1;
-                if (x >= 0 && y >= 0 && x < a.dims[0] && y < a.dims[1]) {
-                    const int c = (x * a.dims[1] + y) * a.dims[2];
+                if (x >= 0 && y >= 0 && x < dims[0] && y < dims[1]) {
+                    const int c = (x * dims[1] + y) * dims[2];
                     beg = a.cell_start[c + z0] + pos;
                     end = a.cell_start[c + z1 + 1];
                     if (beg < end)
