@@ -82,6 +82,12 @@ int rsx_debug_theta_level(int uniform, double dq, double diag);
  * q of the remainder slab, q it covers, width of its kernel (0: none). */
 rsx_status rsx_debug_wide_plan(int n_q, int q_slab, int *out);
 
+/* Host-only view of the chain plan of the uniform forward (q_slab 192, no
+ * water): out[0..4] = chains of three 192-q slabs from q 0, first q of the
+ * rest chain, its 192-q slabs, its tail slab's width (a multiple of 16, 0 for
+ * none), 1 if there is a rest chain. */
+rsx_status rsx_debug_chain_plan(int n_q, int *out);
+
 /* Host-only check of the shard split used by rsx_debye_calc_shard: item
  * bounds[0..n_shards] (shard s = items [bounds[s], bounds[s+1])) and, if
  * pairs is not NULL, the body pairs of each shard. */

@@ -82,6 +82,7 @@ SIGNATURES = [
     ("rsx_debye_calc_shard", _st, [_vp, _f32p, _i, _i, _f64p]),
     ("rsx_debug_theta_level", _i, [_i, ctypes.c_double, ctypes.c_double]),
     ("rsx_debug_wide_plan", _st, [_i, _i, np.ctypeslib.ndpointer(np.int32)]),
+    ("rsx_debug_chain_plan", _st, [_i, np.ctypeslib.ndpointer(np.int32)]),
     ("rsx_debug_shard_items", _st, [_f32p, _i, _i, _i, _i, np.ctypeslib.ndpointer(np.int32),
                                     _vp]),
     ("rsx_debug_autotune_lookup", _i, [ctypes.c_char_p, ctypes.POINTER(_i)]),

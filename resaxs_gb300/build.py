@@ -22,7 +22,7 @@ LIB = os.path.join(PKG, "librsx.so")
 BIN_DIR = os.path.join(PKG, "bin")
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
-CUDA_SOURCES = ["debye_kernels.cu", "adjoint_kernels.cu", "grid_kernels.cu", "sasa_kernels.cu", "batch_kernels.cu", "calib_kernels.cu",
+CUDA_SOURCES = ["debye_kernels.cu", "chain_kernels.cu", "adjoint_kernels.cu", "grid_kernels.cu", "sasa_kernels.cu", "batch_kernels.cu", "calib_kernels.cu",
                 "noalloc_kernels.cu"]
 HOST_SOURCES = ["rsx_common.cpp", "rsx_debye.cpp", "rsx_sasa.cpp", "rsx_batch.cpp",
                 "rsx_ff.cpp", "rsx_autotune.cpp",

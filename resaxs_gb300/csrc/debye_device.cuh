@@ -284,6 +284,16 @@ __device__ __forceinline__ WideSeed wide_seed(float q0, float dq, float r, float
 
 __device__ __forceinline__ float2 splat2(float x) { return make_float2(x, x); }
 
+// A chain's state between two slabs keeps the sign of its odd steps (sg, +1
+// or -1) in the sign bit of lam, which is -4 x^2 (sign bit set, -0.0
+// included): a clear sign bit stands for sg = -1.
+__device__ __forceinline__ float pack_lam_sign(float l, float sg) { return sg > 0.f ? l : -l; }
+__device__ __forceinline__ void unpack_lam_sign(float x, float &l, float &sg)
+{
+    sg = signbit(x) ? 1.f : -1.f;
+    l = -fabsf(x);
+}
+
 // Two pairs, interleaved for ILP (the hot loop: per paired step of both
 // pairs 6 FP32x2 instructions = 12 lane-ops for 4 pair*q).  S[m] holds
 // (q_{2m}, q_{2m+1}).  SIGNED adds the odd steps with the pairs' signs;

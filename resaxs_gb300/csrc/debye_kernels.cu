@@ -238,15 +238,6 @@ __global__ void __launch_bounds__(kBlockAtoms) delta_kernel(const DeltaArgs a)
     }
 }
 
-// sg (+1 or -1) rides in the sign bit of lam, which is -4 x^2 (sign bit set,
-// -0.0 included): a clear sign bit stands for sg = -1.
-__device__ __forceinline__ float pack_lam_sign(float l, float sg) { return sg > 0.f ? l : -l; }
-__device__ __forceinline__ void unpack_lam_sign(float x, float &l, float &sg)
-{
-    sg = signbit(x) ? 1.f : -1.f;
-    l = -fabsf(x);
-}
-
 // Incremental delta on a uniform grid.  A CTA takes one static block and one
 // group of moved tiles over a chain of two slabs, [k0, k0 + Q1) and
 // [k0 + Q1, k0 + Q1 + Q2) (Q2 = 0: one slab), so each pair chain (new and
@@ -596,6 +587,10 @@ WidePlan wide_plan(int n_q, int q_slab)
 static cudaError_t launch_forward_wide(const DebyeArgs &a, int q_slab, bool water, cudaStream_t st,
                                        const AuxStream *aux)
 {
+    // q_slab 192: chains of 192-q slabs with one seed per pair and chain
+    // (four pairs per step keep the slab kernels)
+    if (!water && q_slab >= 192 && !a.pairs4)
+        return launch_forward_chain(a, st, aux);
     const WidePlan p = wide_plan(a.n_q, water ? std::min(q_slab, 128) : q_slab);
     const bool split = aux && p.full > 0 && p.tail_len > 0;
     if (split) {

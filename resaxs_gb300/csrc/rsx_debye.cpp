@@ -998,6 +998,19 @@ int rsx_debug_theta_level(int uniform, double dq, double diag)
     return theta_level(uniform != 0, dq, diag);
 }
 
+rsx_status rsx_debug_chain_plan(int n_q, int *out)
+{
+    if (n_q <= 0 || !out)
+        return fail(RSX_INVALID_ARG, "need n_q > 0 and an output");
+    const ChainPlan p = chain_plan(n_q);
+    out[0] = p.full;
+    out[1] = p.rest_k0;
+    out[2] = p.rest_main;
+    out[3] = p.rest_tail;
+    out[4] = p.rest ? 1 : 0;
+    return ok();
+}
+
 rsx_status rsx_debug_wide_plan(int n_q, int q_slab, int *out)
 {
     if (n_q <= 0 || !out || (q_slab != 64 && q_slab != 128 && q_slab != 192))

@@ -128,6 +128,16 @@ struct AuxStream {
 };
 cudaError_t launch_forward(const DebyeArgs &a, int q_slab, bool uniform, bool water,
                            cudaStream_t st, const AuxStream *aux = nullptr);
+// Chained forward on uniform grids without water (chain_kernels.cu): `full`
+// chains of three 192-q slabs from q 0, then (rest) one chain from rest_k0
+// of rest_main 192-q slabs and a rest_tail-q tail (a multiple of 16, 0 for
+// none); each pair is seeded once per chain.
+struct ChainPlan {
+    int full, rest_k0, rest_main, rest_tail;
+    bool rest;
+};
+ChainPlan chain_plan(int n_q);
+cudaError_t launch_forward_chain(const DebyeArgs &a, cudaStream_t st, const AuxStream *aux);
 cudaError_t launch_assemble(const AssembleArgs &a, cudaStream_t st);
 // adjoint through tabulated pair functions: builds the tables of the present
 // type pairs into `tab` ([n_types^2][adj_nodes] float4, times 4 with water),

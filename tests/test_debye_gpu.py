@@ -364,3 +364,24 @@ def test_autotuned_slab(saxs, oracle_lib):
     _, again, cfg2 = gpu_curve(saxs, w.q, w.ff, w.bodies, autotune=True)   # cached choice
     assert cfg2["q_slab"] == cfg["q_slab"]
     assert rel(again, out64) < 1e-12
+
+
+@pytest.mark.parametrize("n_q,q_max,spread", [(190, 0.5, 1.0), (577, 0.5, 1.0), (700, 2.0, 8.0),
+                                              (1200, 0.6, 1.0)])
+def test_chained_forward_plans(saxs, oracle_lib, n_q, q_max, spread):
+    """The chained forward (one seed per pair and chain of up to three 192-q
+    slabs): 190 q as one 192-q slab, a full 576-q chain plus a 1-q rest, a
+    spread structure whose far pairs take the signed steps (700 q to 2.0/A:
+    576 + 124), and two full chains plus a rest chain of 48 q on the second
+    stream; FP64 oracle on every q."""
+    w = W.make_config(2, seed=21, n_override=1300)
+    bodies = w.bodies.copy()
+    bodies[:, :3] *= np.float32(spread)
+    rng = np.random.default_rng(n_q)
+    q = W.q_grid(n_q, q_max)
+    ff = W.exp_form_factors(q, W.Z5, rng.uniform(0.5, 2.0, 5))
+    with saxs.Debye(q, ff, len(bodies)) as d:
+        d.calc(bodies)
+        out64 = d.curve_f64()
+    ref = oracle_lib.debye_f64(q, bodies, ff)
+    assert rel(out64, ref) < TOL, rel(out64, ref)
