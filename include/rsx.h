@@ -83,7 +83,7 @@ int rsx_debug_theta_level(int uniform, double dq, double diag);
 rsx_status rsx_debug_wide_plan(int n_q, int q_slab, int *out);
 
 /* Host-only view of the chain plan of the uniform forward (q_slab 192, no
- * water): out[0..4] = chains of three 192-q slabs from q 0, first q of the
+ * water): out[0..4] = chains of two 192-q slabs from q 0, first q of the
  * rest chain, its 192-q slabs, its tail slab's width (a multiple of 16, 0 for
  * none), 1 if there is a rest chain. */
 rsx_status rsx_debug_chain_plan(int n_q, int *out);
@@ -152,9 +152,11 @@ typedef struct rsx_debye_options {
     int q_slab;          /* q values per CTA slab: 8, 16, 32, 64, 128 or 192; 0 = tuned /
                             default (192 on uniform grids of 64 q or more).  On
                             uniform grids 64, 128 and 192 select the wide slabs
-                            (64, up to 128, or up to 192 q per recurrence seed;
-                            192-q slabs for the forward without water only, at
-                            2 CTAs/SM); the other kernels take at most 128. */
+                            (64, up to 128, or up to 192 q per recurrence seed);
+                            192 runs the forward without water as chains of up
+                            to two 192-q slabs and a tail on one seed per pair
+                            (with pairs_per_step 4: 192-q slabs); the other
+                            kernels take at most 128. */
     int max_items;       /* cap on forward work items (scratch = items*n_q*8 B); 0 = default */
     int force_general_q; /* 1: never use the uniform-grid recurrence */
     int timing;          /* 1: record CUDA events around the pair kernel */

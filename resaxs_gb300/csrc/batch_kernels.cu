@@ -35,6 +35,30 @@ __global__ void __launch_bounds__(kBlockAtoms)
     }
 }
 
+// Chained forward (forward_chain_item) over work units (item, chain) handed
+// out by the counter, largest items first; chain c starts at
+// k_chain0 + c * chain_q.
+template <int QT, bool SIGNED>
+__global__ void __launch_bounds__(kBlockAtoms, 2)
+    batch_chain_kernel(const DebyeArgs a, const int *work_order, int n_units, int n_chains,
+                       int k_chain0, int chain_q, int n_main, int q_slots, int *counter)
+{
+    extern __shared__ __align__(16) unsigned char dsm[];
+    __shared__ int s_w;
+    for (;;) {
+        if (threadIdx.x == 0)
+            s_w = atomicAdd(counter, 1);
+        __syncthreads();
+        const int w = s_w;
+        __syncthreads();
+        if (w >= n_units)
+            break;
+        forward_chain_item<QT, SIGNED>(a, work_order[w / n_chains],
+                                       k_chain0 + (w % n_chains) * chain_q, chain_q, n_main,
+                                       q_slots, dsm);
+    }
+}
+
 // Wide uniform slabs with the implicit water term, as forward_wide_water_kernel.
 template <int QS, bool SIGNED>
 __global__ void __launch_bounds__(kBlockAtoms, (QS <= 64 || !SIGNED) ? 3 : 2)
@@ -213,6 +237,7 @@ cudaError_t launch_batch_forward(const DebyeArgs &a, const int *work_order, int 
 template <class K>
 static int occupancy_grid(K kfn, size_t smem, int sms);
 
+
 template <int QS>
 static cudaError_t wide_batch_water_launch(const DebyeArgs &a, const int *order, int n_items,
                                            int n_slabs, int k_base, int *counter, int sms,
@@ -295,6 +320,81 @@ cudaError_t launch_batch_forward_wide(const DebyeArgs &a, const int *work_order,
         RSX_BW(128);
     }
 #undef RSX_BW
+}
+
+template <int QT>
+static cudaError_t batch_chain_launch(const DebyeArgs &a, const int *order, int n_items,
+                                      int n_chains, int k_chain0, int n_main, int *counter,
+                                      int sms, cudaStream_t st)
+{
+    const int chain_q = n_main * kChainMain + QT;
+    const int q_slots = n_main * kChainMain + (QT + 31) / 32 * 32;
+    const size_t smem = chain_smem_bytes(q_slots);
+    auto kfn = a.small_theta >= 2 ? batch_chain_kernel<QT, false> : batch_chain_kernel<QT, true>;
+    if (smem > 32 * 1024) { // with the static arrays past the 48 KB default
+        const cudaError_t e =
+            cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess)
+            return e;
+    }
+    const int grid = std::min(occupancy_grid(kfn, smem, sms), n_items * n_chains);
+    kfn<<<grid, kBlockAtoms, smem, st>>>(a, order, n_items * n_chains, n_chains, k_chain0, chain_q,
+                                        n_main, q_slots, counter);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_forward_chain(const DebyeArgs &a, const int *work_order,
+                                       int n_work_items, int *counters, int sms, cudaStream_t st)
+{
+    if (n_work_items == 0)
+        return cudaSuccess;
+    const ChainPlan p = chain_plan(a.n_q);
+    if (p.full > 0) {
+        const cudaError_t e = batch_chain_launch<0>(a, work_order, n_work_items, p.full, 0,
+                                                    kChainMaxMain, counters, sms, st);
+        if (e != cudaSuccess)
+            return e;
+    }
+    if (!p.rest)
+        return cudaSuccess;
+    // a rest of one tail slab only: the slab kernels (a chain pays its
+    // sub-tile reductions for nothing when no slab follows)
+    if (p.rest_main == 0 && p.rest_tail <= 128) {
+#define RSX_BT(QS)                                                                         \
+    return wide_batch_launch<QS>(a, work_order, n_work_items, 1, p.rest_k0, counters + 1, sms, st)
+        switch (p.rest_tail / 16) {
+        case 1: RSX_BT(16);
+        case 2: RSX_BT(32);
+        case 3: RSX_BT(48);
+        case 4: RSX_BT(64);
+        case 5: RSX_BT(80);
+        case 6: RSX_BT(96);
+        case 7: RSX_BT(112);
+        default: RSX_BT(128);
+        }
+#undef RSX_BT
+    }
+#define RSX_BC(QT)                                                                         \
+    return batch_chain_launch<QT>(a, work_order, n_work_items, 1, p.rest_k0, p.rest_main,   \
+                                  counters + 1, sms, st)
+    switch (p.rest_tail / 16) {
+    case 0: RSX_BC(0);
+    case 1: RSX_BC(16);
+    case 2: RSX_BC(32);
+    case 3: RSX_BC(48);
+    case 4: RSX_BC(64);
+    case 5: RSX_BC(80);
+    case 6: RSX_BC(96);
+    case 7: RSX_BC(112);
+    case 8: RSX_BC(128);
+    case 9: RSX_BC(144);
+    case 10: RSX_BC(160);
+    case 11: RSX_BC(176);
+    default:
+        return cudaErrorInvalidValue;
+    }
+#undef RSX_BC
 }
 
 template <int QS, bool U>

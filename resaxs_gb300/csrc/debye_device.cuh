@@ -1574,4 +1574,148 @@ __device__ __forceinline__ void adjoint_item(const DebyeArgs &a, int item_idx, i
         adjoint_general_item<QS, UNIFORM, WATER>(a, item_idx, n_slabs);
 }
 
+// ----------------------------------------------------------------------------
+// forward, uniform q grid without water: chained slabs
+// ----------------------------------------------------------------------------
+//
+// A work item over a chain of up to two 192-q slabs and a QT-q tail: the J
+// side is taken kChainPairs bodies at a time; every pair chain of such a
+// sub-tile is seeded once, at the start of the chain, runs through the first
+// slab, leaves its recurrence state (s, d of the even/odd sequences, lam with
+// the sign of the odd steps) in shared memory while the slab's sums are
+// reduce-scattered into per-lane FP64 accumulators (shared memory: lane L
+// owns q index 32 c + L of every slab), and resumes from it in the next slab.
+
+template <int QS, int QH, bool SIGNED>
+__device__ __forceinline__ void chain_steps(WideSeed &p1, WideSeed &p2, float2 (&S)[QH])
+{
+    if constexpr (SIGNED) {
+        if (__any_sync(0xffffffffu, p1.sg < 0.f || p2.sg < 0.f))
+            wide_pair2_carry<QS, QH, true>(p1, p2, S);
+        else
+            wide_pair2_carry<QS, QH, false>(p1, p2, S);
+    } else {
+        wide_pair2_carry<QS, QH, false>(p1, p2, S);
+    }
+}
+
+// Forward pair sums of one work item over the chain q [k0, k0 + chain_q)
+// (n_main 192-q slabs, then a QT-q tail): writes partial[k][item_idx] = sum
+// over the item's pairs of f_i f_j sin(q_k r)/r.  q_slots = n_main * 192 + QT
+// rounded up to 32 (the accumulator stride); dsm: chain_smem_bytes(q_slots)
+// of dynamic shared memory.  Called once per CTA by forward_chain_kernel and
+// repeatedly by the persistent batch kernel (hence the leading barrier).
+template <int QT, bool SIGNED>
+__device__ __forceinline__ void forward_chain_item(const DebyeArgs &a, int item_idx, int k0,
+                                                   int chain_q, int n_main, int q_slots,
+                                                   unsigned char *dsm)
+{
+    constexpr int QM = kChainMain, QH = QM / 2, T = kChainPairs;
+    static_assert(QT % 16 == 0 && QT <= QM, "tail slab");
+    __shared__ float4 s_pos[kBlockAtoms];
+    float2 *st_sd = reinterpret_cast<float2 *>(dsm);                       // [T][2][128]
+    float *st_l = reinterpret_cast<float *>(dsm + sizeof(float2) * 2 * T * kBlockAtoms); // [T][128]
+    double *acc = reinterpret_cast<double *>(dsm + chain_state_bytes());   // [4][q_slots]
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    __syncthreads(); // a previous item of this CTA may still read shared memory
+    const PairItem it = a.items[item_idx];
+    const BlockDesc bi = a.blocks[it.bi];
+    const int tj = a.blocks[it.bj_begin].type;
+    const int i = bi.start + tid;
+    const bool valid_i = tid < bi.len;
+    const float4 pi = valid_i ? a.pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float q0 = a.q[k0];
+    const float dq = a.dq;
+    const bool small_th = !SIGNED || a.small_theta >= 2;
+    const int n_slabs = n_main + (QT > 0 ? 1 : 0);
+
+    double *my_acc = acc + (size_t)warp * q_slots;
+    for (int k = lane; k < q_slots; k += 32)
+        my_acc[k] = 0.0;
+
+    for (int b = it.bj_begin; b < it.bj_end; ++b) {
+        const BlockDesc bj = a.blocks[b];
+        __syncthreads();
+        // slots past the block's end repeat its last body: a finite pair
+        // distance, and the pair is masked
+        s_pos[tid] = a.pos[bj.start + min(tid, bj.len - 1)];
+        __syncthreads();
+        const bool diag = (b == it.bi);
+        for (int sub = 0; sub < bj.len; sub += T) {
+            const int np = min(T, bj.len - sub);
+            for (int s = 0; s < n_slabs; ++s) {
+                const bool first = s == 0, last = s == n_slabs - 1, tail = s >= n_main;
+                float2 S[QH];
+#pragma unroll
+                for (int m = 0; m < QH; ++m)
+                    S[m] = make_float2(0.f, 0.f);
+                for (int jp = 0; jp < np; jp += 2) {
+                    const int j = sub + jp;
+                    WideSeed p1, p2;
+                    float2 *sd = st_sd + (size_t)jp * 2 * kBlockAtoms + tid;
+                    float *sl = st_l + (size_t)jp * kBlockAtoms + tid;
+                    if (first) {
+                        float r1, ri1, r2, ri2, dx, dy, dz;
+                        pair_r(pi, s_pos[j], r1, ri1, dx, dy, dz);
+                        pair_r(pi, s_pos[min(j + 1, kBlockAtoms - 1)], r2, ri2, dx, dy, dz);
+                        const bool u1 = valid_i && (!diag || j > tid);
+                        const bool u2 = valid_i && jp + 1 < np && (!diag || j + 1 > tid);
+                        p1 = wide_seed(q0, dq, r1, u1 ? ri1 : 0.f, small_th);
+                        p2 = wide_seed(q0, dq, r2, u2 ? ri2 : 0.f, small_th);
+                    } else {
+                        p1.s = sd[0];
+                        p1.d = sd[kBlockAtoms];
+                        p2.s = sd[2 * kBlockAtoms];
+                        p2.d = sd[3 * kBlockAtoms];
+                        unpack_lam_sign(sl[0], p1.l, p1.sg);
+                        unpack_lam_sign(sl[kBlockAtoms], p2.l, p2.sg);
+                    }
+                    if (tail) {
+                        if constexpr (QT > 0)
+                            chain_steps<QT, QH, SIGNED>(p1, p2, S);
+                    } else {
+                        chain_steps<QM, QH, SIGNED>(p1, p2, S);
+                    }
+                    if (!last) {
+                        sd[0] = p1.s;
+                        sd[kBlockAtoms] = p1.d;
+                        sd[2 * kBlockAtoms] = p2.s;
+                        sd[3 * kBlockAtoms] = p2.d;
+                        sl[0] = pack_lam_sign(p1.l, p1.sg);
+                        sl[kBlockAtoms] = pack_lam_sign(p2.l, p2.sg);
+                    }
+                }
+                // the slab's sums of this sub-tile into the lane accumulators
+                const int base = s * QM;
+                const int n_chunks = tail ? (QT + 31) / 32 : QM / 32;
+#pragma unroll
+                for (int c = 0; c < QM / 32; ++c) {
+                    if (c >= n_chunks)
+                        break;
+                    float v[32];
+#pragma unroll
+                    for (int k = 0; k < 32; ++k)
+                        v[k] = pair_at(S, 32 * c + k);
+                    warp_reduce_scatter<32>(v, lane);
+                    my_acc[base + 32 * c + lane] += (double)v[0];
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (int k = tid; k < chain_q; k += kBlockAtoms) {
+        const int kk = k0 + k;
+        if (kk >= a.n_q)
+            continue;
+        double s = 0.0;
+#pragma unroll
+        for (int w = 0; w < kBlockAtoms / 32; ++w)
+            s += acc[(size_t)w * q_slots + k];
+        const double fi = a.ff[(size_t)kk * a.n_types + bi.type];
+        const double fj = a.ff[(size_t)kk * a.n_types + tj];
+        a.partial[(size_t)kk * a.n_items + item_idx] = s * fi * fj;
+    }
+}
+
 } // namespace rsx

@@ -549,6 +549,11 @@ static cudaError_t wide_tail(const DebyeArgs &a, int k0, int width, bool water, 
     }
 }
 
+cudaError_t launch_forward_slab(const DebyeArgs &a, int k0, int width, cudaStream_t st)
+{
+    return wide_tail(a, k0, width, false, st);
+}
+
 // The cheapest of: 64-q slabs and a tail; 64-q slabs with a short remainder
 // (<= 48 q) folded into the last slab; 112-q or 128-q slabs and a tail
 // (q_slab >= 128); 192-q slabs and a tail of at most 128 q (q_slab >= 192).

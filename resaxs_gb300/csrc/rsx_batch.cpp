@@ -352,7 +352,12 @@ rsx_status enqueue_pass(rsx_batch *h, bool with_adjoint, int q_slab)
     const int n_items = (int)h->items.size();
     const bool water = has_water(h);
     const bool wide = h->uniform && q_slab >= 64;
-    if (wide)
+    // q_slab 192 without water and with two pairs per step: chained slabs
+    if (wide && !water && q_slab >= 192 && h->pairs_per_step != 4)
+        RSX_TRY_CUDA(launch_batch_forward_chain(a, h->d_order, n_items, h->d_counter, h->sms,
+                                                h->st),
+                     "batch forward");
+    else if (wide)
         RSX_TRY_CUDA(launch_batch_forward_wide(a, h->d_order, n_items, q_slab, h->d_counter,
                                                h->sms, h->st, water),
                      "batch forward");

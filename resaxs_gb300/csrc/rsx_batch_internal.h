@@ -44,6 +44,10 @@ cudaError_t launch_batch_forward(const DebyeArgs &a, const int *work_order, int 
 cudaError_t launch_batch_forward_wide(const DebyeArgs &a, const int *work_order,
                                       int n_work_items, int q_slab, int *counters, int sms,
                                       cudaStream_t st, bool water = false);
+// Chained forward (uniform grid, no water, q_slab 192): persistent launches
+// over the full chains (counters[0]) and the rest chain (counters[1]).
+cudaError_t launch_batch_forward_chain(const DebyeArgs &a, const int *work_order,
+                                       int n_work_items, int *counters, int sms, cudaStream_t st);
 cudaError_t launch_batch_adjoint(const DebyeArgs &a, const int *work_order, int n_work_items,
                                  int q_slab, bool uniform, int *counter, int grid,
                                  cudaStream_t st);

@@ -128,15 +128,35 @@ struct AuxStream {
 };
 cudaError_t launch_forward(const DebyeArgs &a, int q_slab, bool uniform, bool water,
                            cudaStream_t st, const AuxStream *aux = nullptr);
+// Chained forward: 192-q main slabs, at most two per chain (the recurrence
+// runs at most 192 paired steps per seed; at 200,000 bodies and 512 q, chains
+// of three slabs left 3e-6 of error 250 paired steps after the seed), J
+// sub-tiles of 32 bodies whose recurrence states wait in shared memory
+// between slabs.
+constexpr int kChainMain = 192;
+constexpr int kChainMaxMain = 2;
+constexpr int kChainPairs = 32;
+// dynamic shared memory of a chain CTA: the states, then the per-warp FP64
+// lane accumulators of q_slots q
+__host__ __device__ constexpr size_t chain_state_bytes()
+{
+    return (sizeof(float2) * 2 + sizeof(float)) * kChainPairs * kBlockAtoms;
+}
+__host__ __device__ constexpr size_t chain_smem_bytes(int q_slots)
+{
+    return chain_state_bytes() + sizeof(double) * (kBlockAtoms / 32) * (size_t)q_slots;
+}
 // Chained forward on uniform grids without water (chain_kernels.cu): `full`
-// chains of three 192-q slabs from q 0, then (rest) one chain from rest_k0
-// of rest_main 192-q slabs and a rest_tail-q tail (a multiple of 16, 0 for
+// chains of two 192-q slabs from q 0, then (rest) one chain from rest_k0 of
+// rest_main 192-q slabs and a rest_tail-q tail (a multiple of 16, 0 for
 // none); each pair is seeded once per chain.
 struct ChainPlan {
     int full, rest_k0, rest_main, rest_tail;
     bool rest;
 };
 ChainPlan chain_plan(int n_q);
+// One wide slab of `width` q (16..128, a multiple of 16) from k0, no water.
+cudaError_t launch_forward_slab(const DebyeArgs &a, int k0, int width, cudaStream_t st);
 cudaError_t launch_forward_chain(const DebyeArgs &a, cudaStream_t st, const AuxStream *aux);
 cudaError_t launch_assemble(const AssembleArgs &a, cudaStream_t st);
 // adjoint through tabulated pair functions: builds the tables of the present

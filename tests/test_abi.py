@@ -133,19 +133,19 @@ def test_wide_slab_plan_covers_every_q(librsx):
 
 
 def test_chain_plan_covers_every_q(librsx):
-    """The chain plan of the uniform forward: full chains of 576 q from q 0,
-    then one rest chain of up to three 192-q slabs and a tail of 16..176 q (a
+    """The chain plan of the uniform forward: full chains of 384 q from q 0,
+    then one rest chain of up to two 192-q slabs and a tail of 16..176 q (a
     multiple of 16) that covers [rest_k0, n_q) with less than 16 q to spare."""
     from resaxs_gb300 import _lib
     out = np.zeros(5, np.int32)
     for n_q in range(1, 2500):
         _lib.check(librsx.rsx_debug_chain_plan(n_q, out))
         full, k0, main, tail, rest = (int(x) for x in out)
-        assert k0 == 576 * full and k0 <= n_q, (n_q, out)
+        assert k0 == 384 * full and k0 <= n_q, (n_q, out)
         assert rest == (k0 < n_q), (n_q, out)
         if rest:
             covered = 192 * main + tail
-            assert tail % 16 == 0 and 0 <= tail <= 176 and 0 <= main <= 3, (n_q, out)
+            assert tail % 16 == 0 and 0 <= tail <= 176 and 0 <= main <= 2, (n_q, out)
             assert n_q - k0 <= covered < n_q - k0 + 16, (n_q, out)
     assert librsx.rsx_debug_chain_plan(0, out) == _lib.RSX_INVALID_ARG
 

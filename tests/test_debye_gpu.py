@@ -369,11 +369,11 @@ def test_autotuned_slab(saxs, oracle_lib):
 @pytest.mark.parametrize("n_q,q_max,spread", [(190, 0.5, 1.0), (577, 0.5, 1.0), (700, 2.0, 8.0),
                                               (1200, 0.6, 1.0)])
 def test_chained_forward_plans(saxs, oracle_lib, n_q, q_max, spread):
-    """The chained forward (one seed per pair and chain of up to three 192-q
-    slabs): 190 q as one 192-q slab, a full 576-q chain plus a 1-q rest, a
-    spread structure whose far pairs take the signed steps (700 q to 2.0/A:
-    576 + 124), and two full chains plus a rest chain of 48 q on the second
-    stream; FP64 oracle on every q."""
+    """The chained forward (one seed per pair and chain of up to two 192-q
+    slabs): 190 q as one 192-q slab, a full 384-q chain and a 192 + 16 rest
+    chain (577 q), a spread structure whose far pairs take the signed steps
+    (700 q to 2.0/A: 384, then 192 + 128), and three full chains with a 48-q
+    rest slab on the second stream (1,200 q); FP64 oracle on every q."""
     w = W.make_config(2, seed=21, n_override=1300)
     bodies = w.bodies.copy()
     bodies[:, :3] *= np.float32(spread)

@@ -1,8 +1,9 @@
 """Precision at the full 200,000-body configuration: FP32 kernel with FP64
 cross-block reduction against the FP64 oracle on 15 of the 512 q values (the
-FP32 grid values themselves), chosen at the starts, middles and ends of the
-four 128-q slabs the kernels run at 512 q, so both the seeds and the
-recurrence are covered.  Bound: 1e-5 relative per q."""
+FP32 grid values themselves), chosen along the chain of 192 + 192 + 128 q the
+forward runs at 512 q: its start (the seed), both slab boundaries (where the
+recurrence resumes from shared memory) and its far end (288 paired steps
+after the seed).  Bound: 1e-5 relative per q."""
 import numpy as np
 import pytest
 
@@ -18,7 +19,7 @@ def test_config4_per_q_error():
     with Debye(w.q, w.ff, w.n) as d:
         d.calc(w.bodies)
         out = d.curve_f64()
-    sel = np.array([0, 63, 100, 127, 128, 200, 255, 256, 300, 383, 384, 420, 448, 480, 511])
+    sel = np.array([0, 100, 191, 192, 200, 255, 256, 300, 383, 384, 420, 448, 480, 500, 511])
     ref = oracle.debye_f64(w.q[sel].astype(np.float64), w.bodies, w.ff[sel])
     err = np.abs(out[sel] - ref) / np.abs(ref)
     print("config4 q:", [round(float(x), 4) for x in w.q[sel]])
