@@ -593,9 +593,17 @@ static cudaError_t launch_forward_wide(const DebyeArgs &a, int q_slab, bool wate
                                        const AuxStream *aux)
 {
     // q_slab 192: chains of 192-q slabs with one seed per pair and chain
-    // (four pairs per step keep the slab kernels)
-    if (!water && q_slab >= 192 && !a.pairs4)
-        return launch_forward_chain(a, st, aux);
+    // (four pairs per step keep the slab kernels), when the items fill at
+    // least 4 waves of the chain kernel (2 CTAs per SM); a small structure's
+    // few items get twice the CTAs from the slab kernels (one per slab)
+    if (!water && q_slab >= 192 && !a.pairs4) {
+        int dev = 0, sms = 152;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            sms = 152;
+        if (a.n_items >= 8 * sms)
+            return launch_forward_chain(a, st, aux);
+    }
     const WidePlan p = wide_plan(a.n_q, water ? std::min(q_slab, 128) : q_slab);
     const bool split = aux && p.full > 0 && p.tail_len > 0;
     if (split) {
