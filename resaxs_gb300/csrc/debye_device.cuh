@@ -369,42 +369,6 @@ __device__ __forceinline__ void wide_pair4_body(const WideSeed &a, const WideSee
     }
 }
 
-// wide_pair4_body leaving the four chains' states in the seeds (see
-// wide_pair2_carry).
-template <int QS, int QH, bool SIGNED>
-__device__ __forceinline__ void wide_pair4_carry(WideSeed &a, WideSeed &b, WideSeed &c,
-                                                 WideSeed &e, float2 (&S)[QH])
-{
-    float2 sa = a.s, da = a.d, sb = b.s, db = b.d, sc = c.s, dc = c.d, se = e.s, de = e.d;
-    const float2 la = splat2(a.l), lb = splat2(b.l), lc = splat2(c.l), le = splat2(e.l);
-#pragma unroll
-    for (int m = 0; m < QS / 2; ++m) {
-        if (SIGNED && (m & 1))
-            S[m] = __ffma2_rn(splat2(a.sg), sa,
-                              __ffma2_rn(splat2(b.sg), sb,
-                                         __ffma2_rn(splat2(c.sg), sc,
-                                                    __ffma2_rn(splat2(e.sg), se, S[m]))));
-        else
-            S[m] = __fadd2_rn(S[m], __fadd2_rn(__fadd2_rn(sa, sb), __fadd2_rn(sc, se)));
-        da = __ffma2_rn(la, sa, da);
-        db = __ffma2_rn(lb, sb, db);
-        dc = __ffma2_rn(lc, sc, dc);
-        de = __ffma2_rn(le, se, de);
-        sa = __fadd2_rn(sa, da);
-        sb = __fadd2_rn(sb, db);
-        sc = __fadd2_rn(sc, dc);
-        se = __fadd2_rn(se, de);
-    }
-    a.s = sa;
-    a.d = da;
-    b.s = sb;
-    b.d = db;
-    c.s = sc;
-    c.d = dc;
-    e.s = se;
-    e.d = de;
-}
-
 template <int QS, int QH>
 __device__ __forceinline__ void wide_pair4(const WideSeed &a, const WideSeed &b, const WideSeed &c,
                                            const WideSeed &e, float2 (&S)[QH])
@@ -1623,20 +1587,6 @@ __device__ __forceinline__ void adjoint_item(const DebyeArgs &a, int item_idx, i
 // owns q index 32 c + L of every slab), and resumes from it in the next slab.
 
 template <int QS, int QH, bool SIGNED>
-__device__ __forceinline__ void chain_steps4(WideSeed (&p)[4], float2 (&S)[QH])
-{
-    if constexpr (SIGNED) {
-        if (__any_sync(0xffffffffu, p[0].sg < 0.f || p[1].sg < 0.f || p[2].sg < 0.f ||
-                                        p[3].sg < 0.f))
-            wide_pair4_carry<QS, QH, true>(p[0], p[1], p[2], p[3], S);
-        else
-            wide_pair4_carry<QS, QH, false>(p[0], p[1], p[2], p[3], S);
-    } else {
-        wide_pair4_carry<QS, QH, false>(p[0], p[1], p[2], p[3], S);
-    }
-}
-
-template <int QS, int QH, bool SIGNED>
 __device__ __forceinline__ void chain_steps(WideSeed &p1, WideSeed &p2, float2 (&S)[QH])
 {
     if constexpr (SIGNED) {
@@ -1655,7 +1605,7 @@ __device__ __forceinline__ void chain_steps(WideSeed &p1, WideSeed &p2, float2 (
 // rounded up to 32 (the accumulator stride); dsm: chain_smem_bytes(q_slots)
 // of dynamic shared memory.  Called once per CTA by forward_chain_kernel and
 // repeatedly by the persistent batch kernel (hence the leading barrier).
-template <int QT, bool SIGNED, int IL = kChainIL>
+template <int QT, bool SIGNED>
 __device__ __forceinline__ void forward_chain_item(const DebyeArgs &a, int item_idx, int k0,
                                                    int chain_q, int n_main, int q_slots,
                                                    unsigned char *dsm)
@@ -1700,49 +1650,40 @@ __device__ __forceinline__ void forward_chain_item(const DebyeArgs &a, int item_
 #pragma unroll
                 for (int m = 0; m < QH; ++m)
                     S[m] = make_float2(0.f, 0.f);
-                for (int jp = 0; jp < np; jp += IL) {
+                for (int jp = 0; jp < np; jp += 2) {
                     const int j = sub + jp;
-                    WideSeed p[IL];
+                    WideSeed p1, p2;
                     float2 *sd = st_sd + (size_t)jp * 2 * kBlockAtoms + tid;
                     float *sl = st_l + (size_t)jp * kBlockAtoms + tid;
                     if (first) {
-#pragma unroll
-                        for (int u = 0; u < IL; ++u) {
-                            float r, ri, dx, dy, dz;
-                            pair_r(pi, s_pos[min(j + u, kBlockAtoms - 1)], r, ri, dx, dy, dz);
-                            const bool use = valid_i && jp + u < np && (!diag || j + u > tid);
-                            p[u] = wide_seed(q0, dq, r, use ? ri : 0.f, small_th);
-                        }
+                        float r1, ri1, r2, ri2, dx, dy, dz;
+                        pair_r(pi, s_pos[j], r1, ri1, dx, dy, dz);
+                        pair_r(pi, s_pos[min(j + 1, kBlockAtoms - 1)], r2, ri2, dx, dy, dz);
+                        const bool u1 = valid_i && (!diag || j > tid);
+                        const bool u2 = valid_i && jp + 1 < np && (!diag || j + 1 > tid);
+                        p1 = wide_seed(q0, dq, r1, u1 ? ri1 : 0.f, small_th);
+                        p2 = wide_seed(q0, dq, r2, u2 ? ri2 : 0.f, small_th);
                     } else {
-#pragma unroll
-                        for (int u = 0; u < IL; ++u) {
-                            p[u].s = sd[2 * u * kBlockAtoms];
-                            p[u].d = sd[(2 * u + 1) * kBlockAtoms];
-                            unpack_lam_sign(sl[u * kBlockAtoms], p[u].l, p[u].sg);
-                        }
+                        p1.s = sd[0];
+                        p1.d = sd[kBlockAtoms];
+                        p2.s = sd[2 * kBlockAtoms];
+                        p2.d = sd[3 * kBlockAtoms];
+                        unpack_lam_sign(sl[0], p1.l, p1.sg);
+                        unpack_lam_sign(sl[kBlockAtoms], p2.l, p2.sg);
                     }
-                    if constexpr (IL == 4) {
-                        if (tail) {
-                            if constexpr (QT > 0)
-                                chain_steps4<QT, QH, SIGNED>(p, S);
-                        } else {
-                            chain_steps4<QM, QH, SIGNED>(p, S);
-                        }
+                    if (tail) {
+                        if constexpr (QT > 0)
+                            chain_steps<QT, QH, SIGNED>(p1, p2, S);
                     } else {
-                        if (tail) {
-                            if constexpr (QT > 0)
-                                chain_steps<QT, QH, SIGNED>(p[0], p[1], S);
-                        } else {
-                            chain_steps<QM, QH, SIGNED>(p[0], p[1], S);
-                        }
+                        chain_steps<QM, QH, SIGNED>(p1, p2, S);
                     }
                     if (!last) {
-#pragma unroll
-                        for (int u = 0; u < IL; ++u) {
-                            sd[2 * u * kBlockAtoms] = p[u].s;
-                            sd[(2 * u + 1) * kBlockAtoms] = p[u].d;
-                            sl[u * kBlockAtoms] = pack_lam_sign(p[u].l, p[u].sg);
-                        }
+                        sd[0] = p1.s;
+                        sd[kBlockAtoms] = p1.d;
+                        sd[2 * kBlockAtoms] = p2.s;
+                        sd[3 * kBlockAtoms] = p2.d;
+                        sl[0] = pack_lam_sign(p1.l, p1.sg);
+                        sl[kBlockAtoms] = pack_lam_sign(p2.l, p2.sg);
                     }
                 }
                 // the slab's sums of this sub-tile into the lane accumulators

@@ -136,7 +136,6 @@ cudaError_t launch_forward(const DebyeArgs &a, int q_slab, bool uniform, bool wa
 constexpr int kChainMain = 192;
 constexpr int kChainMaxMain = 2;
 constexpr int kChainPairs = 32;
-constexpr int kChainIL = 2; // pair chains a thread steps together
 // dynamic shared memory of a chain CTA: the states, then the per-warp FP64
 // lane accumulators of q_slots q
 __host__ __device__ constexpr size_t chain_state_bytes()
