@@ -126,7 +126,9 @@ __global__ void __launch_bounds__(256) batch_assemble_kernel(const BatchAssemble
     const int2 rg = a.item_range[m];
     const double *row = a.partial + (size_t)k * a.n_items;
     double s = 0.0;
-    for (int x = rg.x + threadIdx.x; x < rg.y; x += blockDim.x)
+    // at q = 0 the cross sums are not used (the row may not be written)
+    const int end = a.q[k] != 0.f ? rg.y : rg.x;
+    for (int x = rg.x + threadIdx.x; x < end; x += blockDim.x)
         s += row[x];
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1)
@@ -363,7 +365,7 @@ cudaError_t launch_batch_forward_chain(const DebyeArgs &a, const int *work_order
     if (p.rest_main == 0 && p.rest_tail <= 128) {
 #define RSX_BT(QS)                                                                         \
     return wide_batch_launch<QS>(a, work_order, n_work_items, 1, p.rest_k0, counters + 1, sms, st)
-        switch (p.rest_tail / 16) {
+        switch ((p.rest_tail + 15) / 16) { // a tail of 8 runs as 16
         case 1: RSX_BT(16);
         case 2: RSX_BT(32);
         case 3: RSX_BT(48);
@@ -378,6 +380,8 @@ cudaError_t launch_batch_forward_chain(const DebyeArgs &a, const int *work_order
 #define RSX_BC(QT)                                                                         \
     return batch_chain_launch<QT>(a, work_order, n_work_items, 1, p.rest_k0, p.rest_main,   \
                                   counters + 1, sms, st)
+    if (p.rest_tail == 8)
+        RSX_BC(8);
     switch (p.rest_tail / 16) {
     case 0: RSX_BC(0);
     case 1: RSX_BC(16);

@@ -46,6 +46,8 @@ static cudaError_t chain_launch(const DebyeArgs &a, int k_chain0, int n_chains, 
 static cudaError_t chain_launch_tail(const DebyeArgs &a, int k_chain0, int n_chains, int n_main,
                                      int tail_w, cudaStream_t st)
 {
+    if (tail_w == 8)
+        return chain_launch<8>(a, k_chain0, n_chains, n_main, st);
     switch (tail_w / 16) {
     case 0: return chain_launch<0>(a, k_chain0, n_chains, n_main, st);
     case 1: return chain_launch<16>(a, k_chain0, n_chains, n_main, st);
@@ -72,7 +74,10 @@ ChainPlan chain_plan(int n_q)
     const int rest = n_q - p.full * span;
     p.rest_k0 = p.full * span;
     p.rest_main = rest / kChainMain;
-    p.rest_tail = (rest - p.rest_main * kChainMain + 15) / 16 * 16;
+    // the tail in steps of 16 q, or 8 for a remainder of 1..8 q (n_q = 201
+    // from q = 0: the 200 q past q = 0 make one chain of 192 + 8)
+    const int left = rest - p.rest_main * kChainMain;
+    p.rest_tail = left > 0 && left <= 8 ? 8 : (left + 15) / 16 * 16;
     if (p.rest_tail == kChainMain) { // a rest of 177..191 q: one more main slab
         ++p.rest_main;
         p.rest_tail = 0;
@@ -81,9 +86,10 @@ ChainPlan chain_plan(int n_q)
     return p;
 }
 
-// Chains of two 192-q slabs from q 0, then one chain over the rest (its
-// main slabs and a tail rounded up to 16 q); with both, the rest chain runs
-// on the aux stream beside the full ones.
+// Chains of two 192-q slabs from q row 0 of `a` (row 1 of the grid for a
+// past_q0 view), then one chain over the rest (its main slabs and a tail of
+// chain_plan's width); with both, the rest chain runs on the aux stream
+// beside the full ones.
 cudaError_t launch_forward_chain(const DebyeArgs &a, cudaStream_t st, const AuxStream *aux)
 {
     if (a.n_items == 0)
@@ -108,7 +114,7 @@ cudaError_t launch_forward_chain(const DebyeArgs &a, cudaStream_t st, const AuxS
     // sub-tile reductions for nothing when no slab follows)
     auto rest = [&](cudaStream_t s) {
         return p.rest_main == 0 && p.rest_tail <= 128
-                   ? launch_forward_slab(a, p.rest_k0, p.rest_tail, s)
+                   ? launch_forward_slab(a, p.rest_k0, std::max(16, p.rest_tail), s)
                    : chain_launch_tail(a, p.rest_k0, 1, p.rest_main, p.rest_tail, s);
     };
     if (!split)

@@ -78,7 +78,9 @@ __global__ void __launch_bounds__(256) assemble_kernel(const AssembleArgs a)
     }
     double s = 0.0;
     const double *row = a.partial + (size_t)k * a.n_parts;
-    for (int x = threadIdx.x; x < a.n_parts; x += blockDim.x)
+    // at q = 0 the cross sums are not used (the row may not be written)
+    const int n_read = a.q[k] != 0.f ? a.n_parts : 0;
+    for (int x = threadIdx.x; x < n_read; x += blockDim.x)
         s += row[x];
 #pragma unroll
     for (int m = 16; m >= 1; m >>= 1)
@@ -260,7 +262,7 @@ template <int Q1, int Q2, bool SMALL>
 __global__ void __launch_bounds__(kBlockAtoms, 3) delta_chain_kernel(const DeltaArgs a,
                                                                     int k_base)
 {
-    static_assert(Q1 % 16 == 0 && Q2 % 16 == 0 && Q1 <= 112 && Q2 <= 112, "chain slabs");
+    static_assert(Q1 % 16 == 0 && Q2 % 8 == 0 && Q1 <= 112 && Q2 <= 112, "chain slabs");
     constexpr int QP1 = WideSlab<Q1>::QP, NR1 = WideSlab<Q1>::NR;
     constexpr int QP2 = Q2 > 0 ? WideSlab<Q2>::QP : 0, NR2 = QP2 / 32;
     constexpr int T = kDeltaTile;
@@ -592,6 +594,8 @@ WidePlan wide_plan(int n_q, int q_slab)
 static cudaError_t launch_forward_wide(const DebyeArgs &a, int q_slab, bool water, cudaStream_t st,
                                        const AuxStream *aux)
 {
+    if (a.q0_free && a.n_q > 1)
+        return launch_forward_wide(past_q0(a, a.n_items), q_slab, water, st, aux);
     // q_slab 192: chains of 192-q slabs with one seed per pair and chain
     // (four pairs per step keep the slab kernels), when the items fill at
     // least 4 waves of the chain kernel (2 CTAs per SM); a small structure's
@@ -705,9 +709,30 @@ int delta_groups(const DeltaArgs &a)
     return std::max(1, std::min(std::min(kDeltaGroups, a.n_mtiles), a.max_groups));
 }
 
-// One chain over the last `width` q (a multiple of 16, at most 224) from k0.
+// One chain over the last `width` q from k0: one slab of 16..112 q (a
+// multiple of 16), or 112 q and a second slab of 8..112 q (a multiple of 8).
 static cudaError_t delta_chain_rest(const DeltaArgs &a, int k0, int width, cudaStream_t st)
 {
+    if (width > 112) {
+        switch ((width - 112) / 8) {
+        case 1: return delta_chain_launch<112, 8>(a, k0, 1, st);
+        case 2: return delta_chain_launch<112, 16>(a, k0, 1, st);
+        case 3: return delta_chain_launch<112, 24>(a, k0, 1, st);
+        case 4: return delta_chain_launch<112, 32>(a, k0, 1, st);
+        case 5: return delta_chain_launch<112, 40>(a, k0, 1, st);
+        case 6: return delta_chain_launch<112, 48>(a, k0, 1, st);
+        case 7: return delta_chain_launch<112, 56>(a, k0, 1, st);
+        case 8: return delta_chain_launch<112, 64>(a, k0, 1, st);
+        case 9: return delta_chain_launch<112, 72>(a, k0, 1, st);
+        case 10: return delta_chain_launch<112, 80>(a, k0, 1, st);
+        case 11: return delta_chain_launch<112, 88>(a, k0, 1, st);
+        case 12: return delta_chain_launch<112, 96>(a, k0, 1, st);
+        case 13: return delta_chain_launch<112, 104>(a, k0, 1, st);
+        case 14: return delta_chain_launch<112, 112>(a, k0, 1, st);
+        default:
+            return cudaErrorInvalidValue;
+        }
+    }
     switch (width / 16) {
     case 1: return delta_chain_launch<16, 0>(a, k0, 1, st);
     case 2: return delta_chain_launch<32, 0>(a, k0, 1, st);
@@ -716,28 +741,23 @@ static cudaError_t delta_chain_rest(const DeltaArgs &a, int k0, int width, cudaS
     case 5: return delta_chain_launch<80, 0>(a, k0, 1, st);
     case 6: return delta_chain_launch<96, 0>(a, k0, 1, st);
     case 7: return delta_chain_launch<112, 0>(a, k0, 1, st);
-    case 8: return delta_chain_launch<112, 16>(a, k0, 1, st);
-    case 9: return delta_chain_launch<112, 32>(a, k0, 1, st);
-    case 10: return delta_chain_launch<112, 48>(a, k0, 1, st);
-    case 11: return delta_chain_launch<112, 64>(a, k0, 1, st);
-    case 12: return delta_chain_launch<112, 80>(a, k0, 1, st);
-    case 13: return delta_chain_launch<112, 96>(a, k0, 1, st);
-    case 14: return delta_chain_launch<112, 112>(a, k0, 1, st);
     default:
         return cudaErrorInvalidValue;
     }
 }
 
 // Uniform grids: chains of 224 q (two 112-q slabs, one seed per pair chain)
-// from q 0, then one chain over the rest rounded up to 16 q (n_q = 201: a
-// single 112 + 96 chain, one launch).  With full chains and a rest, the rest
+// from q row 0 of `a` (row 1 of the grid for a past_q0 view), then one chain
+// over the rest: up to 112 q rounded up to 16, past that 112 q and the
+// remainder rounded up to 8 (n_q = 201 from q = 0: the 200 q past q = 0 as a
+// single 112 + 88 chain, one launch).  With full chains and a rest, the rest
 // goes to the aux stream when there is one, so that its CTAs fill the last
 // wave of the main launch.
 static cudaError_t launch_delta_wide(const DeltaArgs &a, cudaStream_t st, const AuxStream *aux)
 {
     constexpr int kSpan = 224;
     const int full = a.n_q / kSpan, rest = a.n_q - full * kSpan;
-    const int rest_w = (rest + 15) / 16 * 16;
+    const int rest_w = rest <= 112 ? (rest + 15) / 16 * 16 : 112 + (rest - 112 + 7) / 8 * 8;
     const bool split = aux && full > 0 && rest > 0;
     if (split) {
         cudaError_t e = cudaEventRecord(aux->fork, st);
@@ -774,7 +794,8 @@ cudaError_t launch_delta(const DeltaArgs &a, int q_slab, bool uniform, cudaStrea
     if (a.n_blocks == 0 || a.k == 0)
         return cudaSuccess;
     if (uniform && q_slab >= 64)
-        return launch_delta_wide(a, st, aux);
+        return launch_delta_wide(a.q0_free && a.n_q > 1 ? past_q0(a, a.n_blocks * delta_groups(a)) : a,
+                                 st, aux);
     switch (q_slab > 32 ? 32 : q_slab) { // two chains per pair: at most 32 q per slab
     case 8:
         return delta_qs<8>(a, uniform, st);

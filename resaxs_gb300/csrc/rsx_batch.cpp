@@ -352,13 +352,17 @@ rsx_status enqueue_pass(rsx_batch *h, bool with_adjoint, int q_slab)
     const int n_items = (int)h->items.size();
     const bool water = has_water(h);
     const bool wide = h->uniform && q_slab >= 64;
+    // the wide launches of a grid from q = 0 (with q[1] == dq) run on q[1..]
+    // (past_q0)
+    const bool q0_free = wide && h->n_q > 1 && h->q[0] == 0.f && h->q[1] == h->dq;
+    const DebyeArgs aw = q0_free ? past_q0(a, n_items) : a;
     // q_slab 192 without water and with two pairs per step: chained slabs
     if (wide && !water && q_slab >= 192 && h->pairs_per_step != 4)
-        RSX_TRY_CUDA(launch_batch_forward_chain(a, h->d_order, n_items, h->d_counter, h->sms,
+        RSX_TRY_CUDA(launch_batch_forward_chain(aw, h->d_order, n_items, h->d_counter, h->sms,
                                                 h->st),
                      "batch forward");
     else if (wide)
-        RSX_TRY_CUDA(launch_batch_forward_wide(a, h->d_order, n_items, q_slab, h->d_counter,
+        RSX_TRY_CUDA(launch_batch_forward_wide(aw, h->d_order, n_items, q_slab, h->d_counter,
                                                h->sms, h->st, water),
                      "batch forward");
     const int slab = water_slab(h, q_slab);

@@ -398,6 +398,14 @@ int small_theta(const rsx_debye *h)
     return theta_level(true, (double)h->dq, std::sqrt(d2));
 }
 
+// A uniform grid that starts at q = 0 with q[1] == dq: the wide launches
+// skip that q (past_q0), and their first seeds take sin/cos(q[1] r) from the
+// step's sin/cos(dq r).
+bool q0_free(const rsx_debye *h)
+{
+    return h->uniform && h->n_q > 1 && h->q[0] == 0.f && h->q[1] == h->dq;
+}
+
 DebyeArgs debye_args(rsx_debye *h)
 {
     DebyeArgs a{};
@@ -414,6 +422,7 @@ DebyeArgs debye_args(rsx_debye *h)
     a.n_items = (int)h->L.items.size();
     a.dq = h->dq;
     a.small_theta = small_theta(h);
+    a.q0_free = q0_free(h) ? 1 : 0;
     a.pairs4 = h->pairs_per_step == 4 ? 1 : 0;
     a.water_weight = h->water_weight;
     a.water_index = h->water_index;
@@ -717,6 +726,7 @@ rsx_status delta_update(rsx_debye *h, const rsx_body *moved, const unsigned *idx
     a.n_mtiles = (int)tiles.size();
     a.max_groups = kDeltaGroups;
     a.dq = h->dq;
+    a.q0_free = q0_free(h) ? 1 : 0;
     // one partial row per static block and moved-list group
     RSX_TRY(ensure(&h->d_partial, h->partial_cap,
                    (size_t)delta_parts(a, slab_for(h), h->uniform) * h->n_q, "partial sums"));

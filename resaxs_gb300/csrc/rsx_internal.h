@@ -52,6 +52,7 @@ struct DebyeArgs {
     int pairs4;              // 1: the wide main slabs step 4 pairs at a time (else 2)
     float water_weight;      // w (water path)
     int water_index;         // column of the water factor
+    int q0_free;             // host side: q[0] == 0 on a uniform grid (see past_q0)
     // adjoint
     const float *lambda;     // [n_q] dL/dI(q)
     double *grad;            // [n][3] sorted-order FP64 gradient accumulators
@@ -104,10 +105,29 @@ struct DeltaArgs {
     int max_groups;          // cap on the moved-list groups (partial holds n_blocks * groups rows)
     float dq;
     int small_theta;         // theta_level() of the bodies before and after the move
+    int q0_free;             // host side: q[0] == 0 on a uniform grid (see past_q0)
 };
 
 constexpr int kDeltaGroups = 16; // moved-list groups of the wide delta kernel (at most)
 constexpr int kDeltaTile = 8;   // moved bodies per tile of the wide delta kernel
+
+// I(0) = (sum of the factors)^2 needs no pair sum: the assembly kernels take
+// it from the type counts, and an incremental step leaves it unchanged.  So
+// the wide uniform launches over a grid that starts at q = 0 run on q[1..]
+// only, through a view of the q, factor and partial arrays one row in (the
+// kernels index them by q row and never see the shift).  Partial row 0 is
+// then not written; every reader skips it at q = 0.
+template <class Args>
+inline Args past_q0(const Args &a, int parts)
+{
+    Args v = a;
+    v.q += 1;
+    v.ff += a.n_types;
+    v.partial += parts;
+    v.n_q -= 1;
+    v.q0_free = 0;
+    return v;
+}
 
 // launchers (debye_kernels.cu, adjoint_kernels.cu); all asynchronous on `st`
 // Slab plan of the wide uniform forward: `full` slabs of `main` q from q 0,
@@ -148,14 +168,15 @@ __host__ __device__ constexpr size_t chain_smem_bytes(int q_slots)
 }
 // Chained forward on uniform grids without water (chain_kernels.cu): `full`
 // chains of two 192-q slabs from q 0, then (rest) one chain from rest_k0 of
-// rest_main 192-q slabs and a rest_tail-q tail (a multiple of 16, 0 for
-// none); each pair is seeded once per chain.
+// rest_main 192-q slabs and a rest_tail-q tail (8, or a multiple of 16; 0
+// for none); each pair is seeded once per chain.
 struct ChainPlan {
     int full, rest_k0, rest_main, rest_tail;
     bool rest;
 };
 ChainPlan chain_plan(int n_q);
-// One wide slab of `width` q (16..128, a multiple of 16) from k0, no water.
+// One wide slab of `width` q (8..128: 16 or wider in steps of 16, a width of
+// 8 runs as 16) from k0, no water.
 cudaError_t launch_forward_slab(const DebyeArgs &a, int k0, int width, cudaStream_t st);
 cudaError_t launch_forward_chain(const DebyeArgs &a, cudaStream_t st, const AuxStream *aux);
 cudaError_t launch_assemble(const AssembleArgs &a, cudaStream_t st);

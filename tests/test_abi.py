@@ -134,8 +134,9 @@ def test_wide_slab_plan_covers_every_q(librsx):
 
 def test_chain_plan_covers_every_q(librsx):
     """The chain plan of the uniform forward: full chains of 384 q from q 0,
-    then one rest chain of up to two 192-q slabs and a tail of 16..176 q (a
-    multiple of 16) that covers [rest_k0, n_q) with less than 16 q to spare."""
+    then one rest chain of up to two 192-q slabs and a tail of 8 q (for a
+    remainder of 1..8 q) or of 16..176 q (a multiple of 16) that covers
+    [rest_k0, n_q) with less than 16 q to spare (less than 8 for a tail of 8)."""
     from resaxs_gb300 import _lib
     out = np.zeros(5, np.int32)
     for n_q in range(1, 2500):
@@ -145,8 +146,9 @@ def test_chain_plan_covers_every_q(librsx):
         assert rest == (k0 < n_q), (n_q, out)
         if rest:
             covered = 192 * main + tail
-            assert tail % 16 == 0 and 0 <= tail <= 176 and 0 <= main <= 2, (n_q, out)
-            assert n_q - k0 <= covered < n_q - k0 + 16, (n_q, out)
+            assert (tail == 8 or tail % 16 == 0) and 0 <= tail <= 176 and 0 <= main <= 2, (n_q, out)
+            assert n_q - k0 <= covered < n_q - k0 + (8 if tail == 8 else 16), (n_q, out)
+            assert (tail == 8) == (0 < (n_q - k0) % 192 <= 8), (n_q, out)
     assert librsx.rsx_debug_chain_plan(0, out) == _lib.RSX_INVALID_ARG
 
 

@@ -275,3 +275,19 @@ def test_batch_water_errors(ensemble):
         b.set_water(0.0, 1)
         _, chi2, _ = b.forward_chi2_backward(members)
         assert np.all(np.isfinite(chi2))
+
+
+@pytest.mark.parametrize("q_min,n_q", [(0.01, 201), (0.01, 200), (0.0, 193)])
+def test_batch_chain_grids(oracle_lib, ensemble, q_min, n_q):
+    """The chained batch pass on grids that do not start at q = 0 (every q
+    takes pair work: 201 q as 192 + 16, 200 q as 192 + 8) and on 193 q from
+    q = 0 (the 192 q past it: one 192-q slab, no tail)."""
+    from resaxs_gb300.batch import DebyeBatch
+    _, _, members = ensemble
+    q = W.q_grid(n_q, 0.5, q_min)
+    ff = W.exp_form_factors(q, W.Z5, np.random.default_rng(n_q).uniform(0.5, 2.0, 5))
+    with DebyeBatch(q, ff, [len(m) for m in members], q_slab=192, pairs_per_step=2) as b:
+        out = b.forward(members)
+    for m, body in enumerate(members):
+        if len(body) > 0:
+            assert rel(out[m], oracle_lib.debye_f64(q, body, ff)) < TOL, m

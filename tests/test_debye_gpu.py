@@ -366,27 +366,32 @@ def test_autotuned_slab(saxs, oracle_lib):
     assert rel(again, out64) < 1e-12
 
 
-@pytest.mark.parametrize("n_q,q_max,spread", [(190, 0.5, 1.0), (577, 0.5, 1.0), (700, 2.0, 8.0),
-                                              (1200, 0.6, 1.0)])
-def test_chained_forward_plans(saxs, oracle_lib, n_q, q_max, spread):
+@pytest.mark.parametrize("n_q,q_max,spread,q_min", [(190, 0.5, 1.0, 0.0), (577, 0.5, 1.0, 0.0),
+                                                    (700, 2.0, 8.0, 0.0), (1200, 0.6, 1.0, 0.0),
+                                                    (201, 0.5, 1.0, 0.0), (201, 0.5, 1.0, 0.01),
+                                                    (200, 0.5, 8.0, 0.01), (578, 0.5, 1.0, 0.01)])
+def test_chained_forward_plans(saxs, oracle_lib, n_q, q_max, spread, q_min):
     """The chained forward (one seed per pair and chain of up to two 192-q
     slabs; it runs when the work items fill 4 waves, >= 8 per SM: 9,000
-    bodies give ~2,700): 190 q as one 192-q slab, a full 384-q chain and a
-    192 + 16 rest chain (577 q), a spread structure whose far pairs take the
-    signed steps (700 q to 2.0/A: 384, then 192 + 128), and three full chains
-    with a 48-q rest slab on the second stream (1,200 q); FP64 oracle on the
-    chains' first, boundary and last q and every 23rd."""
+    bodies give ~2,700).  A grid from q = 0 runs on the q past it: 190 q as
+    one 192-q slab, a full 384-q chain and a 192-q rest chain (577 q), a
+    spread structure whose far pairs take the signed steps (700 q to 2.0/A:
+    384, then 192 + 128), three full chains with a 48-q rest slab on the
+    second stream (1,200 q), one 192 + 8 chain (201 q).  From q = 0.01: 192 +
+    16 (201 q), 192 + 8 with signed steps (200 q), 384 and 192 + 8 (578 q).
+    FP64 oracle on the chains' first, boundary and last q and every 23rd."""
     w = W.make_config(2, seed=21, n_override=9000)
     bodies = w.bodies.copy()
     bodies[:, :3] *= np.float32(spread)
     rng = np.random.default_rng(n_q)
-    q = W.q_grid(n_q, q_max)
+    q = W.q_grid(n_q, q_max, q_min)
     ff = W.exp_form_factors(q, W.Z5, rng.uniform(0.5, 2.0, 5))
     with saxs.Debye(q, ff, len(bodies)) as d:
         d.calc(bodies)
         out64 = d.curve_f64()
         assert d.config()["n_items"] >= 8 * 152
-    edges = [k for c in range(0, n_q, 384) for k in (c, c + 191, c + 192, c + 383)]
+    edges = [k + d for c in range(0, n_q, 384) for k in (c, c + 191, c + 192, c + 383)
+             for d in (0, 1)]
     sel = np.array(sorted({k for k in edges + list(range(0, n_q, 23)) + [n_q - 1] if k < n_q}))
     ref = oracle_lib.debye_f64(q[sel], bodies, ff[sel])
     assert rel(out64[sel], ref) < TOL, rel(out64[sel], ref)

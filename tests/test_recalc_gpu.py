@@ -21,16 +21,20 @@ def S():
     return saxs
 
 
-@pytest.mark.parametrize("q_slab,n_q", [(0, 201), (32, 201), (16, 201), (128, 101),
-                                         (128, 256), (64, 150), (64, 40), (0, 113),
-                                         (0, 384), (0, 450), (0, 97)])
-def test_recalc_indices_matches_full_recompute(S, oracle_lib, q_slab, n_q):
+@pytest.mark.parametrize("q_slab,n_q,q_min", [(0, 201, 0.0), (32, 201, 0.0), (16, 201, 0.0),
+                                               (128, 101, 0.0), (128, 256, 0.0), (64, 150, 0.0),
+                                               (64, 40, 0.0), (0, 113, 0.0), (0, 384, 0.0),
+                                               (0, 450, 0.0), (0, 97, 0.0), (0, 201, 0.01),
+                                               (0, 200, 0.01)])
+def test_recalc_indices_matches_full_recompute(S, oracle_lib, q_slab, n_q, q_min):
     """Config-2 style moves (k random bodies, Gaussian sigma 0.5 A) at a size the
     oracle recomputes quickly; every step is checked.  The slab sizes and q
-    counts cover the wide delta slabs (main slabs of 64 to 128 q, remainder
-    slabs up to 128 q wide) and the 16 / 32-q kernel."""
+    counts cover the wide delta chains (a grid from q = 0 runs on the q past
+    it: 201 q as 112 + 88, 384 q as 224 and 112 + 48, 450 q as two 224-q
+    chains and a 16-q slab; from q = 0.01, 201 q as 112 + 96 and 200 q as
+    112 + 88) and the 16 / 32-q kernel."""
     w = W.make_config(2, seed=21, n_override=1200)
-    q = W.q_grid(n_q, 0.5)
+    q = W.q_grid(n_q, 0.5, q_min)
     ff = W.exp_form_factors(q, W.Z5, np.random.default_rng(n_q).uniform(0.5, 2.0, 5))
     rng = np.random.default_rng(1)
     bodies = w.bodies.copy()
