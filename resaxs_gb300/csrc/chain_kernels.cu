@@ -20,8 +20,10 @@ __global__ void __launch_bounds__(kBlockAtoms, 2)
     forward_chain_kernel(const DebyeArgs a, int k_chain0, int chain_q, int n_main, int q_slots)
 {
     extern __shared__ __align__(16) unsigned char dsm[];
-    forward_chain_item<QT, SIGNED>(a, blockIdx.x, k_chain0 + blockIdx.y * chain_q, chain_q,
-                                   n_main, q_slots, dsm);
+    // chains with a tail slab take the seeds of wide_seed_x0_first (measured
+    // faster there; the same values)
+    forward_chain_item<QT, SIGNED, (QT > 0)>(a, blockIdx.x, k_chain0 + blockIdx.y * chain_q,
+                                             chain_q, n_main, q_slots, dsm);
 }
 
 template <int QT>
