@@ -1,9 +1,12 @@
 """Precision at the full 200,000-body configuration: FP32 kernel with FP64
 cross-block reduction against the FP64 oracle on 15 of the 512 q values (the
-FP32 grid values themselves), chosen along the chain of 192 + 192 + 128 q the
-forward runs at 512 q: its start (the seed), both slab boundaries (where the
-recurrence resumes from shared memory) and its far end (288 paired steps
-after the seed).  Bound: 1e-5 relative per q."""
+FP32 grid values themselves).  The forward runs the q past q = 0 as a chain
+over q 1..384 (two 192-q slabs on one seed per pair, the second resuming
+from shared memory) and a 128-q slab over q 385..511; the samples take q = 0
+(from the type counts), the first slab and its end (191, 192), the second
+slab from 8 q after the resume, the chain's far end (383, 384: 192 paired
+steps after the seed) and the reseeded slab up to q = 1.0.  Bound: 1e-5
+relative per q."""
 import numpy as np
 import pytest
 
