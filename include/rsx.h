@@ -83,9 +83,11 @@ int rsx_debug_theta_level(int uniform, double dq, double diag);
 rsx_status rsx_debug_wide_plan(int n_q, int q_slab, int *out);
 
 /* Host-only view of the chain plan of the uniform forward (q_slab 192, no
- * water): out[0..4] = chains of two 192-q slabs from q 0, first q of the
- * rest chain, its 192-q slabs, its tail slab's width (a multiple of 16, 0 for
- * none), 1 if there is a rest chain. */
+ * water) over n_q q: out[0..4] = chains of two 192-q slabs from the first q,
+ * first q of the rest chain, its 192-q slabs, its tail slab's width (8 for a
+ * remainder of 1..8 q, else a multiple of 16; 0 for none), 1 if there is a
+ * rest chain.  A grid that starts at q = 0 is planned over the n_q - 1 q past
+ * it (I(0) needs no pair sums). */
 rsx_status rsx_debug_chain_plan(int n_q, int *out);
 
 /* Host-only check of the shard split used by rsx_debye_calc_shard: item
@@ -94,10 +96,12 @@ rsx_status rsx_debug_chain_plan(int n_q, int *out);
 rsx_status rsx_debug_shard_items(const rsx_body *bodies, int n_bodies, int n_factors,
                                  int max_items, int n_shards, int *bounds, double *pairs);
 
-/* Host-only view of the autotuning cache (the q-slab winners, loaded once from
- * the file named by RSX_AUTOTUNE_CACHE when it is set): 1 and *q_slab when
- * `key` has an entry, else 0.  Lines of the file whose value is not a q-slab
- * size rsx_debye_create accepts (8, 16, 32, 64, 128) are ignored. */
+/* Host-only view of the autotuning cache (the tile-shape winners, loaded once
+ * from the file named by RSX_AUTOTUNE_CACHE when it is set): 1 and *q_slab
+ * when `key` has an entry, else 0.  The value is q_slab + 1000 when the wide
+ * main slabs step four pairs at a time; lines of the file whose value is not
+ * a shape librsx has kernels for (8, 16, 32, 64, 128, 192, 1128, 1192) are
+ * ignored. */
 int rsx_debug_autotune_lookup(const char *key, int *q_slab);
 
 /* Measures the sustained FP32 FMA rate of `device` (-1 = current) with a
