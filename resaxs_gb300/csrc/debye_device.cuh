@@ -262,7 +262,8 @@ __device__ __forceinline__ WideSeed wide_seed(float q0, float dq, float r, float
         sincos_rr2(th, th_lo, st, ct);
     // x0 = q0 r: 0 at q0 = 0; at q0 = dq (the first q of a past_q0 view) the
     // step's own sin/cos, sincos_prod(dq, r) bit for bit.  (This form, one
-    // branch with selects, measured fastest of three on the chained launches.)
+    // branch with selects, measured fastest of three on the two-slab chains
+    // and the batched chains; see wide_seed_x0_first.)
     if (q0 != 0.f && q0 != dq) {
         sincos_prod(q0, r, s0, c0);
     } else {

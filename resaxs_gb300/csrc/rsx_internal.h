@@ -52,7 +52,7 @@ struct DebyeArgs {
     int pairs4;              // 1: the wide main slabs step 4 pairs at a time (else 2)
     float water_weight;      // w (water path)
     int water_index;         // column of the water factor
-    int q0_free;             // host side: q[0] == 0 on a uniform grid (see past_q0)
+    int q0_free;             // host side: a uniform grid with q[0] == 0, q[1] == dq (past_q0)
     // adjoint
     const float *lambda;     // [n_q] dL/dI(q)
     double *grad;            // [n][3] sorted-order FP64 gradient accumulators
@@ -105,7 +105,7 @@ struct DeltaArgs {
     int max_groups;          // cap on the moved-list groups (partial holds n_blocks * groups rows)
     float dq;
     int small_theta;         // theta_level() of the bodies before and after the move
-    int q0_free;             // host side: q[0] == 0 on a uniform grid (see past_q0)
+    int q0_free;             // host side: a uniform grid with q[0] == 0, q[1] == dq (past_q0)
 };
 
 constexpr int kDeltaGroups = 16; // moved-list groups of the wide delta kernel (at most)
